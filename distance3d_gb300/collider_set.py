@@ -1,0 +1,138 @@
+"""Host-side packed collider set: the flat format every C-ABI entry point and
+the device store are built from.
+
+One row per collider:
+
+* ``types``       int32 (n,)     SPHERE=0 CAPSULE=1 BOX=2 CYLINDER=3 ELLIPSOID=4 HULL=5
+* ``poses``       float64 (n,12) rotation R row-major (9 values) then translation t (3)
+* ``params``      float64 (n,4)  sphere (r) | capsule (r, h) | box (size xyz, full edge
+                                 lengths as in distance3d colliders.py:147-184) |
+                                 cylinder (r, L) | ellipsoid (radii xyz) | hull (unused)
+* ``hull_offset`` int64 (n,)     first row of the collider in ``vertices`` (-1: none)
+* ``hull_count``  int32 (n,)     number of hull vertices
+* ``vertices``    float64 (V,4)  world-space hull vertices, xyz plus a zero pad so a
+                                 vertex is 32 B (FP64) / 16 B (FP32) and loads as
+                                 aligned 128-bit words
+
+A sphere keeps its center in ``t`` (its rotation is unused, distance3d
+colliders.py:243-287); a ConvexHullVertices has the identity pose
+(colliders.py:143-144).  Boxes carry no vertices here: the device store derives
+their 8 vertices from pose and size (geometry.py:135-157).
+"""
+import numpy as np
+
+SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL = 0, 1, 2, 3, 4, 5
+TYPE_NAMES = ("Sphere", "Capsule", "Box", "Cylinder", "Ellipsoid", "ConvexHullVertices")
+
+
+class ColliderSet:
+    """Packed host arrays for a batch of colliders (see module docstring)."""
+
+    def __init__(self, types, poses, params, hull_offset, hull_count, vertices):
+        self.types = np.ascontiguousarray(types, dtype=np.int32)
+        n = len(self.types)
+        self.poses = np.ascontiguousarray(poses, dtype=np.float64).reshape(n, 12)
+        self.params = np.ascontiguousarray(params, dtype=np.float64).reshape(n, 4)
+        self.hull_offset = np.ascontiguousarray(hull_offset, dtype=np.int64)
+        self.hull_count = np.ascontiguousarray(hull_count, dtype=np.int32)
+        v = np.asarray(vertices, dtype=np.float64)
+        if v.ndim == 2 and v.shape[1] == 3:
+            v = np.concatenate([v, np.zeros((len(v), 1))], axis=1)
+        self.vertices = np.ascontiguousarray(v.reshape(-1, 4))
+        self.validate()
+
+    def __len__(self):
+        return len(self.types)
+
+    @property
+    def n_vertices(self):
+        return len(self.vertices)
+
+    def validate(self):
+        n = len(self.types)
+        for name in ("poses", "params", "hull_offset", "hull_count"):
+            if len(getattr(self, name)) != n:
+                raise ValueError(f"ColliderSet.{name} has {len(getattr(self, name))} rows, expected {n}")
+        if n and (self.types.min() < 0 or self.types.max() > HULL):
+            raise ValueError("ColliderSet.types holds an unknown collider type")
+        hulls = self.types == HULL
+        if np.any(self.hull_count[hulls] < 1):
+            raise ValueError("ConvexHullVertices needs at least one vertex")
+        if np.any(self.hull_offset[hulls] < 0) or np.any(
+                self.hull_offset[hulls] + self.hull_count[hulls] > len(self.vertices)):
+            raise ValueError("hull vertex range outside the vertex pool")
+        if len(self.vertices) + 8 * int(np.count_nonzero(self.types == BOX)) >= 2 ** 31:
+            raise ValueError("vertex pool larger than 2^31 rows")
+
+    @staticmethod
+    def concatenate(sets):
+        types = np.concatenate([s.types for s in sets])
+        poses = np.concatenate([s.poses for s in sets])
+        params = np.concatenate([s.params for s in sets])
+        counts = np.concatenate([s.hull_count for s in sets])
+        offs, base = [], 0
+        for s in sets:
+            o = s.hull_offset.copy()
+            o[o >= 0] += base
+            offs.append(o)
+            base += len(s.vertices)
+        verts = np.concatenate([s.vertices for s in sets]) if sets else np.zeros((0, 4))
+        return ColliderSet(types, poses, params, np.concatenate(offs), counts, verts)
+
+    @staticmethod
+    def from_colliders(colliders):
+        """Pack collider objects with distance3d's attribute names.
+
+        Accepts this package's colliders and distance3d's own (the class name,
+        searched along the MRO, selects the type; the attributes read are the
+        ones distance3d's constructors set, colliders.py:109-440).
+        """
+        n = len(colliders)
+        types = np.zeros(n, np.int32)
+        poses = np.zeros((n, 12))
+        params = np.zeros((n, 4))
+        offs = np.full(n, -1, np.int64)
+        counts = np.zeros(n, np.int32)
+        verts = []
+        nv = 0
+        for i, c in enumerate(colliders):
+            t = collider_type(c)
+            types[i] = t
+            if t == SPHERE:
+                pose = np.eye(4)
+                pose[:3, 3] = np.asarray(c.c, dtype=float)
+                params[i, 0] = float(c.radius)
+            elif t == CAPSULE:
+                pose = np.asarray(c.capsule2origin, dtype=float)
+                params[i, :2] = (float(c.radius), float(c.height))
+            elif t == BOX:
+                pose = np.asarray(c.box2origin, dtype=float)
+                params[i, :3] = np.asarray(c.size, dtype=float).reshape(-1)[:3] * np.ones(3)
+            elif t == CYLINDER:
+                pose = np.asarray(c.cylinder2origin, dtype=float)
+                params[i, :2] = (float(c.radius), float(c.length))
+            elif t == ELLIPSOID:
+                pose = np.asarray(c.ellipsoid2origin, dtype=float)
+                params[i, :3] = np.asarray(c.radii, dtype=float)
+            else:
+                pose = np.eye(4)
+                v = np.asarray(c.vertices, dtype=float).reshape(-1, 3)
+                offs[i] = nv
+                counts[i] = len(v)
+                verts.append(v)
+                nv += len(v)
+            poses[i, :9] = pose[:3, :3].reshape(-1)
+            poses[i, 9:] = pose[:3, 3]
+        v = np.concatenate(verts) if verts else np.zeros((0, 3))
+        return ColliderSet(types, poses, params, offs, counts, v)
+
+
+def collider_type(c):
+    """Type code of a collider object, from its class name along the MRO."""
+    for klass in type(c).__mro__:
+        name = klass.__name__
+        if name in TYPE_NAMES:
+            return TYPE_NAMES.index(name)
+    raise TypeError(
+        f"{type(c).__name__} is not supported on the GPU path (supported: "
+        + ", ".join(TYPE_NAMES) + ")")

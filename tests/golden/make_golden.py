@@ -1,0 +1,239 @@
+"""Generate the golden fixtures in this folder from the distance3d reference.
+
+Run from the repository root, in a container where the reference source tree
+is available (it is NOT needed at test time):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/distance3d
+
+The reference is imported with its JIT disabled -- the mode its own CI uses --
+through the inert stand-ins in ``_standins/`` (numba: ``njit`` returns the
+function unchanged; pytransform3d: only names imported at module load).
+NumPy 2 removed ``np.row_stack``; it is aliased to ``np.vstack`` for the
+reference's libccd module, which is imported but not used here.
+
+Inputs come from ``distance3d_gb300.workloads`` (seeded).  Outputs:
+
+* ``gjk_mixed6.npz``  -- 1,000 six-type pairs, centers in [-w,w]^3 with w
+  calibrated to ~30% intersecting pairs: reference ``gjk_distance_jolt``
+  (dist, closest points, simplex, number of valid simplex rows, iterations)
+  and ``gjk_intersection_jolt`` flags, plus every collider's ``aabb()``.
+* ``gjk_scb.npz``     -- 1,000 Sphere/Capsule/Box pairs, centers in [-1,1]^3.
+* ``epa_mixed6.npz``  -- reference ``epa.epa`` on the intersecting pairs of
+  gjk_mixed6 whose four simplex rows were all written by GJK, at the default
+  limits (64 faces; AssertionError -> face overflow) and at 256 faces / 128
+  loose edges.
+* ``aabb_tree.npz``   -- a 400-collider scene: reference AabbTree self overlap
+  (both orders, i == j dropped, reduced to i < j), brute force
+  ``all_aabbs_overlap``, BoundingVolumeHierarchy.aabb_overlapping_with_self on
+  the first 150 colliders, and AabbTree.overlaps_aabb for 20 query boxes.
+
+Simplex rows that GJK never wrote are NaN here (the reference leaves
+``np.empty`` memory there).
+"""
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def import_reference(ref_root):
+    sys.path[:0] = [os.path.join(HERE, "_standins"), ref_root, ROOT]
+    np.row_stack = np.vstack
+    import distance3d  # noqa: F401
+    from distance3d import gjk, epa, colliders, aabb_tree, broad_phase
+    return gjk, epa, colliders, aabb_tree, broad_phase
+
+
+def make_ref_colliders(colliders, cs):
+    out = []
+    for i in range(len(cs)):
+        t = int(cs.types[i])
+        pose = np.eye(4)
+        pose[:3, :3] = cs.poses[i, :9].reshape(3, 3)
+        pose[:3, 3] = cs.poses[i, 9:]
+        p = cs.params[i]
+        if t == 0:
+            out.append(colliders.Sphere(pose[:3, 3].copy(), float(p[0])))
+        elif t == 1:
+            out.append(colliders.Capsule(pose, float(p[0]), float(p[1])))
+        elif t == 2:
+            out.append(colliders.Box(pose, p[:3].copy()))
+        elif t == 3:
+            out.append(colliders.Cylinder(pose, float(p[0]), float(p[1])))
+        elif t == 4:
+            out.append(colliders.Ellipsoid(pose, p[:3].copy()))
+        else:
+            o, c = int(cs.hull_offset[i]), int(cs.hull_count[i])
+            out.append(colliders.ConvexHullVertices(np.ascontiguousarray(cs.vertices[o:o + c, :3])))
+    return out
+
+
+def ref_distance(gjk_mod, c1, c2, tolerance=1e-10, max_distance_squared=100000.0):
+    """The outer loop of gjk_distance_jolt (_gjk_jolt.py:189-221) around the
+    reference's own _distance_loop, exposing n_points and the iteration count."""
+    J = sys.modules["distance3d.gjk._gjk_jolt"]
+    Y = np.full((4, 3), np.nan)
+    P = np.full((4, 3), np.nan)
+    Q = np.full((4, 3), np.nan)
+    n_points = 0
+    tol2 = tolerance * tolerance
+    d = np.array([1.0, 0.0, 0.0])
+    v_len_sq = np.dot(d, d)
+    prev = J.MAX_FLOAT
+    it = 0
+    while True:
+        it += 1
+        p = c1.support_function(d)
+        q = c2.support_function(-d)
+        state, n_new, prev, v_len_sq = J._distance_loop(
+            p, q, Y, P, Q, n_points, tol2, prev, v_len_sq, d, max_distance_squared)
+        if state == J.GjkState.Unknown:
+            n_points = n_new
+            continue
+        if state == J.GjkState.Clipped:
+            return J.MAX_FLOAT, None, None, Y, -1, it
+        n_points = n_new
+        a, b = J.calculate_closest_points(Y, P, Q, n_points)
+        dist = np.sqrt(v_len_sq)
+        if dist < J.EPSILON:
+            a = b = 0.5 * (a + b)
+        return float(dist), a, b, Y, n_points, it
+
+
+def gjk_fixture(mods, cs, i1, i2):
+    gjk, epa, colliders, _, _ = mods
+    cols = make_ref_colliders(colliders, cs)
+    n = len(i1)
+    dist = np.empty(n)
+    cp1 = np.full((n, 3), np.nan)
+    cp2 = np.full((n, 3), np.nan)
+    simplex = np.full((n, 4, 3), np.nan)
+    n_simplex = np.empty(n, np.int8)
+    iters = np.empty(n, np.int32)
+    hit = np.empty(n, bool)
+    t0 = time.time()
+    for k in range(n):
+        c1, c2 = cols[i1[k]], cols[i2[k]]
+        d, a, b, Y, m, it = ref_distance(gjk, c1, c2)
+        d0, a0, b0, Y0 = gjk.gjk_distance_jolt(c1, c2)
+        assert d == d0
+        if a is not None:
+            assert np.array_equal(a, a0) and np.array_equal(b, b0)
+            assert np.array_equal(Y[:m], Y0[:m])
+            cp1[k], cp2[k] = a, b
+        dist[k] = d
+        simplex[k] = Y
+        n_simplex[k] = m
+        iters[k] = it
+        hit[k] = gjk.gjk_intersection_jolt(c1, c2)
+    dt = time.time() - t0
+    aabbs = np.stack([c.aabb() for c in cols])
+    print(f"  gjk: {n} pairs in {dt:.1f}s ({n / dt:.0f} pairs/s incl. intersection)")
+    return dict(types=cs.types, poses=cs.poses, params=cs.params, hull_offset=cs.hull_offset,
+                hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), i1=i1, i2=i2,
+                dist=dist, cp1=cp1, cp2=cp2, simplex=simplex, n_simplex=n_simplex,
+                iterations=iters, intersect=hit, aabbs=aabbs), cols
+
+
+def epa_fixture(mods, cols, gf):
+    _, epa, _, _, _ = mods
+    sel = np.flatnonzero((gf["dist"] == 0.0) & ~np.isnan(gf["simplex"]).any(axis=(1, 2)))
+    n = len(sel)
+    out = {"pair": sel.astype(np.int32)}
+    for tag, kw in (("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))):
+        mtv = np.full((n, 3), np.nan)
+        status = np.zeros(n, np.int8)   # 0 converged, 4 max_iter, 5 face overflow, 6 other error
+        nfaces = np.zeros(n, np.int32)
+        t0 = time.time()
+        for k, p in enumerate(sel):
+            c1, c2 = cols[gf["i1"][p]], cols[gf["i2"][p]]
+            try:
+                m, faces, ok = epa.epa(gf["simplex"][p].copy(), c1, c2, **kw)
+                mtv[k] = m
+                nfaces[k] = len(faces)
+                status[k] = 0 if ok else 4
+            except AssertionError:
+                status[k] = 5
+            except Exception:  # noqa: BLE001 - recorded as a distinct outcome
+                status[k] = 6
+        dt = time.time() - t0
+        print(f"  epa[{tag}]: {n} pairs in {dt:.1f}s; status counts {np.bincount(status, minlength=7)}")
+        out[f"mtv_{tag}"] = mtv
+        out[f"status_{tag}"] = status
+        out[f"n_faces_{tag}"] = nfaces
+    return out
+
+
+class _FakeTM:
+    def __init__(self):
+        self.T = {}
+
+    def add_transform(self, a, b, A2B):
+        self.T[(a, b)] = A2B
+
+    def get_transform(self, a, b):
+        return self.T[(a, b)]
+
+
+def tree_fixture(mods, cs, n_bvh=150, n_queries=20, seed=7):
+    _, _, colliders, aabb_tree, broad_phase = mods
+    cols = make_ref_colliders(colliders, cs)
+    aabbs = np.stack([c.aabb() for c in cols])
+    tree = aabb_tree.AabbTree()
+    tree.insert_aabbs(aabbs)
+    _, _, _, pairs = tree.overlaps_aabb_tree(tree)
+    tp = {(min(a, b), max(a, b)) for a, b in pairs if a != b}
+    tree_pairs = np.array(sorted(tp), dtype=np.int32).reshape(-1, 2)
+    _, _, brute = aabb_tree.all_aabbs_overlap(aabbs, aabbs)
+    bp = {(a, b) for a, b in brute if a < b}
+    assert bp == tp, "reference tree and brute force disagree"
+    # incremental BVH (broad_phase.py:129-142, 229-252)
+    bvh = broad_phase.BoundingVolumeHierarchy(_FakeTM(), "base")
+    for i in range(n_bvh):
+        bvh.add_collider(i, cols[i])
+    dp = bvh.aabb_overlapping_with_self()
+    bvh_pairs = np.array(sorted((a[0], b[0]) for a, b in dp), dtype=np.int32).reshape(-1, 2)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lo = rng.uniform(-3.5, 3.0, size=(n_queries, 3))
+    hi = lo + rng.uniform(0.05, 1.5, size=(n_queries, 3))
+    queries = np.stack([lo, hi], axis=2)
+    q_idx, q_ptr = [], [0]
+    for q in queries:
+        _, ov = tree.overlaps_aabb(q)
+        q_idx.extend(sorted(int(x) for x in ov))
+        q_ptr.append(len(q_idx))
+    print(f"  tree: {len(tree_pairs)} pairs (i<j), bvh[{n_bvh}]: {len(bvh_pairs)} ordered pairs")
+    return dict(types=cs.types, poses=cs.poses, params=cs.params, hull_offset=cs.hull_offset,
+                hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), aabbs=aabbs,
+                tree_pairs=tree_pairs, bvh_n=np.int32(n_bvh), bvh_pairs=bvh_pairs,
+                queries=queries, query_idx=np.array(q_idx, np.int32), query_ptr=np.array(q_ptr, np.int64))
+
+
+def main(ref_root):
+    mods = import_reference(ref_root)
+    from distance3d_gb300 import workloads
+    print("mixed six-type pairs (calibrated ~30% intersecting)")
+    cs, i1, i2 = workloads.pairs_mixed_six(1000, seed=1234, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    gf, cols = gjk_fixture(mods, cs, i1, i2)
+    print(f"  intersecting fraction {np.mean(gf['dist'] == 0.0):.3f}")
+    np.savez_compressed(os.path.join(HERE, "gjk_mixed6.npz"), **gf)
+    ef = epa_fixture(mods, cols, gf)
+    np.savez_compressed(os.path.join(HERE, "epa_mixed6.npz"), **ef)
+    print("sphere/capsule/box pairs")
+    cs, i1, i2 = workloads.pairs_sphere_capsule_box(1000, seed=99)
+    gf2, _ = gjk_fixture(mods, cs, i1, i2)
+    print(f"  intersecting fraction {np.mean(gf2['dist'] == 0.0):.3f}")
+    np.savez_compressed(os.path.join(HERE, "gjk_scb.npz"), **gf2)
+    print("aabb tree scene")
+    scene = workloads.scene_mixed_six(400, seed=4321, half_width=3.0)
+    np.savez_compressed(os.path.join(HERE, "aabb_tree.npz"), **tree_fixture(mods, scene))
+
+
+if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    main(sys.argv[1])

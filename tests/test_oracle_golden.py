@@ -1,0 +1,65 @@
+"""The C oracle against golden vectors produced by the distance3d reference.
+
+The oracle restates the reference's rounding sequence (NumPy/OpenBLAS fused
+multiply-add orders), so every comparison here is bit-exact.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb"])
+def test_gjk_distance_bit_exact(golden, name):
+    g, cs = golden(name)
+    r = oracle.gjk_distance(cs, g["i1"], g["i2"])
+    assert np.array_equal(r["dist"], g["dist"])
+    assert np.array_equal(r["n_simplex"], g["n_simplex"])
+    assert np.array_equal(r["iterations"], g["iterations"])
+    assert np.array_equal(r["cp1"], g["cp1"], equal_nan=True)
+    assert np.array_equal(r["cp2"], g["cp2"], equal_nan=True)
+    written = ~np.isnan(g["simplex"])
+    assert np.array_equal(r["simplex"][written], g["simplex"][written])
+    assert np.all(r["status"] == 0)
+
+
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb"])
+def test_gjk_intersection_and_aabbs(golden, name):
+    g, cs = golden(name)
+    h = oracle.gjk_intersection(cs, g["i1"], g["i2"])
+    assert np.array_equal(h["hit"], g["intersect"])
+    assert np.array_equal(g["intersect"], g["dist"] == 0.0)
+    assert np.array_equal(oracle.aabbs(cs), g["aabbs"])
+
+
+@pytest.mark.parametrize("tag,kw", [("default", {}),
+                                    ("large", dict(max_faces=256, max_loose_edges=128))])
+def test_epa_bit_exact(golden, tag, kw):
+    g, cs = golden("gjk_mixed6")
+    e, _ = golden("epa_mixed6")
+    p = e["pair"]
+    r = oracle.epa(cs, g["i1"][p], g["i2"][p], g["simplex"][p], **kw)
+    st = e[f"status_{tag}"]
+    assert np.array_equal(r["status"], st)
+    ok = st == 0
+    assert ok.sum() > 100
+    assert np.array_equal(r["mtv"][ok], e[f"mtv_{tag}"][ok])
+    assert np.array_equal(r["n_faces"][ok], e[f"n_faces_{tag}"][ok])
+
+
+def test_tree_pairs_equal_brute_force(golden):
+    t, cs = golden("aabb_tree")
+    assert np.array_equal(oracle.aabbs(cs), t["aabbs"])
+    assert np.array_equal(oracle.self_pairs(t["aabbs"]), t["tree_pairs"])
+    n = int(t["bvh_n"])
+    sub = oracle.self_pairs(t["aabbs"][:n])
+    both = np.sort(np.concatenate([sub, sub[:, ::-1]]).view("i4,i4"), axis=0).view(np.int32).reshape(-1, 2)
+    assert np.array_equal(both, t["bvh_pairs"])
+
+
+def test_queries_match_tree(golden):
+    t, _ = golden("aabb_tree")
+    for q in range(len(t["queries"])):
+        want = t["query_idx"][t["query_ptr"][q]:t["query_ptr"][q + 1]]
+        got = oracle.cross_pairs(t["queries"][q:q + 1], t["aabbs"])[:, 1]
+        assert np.array_equal(np.sort(got), want)

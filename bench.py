@@ -1,0 +1,382 @@
+"""Benchmark: batched GJK+EPA pairs/s on one GB300, mixed vs plain FP64.
+
+Workload: 1,048,576 collider pairs, types uniform over Sphere, Capsule, Box,
+Cylinder, Ellipsoid and ConvexHullVertices (hulls of N ~ logU[8,256] points on
+the unit sphere scaled by U[0.05,0.3]), centers in [-w,w]^3 with w calibrated
+to ~30% intersecting pairs (w = 1 as literally given yields ~3%; both
+fractions are printed).  One step = GJK distance for every pair, then EPA on
+the intersecting pairs.  Inputs are seeded synthetic data (2.1 M colliders,
+~1.6 GB resident, larger than L2, so no flush is needed between steps).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value`` is the mixed-precision form, inputs resident in HBM; ``fp64`` the
+plain FP64 drop-in on the same data; ``e2e`` the mixed form through the C ABI
+from pinned host buffers with every host<->device copy inside the timed
+region.  ``--impl reference`` times the CPU reference restatement (oracle,
+all host cores) on the same workload.  Under torchrun each rank processes its
+own shard of pairs (no data exchange) and rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_PAIRS = 1 << 20
+SEED = 2024
+METRIC = "GJK+EPA pairs/s (mixed precision form; plain FP64 form alongside)"
+UNIT = "pairs/s"
+EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
+
+# Algorithmic bytes per pair (counted once): two collider records, the hull
+# vertices of hull colliders, and the outputs.  FP64 record 120 B (pose 96 +
+# params 24) + type; FP32 record 60 B.  Hull vertices 24 B (FP64) / 12 B
+# (FP32) each.  Outputs: dist 8 + cp1 24 + cp2 24 + simplex 96 + n_simplex 1 +
+# status 1 = 154 B; EPA: mtv 24 + status 1 + face count 4 per intersecting pair.
+REC64, REC32, OUT_GJK, OUT_EPA = 124, 64, 154, 29
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pairs", type=int, default=N_PAIRS)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(n_pairs, rank):
+    from distance3d_gb300 import workloads
+    cs, i1, i2 = workloads.pairs_mixed_six(n_pairs, seed=SEED + rank,
+                                           center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    return cs, i1, i2
+
+
+def algorithmic_bytes(cs, i1, n_epa, precision):
+    hull = cs.types == 5
+    nv = cs.hull_count.astype(np.float64)
+    per_vertex = 24 if precision == "fp64" else 12
+    rec = REC64 if precision == "fp64" else REC32
+    n = len(i1)
+    inputs = 2 * n * rec + per_vertex * float(nv[hull].sum()) + 8 * n  # + the two int32 indices
+    return inputs + OUT_GJK * n + OUT_EPA * n_epa
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_pass(cs, i1, i2, nthreads=0):
+    """The reference algorithm on the host (C restatement, OpenMP): GJK
+    distance for every pair, EPA on pairs with a full simplex."""
+    from oracle import oracle
+    r = oracle.gjk_distance(cs, i1, i2, nthreads=nthreads)
+    hit = np.flatnonzero((r["dist"] == 0.0) & (r["n_simplex"] == 4))
+    oracle.epa(cs, i1[hit], i2[hit], r["simplex"][hit], nthreads=nthreads, **EPA_KW)
+    return len(i1)
+
+
+def time_cpu(cs, i1, i2, seconds):
+    """Pairs/s of the oracle on all host cores over at least `seconds` (or
+    one full pass), after one warm pass on a slice."""
+    from oracle import oracle
+    cpu_oracle_pass(cs, i1[:20000], i2[:20000])
+    done, t0 = 0, time.perf_counter()
+    while True:
+        done += cpu_oracle_pass(cs, i1, i2)
+        el = time.perf_counter() - t0
+        if el >= seconds or done >= 20 * len(i1):
+            break
+    return done / el, oracle.max_threads(), done, el
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    cs, i1, i2 = make_workload(args.pairs, 0)
+    from oracle import oracle
+    for _ in range(args.warmup):
+        cpu_oracle_pass(cs, i1[:50000], i2[:50000])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_oracle_pass(cs, i1, i2)
+    el = time.perf_counter() - t0
+    value = args.steps * len(i1) / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "1,048,576 six-type pairs, GJK distance + EPA (256 faces) on intersecting pairs",
+                   "pairs": len(i1)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
+                         "sample": f"{args.steps} full passes over {len(i1)} pairs"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    from distance3d_gb300 import _lib
+    from distance3d_gb300.store import ColliderStore, PinnedColliderSet
+    from distance3d_gb300.gjk import gjk_distance_batch
+    from distance3d_gb300.epa import epa_batch, epa_scratch_bytes
+
+    _lib.load()
+    cs, i1_np, i2_np = make_workload(args.pairs, rank)
+    n = len(i1_np)
+    store = ColliderStore(cs, device=dev)
+    i1 = torch.as_tensor(i1_np, device=dev)
+    i2 = torch.as_tensor(i2_np, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    scratch = torch.empty(epa_scratch_bytes(n, **{k: v for k, v in EPA_KW.items() if k != "epsilon"}),
+                          dtype=torch.uint8, device=dev)
+
+    def step(precision, ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        g = gjk_distance_batch(store, i1, i2, precision=precision)
+        if ev is not None:
+            ev[1].record(stream)
+        hit = torch.nonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4)).flatten()
+        if ev is not None:
+            ev[2].record(stream)
+        e = epa_batch(store, i1[hit], i2[hit], g["simplex"][hit], scratch=scratch, **EPA_KW)
+        if ev is not None:
+            ev[3].record(stream)
+        return g, hit, e
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(precision):
+        for _ in range(args.warmup):
+            step(precision)
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+        barrier()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        out = None
+        for k in range(args.steps):
+            out = step(precision, evs[k])
+        end.record(stream)
+        barrier()
+        total = start.elapsed_time(end) / 1e3
+        gjk = float(np.mean([e[0].elapsed_time(e[1]) for e in evs])) / 1e3
+        epa = float(np.mean([e[2].elapsed_time(e[3]) for e in evs])) / 1e3
+        if world > 1:
+            t = torch.tensor([total], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        return total, gjk, epa, out
+
+    with ClockSampler(local) as clocks:
+        t_mixed, gjk_mixed, epa_mixed, out_mixed = timed("mixed")
+    t_fp64, gjk_fp64, epa_fp64, out_fp64 = timed("fp64")
+
+    # accuracy of the mixed form against the FP64 form (which equals the
+    # reference bit for bit): relative distance error, flags, EPA depth
+    gm, hm, em = out_mixed
+    gf, hf, ef = out_fp64
+    dm, df = gm["dist"].double(), gf["dist"].double()
+    rel_raw = ((dm - df).abs() / df.abs().clamp(min=1.0)).cpu().numpy()
+    # where the reference's distance disagrees with its own closest points
+    # (rare sliver-triangle projections in Jolt's solve), compare with the
+    # separation of those closest points instead
+    sep_f = (gf["cp1"] - gf["cp2"]).norm(dim=1)
+    incons = ((sep_f - df).abs() > 1e-9 * df.clamp(min=1.0)) & (df > 0)
+    want = torch.where(incons, sep_f, df)
+    rel = ((dm - want).abs() / want.abs().clamp(min=1.0)).cpu().numpy()
+    n_incons = int(incons.sum().item())
+    sep = df > 1e-6
+    flags_ok = bool(torch.equal(dm[sep] > 0, df[sep] > 0))
+    depth_err = None
+    if hm.numel() and hf.numel() and torch.equal(hm, hf):
+        ok = (em["status"] == 0) & (ef["status"] == 0)
+        if ok.any():
+            a = em["mtv"][ok].norm(dim=1)
+            b = ef["mtv"][ok].norm(dim=1)
+            depth_err = float(((a - b).abs() / b.clamp(min=1e-12)).max().item())
+    n_epa = int(hm.numel())
+
+    # end to end through the C ABI from pinned host buffers
+    pinned = PinnedColliderSet(cs)
+    i1_h = torch.from_numpy(i1_np).pin_memory()
+    i2_h = torch.from_numpy(i2_np).pin_memory()
+    host_out = {}
+
+    def e2e_step():
+        st = ColliderStore(pinned, device=dev)
+        a = i1_h.to(dev, non_blocking=True)
+        b = i2_h.to(dev, non_blocking=True)
+        g = gjk_distance_batch(st, a, b, precision="mixed")
+        hit = torch.nonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4)).flatten()
+        e = epa_batch(st, a[hit], b[hit], g["simplex"][hit], scratch=scratch, **EPA_KW)
+        d2h = 0
+        for k, v in list(g.items()) + [("mtv", e["mtv"]), ("epa_status", e["status"]), ("hit", hit)]:
+            if k not in host_out or host_out[k].shape != v.shape:
+                host_out[k] = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+            host_out[k].copy_(v, non_blocking=True)
+            d2h += v.numel() * v.element_size()
+        return d2h
+
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d2h = e2e_step()
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    h2d = pinned.nbytes() + i1_h.numel() * 4 * 2
+
+    value = world * n * args.steps / t_mixed
+    fp64_value = world * n * args.steps / t_fp64
+    e2e_value = world * n * args.steps / t_e2e
+
+    # roofline: the dominant kernel of the mixed step
+    gjk_bytes = algorithmic_bytes(cs, i1_np, 0, "mixed") - OUT_EPA * 0
+    epa_bytes = n_epa * (2 * REC64 + OUT_EPA + 96)
+    if gjk_mixed >= epa_mixed:
+        dom, t_dom, bytes_dom = "k_gjk_distance_mixed", gjk_mixed, gjk_bytes
+    else:
+        dom, t_dom, bytes_dom = "k_epa", epa_mixed, epa_bytes
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = bytes_dom / t_dom / 1e9
+
+    line = None
+    if rank == 0:
+        cpu_value, cores, cpu_pairs, cpu_s = time_cpu(cs, i1_np, i2_np, args.cpu_seconds)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+            "config": {"workload": "1,048,576 six-type pairs, GJK distance + EPA (256 faces) on "
+                                   "intersecting pairs, centers in [-0.38,0.38]^3",
+                       "pairs_per_gpu": n, "intersecting_fraction": n_epa / n, "epa_pairs": n_epa,
+                       "l2": "inputs 1.6 GB > L2, no flush", "parallelism": f"replicas x{world}"},
+            "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * t_fp64 / args.steps,
+                     "gjk_ms": 1e3 * gjk_fp64, "epa_ms": 1e3 * epa_fp64},
+            "mixed_over_fp64": value / fp64_value,
+            "kernels_ms": {"gjk_mixed": 1e3 * gjk_mixed, "epa": 1e3 * epa_mixed,
+                           "gjk_fp64": 1e3 * gjk_fp64},
+            "accuracy": {"max_rel_dist_err": float(rel.max()), "p99_rel_dist_err": float(np.percentile(rel, 99)),
+                         "max_rel_dist_err_vs_raw_reference_dist": float(rel_raw.max()),
+                         "reference_self_inconsistent_pairs": n_incons,
+                         "flags_identical_beyond_1e-6": flags_ok, "epa_depth_max_rel_err": depth_err},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
+            "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{cpu_pairs} pairs ({cpu_s:.1f} s) of the same workload, "
+                                       "GJK + EPA, C restatement with OpenMP"},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

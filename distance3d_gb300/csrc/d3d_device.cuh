@@ -1,0 +1,230 @@
+// d3d_device.cuh -- device-side building blocks shared by the kernels of
+// libd3d_gb300: vector arithmetic with the reference's rounding sequence,
+// collider loads from the store, and the six support functions.
+//
+// Rounding.  The reference computes its small dot products through NumPy,
+// whose BLAS rounds them as fused multiply-add chains in two fixed orders
+// (dot012 and dot102 below); element-wise arithmetic, np.cross and Python
+// scalar arithmetic are unfused.  Translation units that must reproduce the
+// reference bit for bit are compiled with -fmad=false, so that only the fma()
+// calls written here fuse.  The same code compiled with -fmad=true (the
+// mixed-precision unit) is free to contract.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "d3d_gb300.h"
+
+namespace d3d {
+
+template <typename T>
+struct V3 {
+    T x, y, z;
+};
+using d3 = V3<double>;
+using f3 = V3<float>;
+
+template <typename T>
+__device__ __forceinline__ V3<T> mk(T x, T y, T z) {
+    V3<T> r;
+    r.x = x;
+    r.y = y;
+    r.z = z;
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ V3<T> operator+(V3<T> a, V3<T> b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <typename T>
+__device__ __forceinline__ V3<T> operator-(V3<T> a, V3<T> b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+template <typename T>
+__device__ __forceinline__ V3<T> operator-(V3<T> a) { return mk(-a.x, -a.y, -a.z); }
+template <typename T>
+__device__ __forceinline__ V3<T> operator*(V3<T> a, T s) { return mk(a.x * s, a.y * s, a.z * s); }
+
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double sqrt_t(double a) { return sqrt(a); }
+__device__ __forceinline__ float sqrt_t(float a) { return sqrtf(a); }
+__device__ __forceinline__ double abs_t(double a) { return fabs(a); }
+__device__ __forceinline__ float abs_t(float a) { return fabsf(a); }
+
+// np.dot of two 3-vectors (ddot), np.linalg.norm, and the small GEMMs of
+// geometry.py:157 / containment.py:147: fma(a2,b2, fma(a1,b1, a0*b0))
+template <typename T>
+__device__ __forceinline__ T dot012(T a0, T a1, T a2, T b0, T b1, T b2) {
+    return fma_t(a2, b2, fma_t(a1, b1, a0 * b0));
+}
+// matrix-times-vector through BLAS gemv (pose products utils.py:143,
+// geometry.py:198,245,281; hull support colliders.py:132):
+// fma(a2,b2, fma(a0,b0, a1*b1))
+template <typename T>
+__device__ __forceinline__ T dot102(T a0, T a1, T a2, T b0, T b1, T b2) {
+    return fma_t(a2, b2, fma_t(a0, b0, a1 * b1));
+}
+template <typename T>
+__device__ __forceinline__ T dot(V3<T> a, V3<T> b) { return dot012(a.x, a.y, a.z, b.x, b.y, b.z); }
+template <typename T>
+__device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// ----------------------------------------------------------------------------
+// Colliders
+// ----------------------------------------------------------------------------
+
+// One collider as the kernels see it.  R row-major, t, params; hull vertex
+// range [off, off + nv) for boxes and hulls.
+template <typename T>
+struct Col {
+    int type, nv, off;
+    T R[9], t[3], p[3];
+};
+
+__device__ __forceinline__ void load_meta(const d3d_store& s, int idx, int& type, int& nv, int& off) {
+    int4 m = __ldg(reinterpret_cast<const int4*>(s.meta) + idx);
+    type = m.x;
+    nv = m.y;
+    off = m.z;
+}
+
+__device__ __forceinline__ void load_col(const d3d_store& s, int idx, Col<double>& c) {
+    load_meta(s, idx, c.type, c.nv, c.off);
+    const double2* r = reinterpret_cast<const double2*>(s.rec64) + (size_t)idx * 8;
+    double v[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        double2 q = __ldg(r + k);
+        v[2 * k] = q.x;
+        v[2 * k + 1] = q.y;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) c.R[k] = v[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        c.t[k] = v[9 + k];
+        c.p[k] = v[12 + k];
+    }
+}
+
+__device__ __forceinline__ void load_col(const d3d_store& s, int idx, Col<float>& c) {
+    load_meta(s, idx, c.type, c.nv, c.off);
+    const float4* r = reinterpret_cast<const float4*>(s.rec32) + (size_t)idx * 4;
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float4 q = __ldg(r + k);
+        v[4 * k] = q.x;
+        v[4 * k + 1] = q.y;
+        v[4 * k + 2] = q.z;
+        v[4 * k + 3] = q.w;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) c.R[k] = v[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        c.t[k] = v[9 + k];
+        c.p[k] = v[12 + k];
+    }
+}
+
+__device__ __forceinline__ d3 load_vertex(const double* verts, int row) {
+    const double2* v = reinterpret_cast<const double2*>(verts) + (size_t)row * 2;
+    double2 a = __ldg(v), b = __ldg(v + 1);
+    return mk(a.x, a.y, b.x);
+}
+__device__ __forceinline__ f3 load_vertex(const float* verts, int row) {
+    float4 a = __ldg(reinterpret_cast<const float4*>(verts) + row);
+    return mk(a.x, a.y, a.z);
+}
+
+// R^T d (np.dot(pose[:3, :3].T, d))
+template <typename T>
+__device__ __forceinline__ V3<T> rt_mul(const T* R, V3<T> d) {
+    return mk(dot102(R[0], R[3], R[6], d.x, d.y, d.z), dot102(R[1], R[4], R[7], d.x, d.y, d.z),
+              dot102(R[2], R[5], R[8], d.x, d.y, d.z));
+}
+// t + R v (utils.py:125-143 transform_point)
+template <typename T>
+__device__ __forceinline__ V3<T> xform(const T* R, const T* t, V3<T> v) {
+    return mk(t[0] + dot102(R[0], R[1], R[2], v.x, v.y, v.z), t[1] + dot102(R[3], R[4], R[5], v.x, v.y, v.z),
+              t[2] + dot102(R[6], R[7], R[8], v.x, v.y, v.z));
+}
+
+// Index of the first maximum of V . d over a hull's vertices
+// (np.argmax(vertices.dot(d)), colliders.py:131-132).  A one-row vertex
+// array goes through ddot instead of gemv, hence the dot012 special case.
+template <typename T>
+__device__ __forceinline__ int hull_argmax(const T* verts, int off, int nv, V3<T> d) {
+    if (nv == 1) return 0;
+    int best = 0;
+    V3<T> v = load_vertex(verts, off);
+    T bd = dot102(v.x, v.y, v.z, d.x, d.y, d.z);
+    for (int k = 1; k < nv; ++k) {
+        v = load_vertex(verts, off + k);
+        T s = dot102(v.x, v.y, v.z, d.x, d.y, d.z);
+        if (s > bd) {
+            bd = s;
+            best = k;
+        }
+    }
+    return best;
+}
+
+// Support point of collider c along d.  Sphere geometry.py:314-346, capsule
+// :209-256, cylinder :160-206, ellipsoid :259-284 (norm_vector utils.py:12-30),
+// box and hull: first-maximum vertex (colliders.py:131-132).
+template <typename T>
+__device__ __forceinline__ V3<T> support(const Col<T>& c, const T* verts, V3<T> d) {
+    switch (c.type) {
+    case D3D_SPHERE: {
+        T n = sqrt_t(dot(d, d));
+        V3<T> ctr = mk(c.t[0], c.t[1], c.t[2]);
+        if (n == T(0)) return ctr + mk(T(0), T(0), c.p[0]);
+        return ctr + mk(d.x / n * c.p[0], d.y / n * c.p[0], d.z / n * c.p[0]);
+    }
+    case D3D_CAPSULE: {
+        V3<T> l = rt_mul(c.R, d);
+        T s = sqrt_t(l.x * l.x + l.y * l.y + l.z * l.z);
+        V3<T> v;
+        if (s == T(0)) {
+            v = mk(c.p[0], T(0), T(0));
+        } else {
+            T f = c.p[0] / s;
+            v = mk(l.x * f, l.y * f, l.z * f);
+        }
+        if (l.z > T(0))
+            v.z += T(0.5) * c.p[1];
+        else
+            v.z -= T(0.5) * c.p[1];
+        return xform(c.R, c.t, v);
+    }
+    case D3D_CYLINDER: {
+        V3<T> l = rt_mul(c.R, d);
+        T s = sqrt_t(l.x * l.x + l.y * l.y);
+        T z = (l.z < T(0)) ? T(-0.5) * c.p[1] : T(0.5) * c.p[1];
+        V3<T> v;
+        if (s == T(0)) {
+            v = mk(c.p[0], T(0), z);
+        } else {
+            T f = c.p[0] / s;
+            v = mk(l.x * f, l.y * f, z);
+        }
+        return xform(c.R, c.t, v);
+    }
+    case D3D_ELLIPSOID: {
+        V3<T> l = rt_mul(c.R, d);
+        V3<T> a = mk(l.x * c.p[0], l.y * c.p[1], l.z * c.p[2]);
+        T n = sqrt_t(dot(a, a));
+        if (n != T(0)) a = mk(a.x / n, a.y / n, a.z / n);
+        a = mk(a.x * c.p[0], a.y * c.p[1], a.z * c.p[2]);
+        return xform(c.R, c.t, a);
+    }
+    default:
+        if (c.nv < 1) return mk(T(NAN), T(NAN), T(NAN));  // rejected by d3d_store_pack
+        return load_vertex(verts, c.off + hull_argmax(verts, c.off, c.nv, d));
+    }
+}
+
+}  // namespace d3d

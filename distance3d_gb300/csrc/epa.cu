@@ -1,0 +1,279 @@
+// epa.cu -- batched FP64 EPA (expanding polytope), one thread per pair.
+//
+// Restates distance3d epa.py (Kevin Moran's formulation): the polytope is an
+// unordered array of faces (3 vertices + unit normal), the face closest to the
+// origin is found by a linear scan with first-minimum tie-breaking, faces
+// visible from the new support point are removed by moving the last face into
+// their slot and re-testing that slot, and the horizon ("loose") edges are
+// matched by coordinates within epsilon.  Every order-dependent step keeps the
+// reference's order, so faces, normals and the MTV are the reference's bit for
+// bit (-fmad=false; see d3d_device.cuh).
+//
+// Where the reference raises (face buffer full, epa.py:128; np.argmin on an
+// empty polytope) the pair gets a status code instead.
+//
+// Scheduling: pairs are sorted by collider types, and a persistent grid runs
+// one EPA iteration per round per lane; a lane whose pair ends fetches the
+// next one.  Each thread owns one scratch slot of max_faces faces and
+// max_loose_edges edges (d3d_epa_scratch_bytes), reused across its pairs, so
+// the scratch is bounded by the slot count, not by n.
+#include "capi_util.h"
+#include "d3d_device.cuh"
+#include "persist.cuh"
+#include "scratch.h"
+
+namespace {
+
+using namespace d3d;
+
+constexpr int64_t kMaxSlots = 32768;  // scratch slots (threads) per launch
+constexpr int kBlock = 128;
+constexpr int64_t kScheduleMin = 4096;
+
+__device__ __forceinline__ d3 ld(const double* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ void st(double* p, d3 v) {
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+
+// utils.py:12-30 norm_vector
+__device__ __forceinline__ d3 norm_vec(d3 v) {
+    double n = sqrt(dot(v, v));
+    if (n == 0.0) return v;
+    return mk(v.x / n, v.y / n, v.z / n);
+}
+
+// epa.py:99-102; a face is 12 doubles: v0, v1, v2, n
+__device__ __forceinline__ void face_normal(double* f) {
+    d3 v0 = ld(f), v1 = ld(f + 3), v2 = ld(f + 6);
+    st(f + 9, norm_vec(cross(v1 - v0, v2 - v0)));
+}
+
+__device__ __forceinline__ void copy12(double* dst, const double* src) {
+#pragma unroll
+    for (int j = 0; j < 12; ++j) dst[j] = src[j];
+}
+
+// One pair's EPA between iterations.  F (faces) and E (loose edges) live in
+// the thread's scratch slot.
+struct EpaLoop {
+    int nf;       // faces in the polytope
+    int closest;  // face chosen by the last iteration's scan
+    int it;
+};
+
+// epa.py:56-57, 89-97: the initial faces ABC, ACD, ADB, BDC
+__device__ __forceinline__ void epa_begin(EpaLoop& L, const double* simplex, double* F) {
+    const int init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) st(F + 12 * i + 3 * j, ld(simplex + 3 * init[i][j]));
+        face_normal(F + 12 * i);
+    }
+    L.nf = 4;
+    L.closest = 0;
+    L.it = 0;
+}
+
+// One iteration of epa.py:59-74.  Returns -1 while running, else the status
+// (mtv written).
+__device__ __forceinline__ int epa_step(EpaLoop& L, const Col<double>& c1, const Col<double>& c2,
+                                        const double* verts, const d3d_epa_options& o, double* F, double* E,
+                                        d3& mtv) {
+    const double eps = o.epsilon;
+    if (L.it >= o.max_iterations) {
+        // epa.py:77: closest_face is a view, read after the last iteration's edits
+        const double* f = F + 12 * L.closest;
+        d3 n = ld(f + 9);
+        mtv = n * dot(ld(f), n);
+        return D3D_STATUS_EPA_NOT_CONVERGED;
+    }
+    ++L.it;
+    int nf = L.nf;
+    if (nf == 0) {
+        mtv = mk(double(NAN), double(NAN), double(NAN));
+        return D3D_STATUS_EPA_DEGENERATE;
+    }
+    // epa.py:104-109: np.sum(v0 * n, axis=1), np.argmin (first minimum)
+    double md = 0.0;
+    int closest = 0;
+    for (int i = 0; i < nf; ++i) {
+        const double* f = F + 12 * i;
+        double d = (f[0] * f[9] + f[1] * f[10]) + f[2] * f[11];
+        if (i == 0 || d < md) {
+            md = d;
+            closest = i;
+        }
+    }
+    L.closest = closest;
+    d3 sd = ld(F + 12 * closest + 9);
+    d3 np_ = support(c1, verts, sd) - support(c2, verts, -sd);
+    double pd = dot(np_, sd);
+    if (pd - md < eps) {  // epa.py:67-70
+        mtv = sd * pd;
+        return D3D_STATUS_OK;
+    }
+    // epa.py:157-165 remove visible faces, collect horizon edges
+    int ne = 0;
+    int i = 0;
+    while (i < nf) {
+        double* f = F + 12 * i;
+        if (dot(ld(f + 9), np_ - ld(f)) > eps) {  // epa.py:122-124
+            for (int j = 0; j < 3; ++j) {         // epa.py:167-187
+                d3 e0 = ld(f + 3 * j), e1 = ld(f + 3 * ((j + 1) % 3));
+                bool found = false;
+                for (int k = 0; k < ne; ++k) {
+                    double* e = E + 6 * k;
+                    d3 d1 = ld(e + 3) - e0, d0 = ld(e) - e1;
+                    if (sqrt(dot(d1, d1)) < eps && sqrt(dot(d0, d0)) < eps) {
+                        const double* last = E + 6 * (ne - 1);
+#pragma unroll
+                        for (int q = 0; q < 6; ++q) e[q] = last[q];
+                        --ne;
+                        found = true;
+                        break;
+                    }
+                }
+                if (!found) {
+                    if (ne >= o.max_loose_edges) break;  // epa.py:193-198
+                    st(E + 6 * ne, e0);
+                    st(E + 6 * ne + 3, e1);
+                    ++ne;
+                }
+            }
+            copy12(f, F + 12 * (nf - 1));  // epa.py:118-120
+            --nf;
+            continue;
+        }
+        ++i;
+    }
+    // epa.py:126-137 extend_with_point
+    for (int k = 0; k < ne; ++k) {
+        if (!(nf < o.max_faces)) {
+            L.nf = nf;
+            mtv = mk(double(NAN), double(NAN), double(NAN));
+            return D3D_STATUS_EPA_FACE_OVERFLOW;
+        }
+        double* f = F + 12 * nf;
+        st(f, ld(E + 6 * k));
+        st(f + 3, ld(E + 6 * k + 3));
+        st(f + 6, np_);
+        face_normal(f);
+        d3 n = ld(f + 9);
+        if (sqrt(dot(n, n)) < 0.5) continue;
+        // epa.py:139-146: the reference swaps through a NumPy view of row
+        // 0, so the net effect is v0 := v1 (v1 unchanged), n := -n
+        if (dot(ld(f), n) + 1e-6 < 0.0) {
+            st(f, ld(f + 3));
+            st(f + 9, -n);
+        }
+        ++nf;
+    }
+    L.nf = nf;
+    return -1;
+}
+
+__global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __restrict__ i1,
+                                                const int32_t* __restrict__ i2, const int32_t* __restrict__ order,
+                                                int64_t n, unsigned long long* __restrict__ cursor,
+                                                const double* __restrict__ simplex, d3d_epa_options o,
+                                                double* __restrict__ mtv, int8_t* __restrict__ status,
+                                                int32_t* __restrict__ n_faces, double* __restrict__ faces,
+                                                double* __restrict__ scratch, int64_t slot_doubles) {
+    const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double* F = scratch + slot * slot_doubles;
+    double* E = F + 12 * (int64_t)o.max_faces;
+    EpaLoop L;
+    int64_t pid = 0;
+    int a = 0, b = 0;
+    bool need = true;
+    while (true) {
+        const long long k = fetch_slot(cursor, need);
+        if (need) {
+            if (k >= n) break;
+            pid = order ? order[k] : k;
+            a = i1[pid];
+            b = i2[pid];
+            epa_begin(L, simplex + 12 * pid, F);
+            need = false;
+        }
+        Col<double> c1, c2;
+        load_col(s, a, c1);
+        load_col(s, b, c2);
+        d3 m;
+        const int stt = epa_step(L, c1, c2, s.verts64, o, F, E, m);
+        if (stt >= 0) {
+            mtv[3 * pid] = m.x;
+            mtv[3 * pid + 1] = m.y;
+            mtv[3 * pid + 2] = m.z;
+            status[pid] = (int8_t)stt;
+            const int nf = stt == D3D_STATUS_EPA_DEGENERATE ? 0 : L.nf;
+            n_faces[pid] = nf;
+            if (faces) {
+                double* out = faces + pid * 12 * (int64_t)o.max_faces;
+                for (int j = 0; j < 12 * nf; ++j) out[j] = F[j];
+            }
+            need = true;
+        }
+    }
+}
+
+int64_t slot_doubles(const d3d_epa_options& o) {
+    return 12 * (int64_t)o.max_faces + 6 * (int64_t)o.max_loose_edges;
+}
+
+int64_t slots_for(int64_t n) {
+    int64_t s = n < kMaxSlots ? n : kMaxSlots;
+    return ((s + kBlock - 1) / kBlock) * kBlock;
+}
+
+bool valid(const d3d_epa_options* o) {
+    return o && o->max_iterations >= 0 && o->max_faces >= 4 && o->max_loose_edges >= 0 && o->epsilon >= 0.0;
+}
+
+}  // namespace
+
+extern "C" size_t d3d_epa_scratch_bytes(int64_t n, const d3d_epa_options* options) {
+    if (!valid(options) || n <= 0) return 0;
+    return (size_t)(slots_for(n) * slot_doubles(*options) * (int64_t)sizeof(double));
+}
+
+extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n, const double* simplex,
+                       const d3d_epa_options* options, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                       void* scratch, size_t scratch_bytes, void* stream) {
+    int rc = d3d::check_store(store, "d3d_epa");
+    if (rc) return rc;
+    D3D_REQUIRE(valid(options), "d3d_epa: invalid options (need max_faces >= 4, limits >= 0, epsilon >= 0)");
+    D3D_REQUIRE(n >= 0, "d3d_epa: n < 0");
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(i1 && i2 && simplex && mtv && status && n_faces, "d3d_epa: null pointer");
+    size_t need = d3d_epa_scratch_bytes(n, options);
+    if (!scratch || scratch_bytes < need) {
+        d3d::set_error("d3d_epa: scratch of %zu bytes < %zu needed", scratch_bytes, need);
+        return D3D_ERR_CAPACITY;
+    }
+    cudaStream_t st = d3d::as_stream(stream);
+    const bool sched = n >= kScheduleMin;
+    const size_t order_bytes = sched ? ((sizeof(int32_t) * (size_t)n + 255) & ~size_t(255)) : 0;
+    const size_t temp_bytes = sched ? d3d::pair_order_temp_bytes(n) : 0;
+    void* block = nullptr;
+    rc = d3d::scratch_alloc(&block, 256 + order_bytes + temp_bytes, st);
+    if (rc) return rc;
+    unsigned long long* cursor = static_cast<unsigned long long*>(block);
+    int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(block) + 256) : nullptr;
+    cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
+    if (sched)
+        rc = d3d::pair_order(*store, i1, i2, n, order, static_cast<char*>(block) + 256 + order_bytes, temp_bytes, st);
+    if (!rc) {
+        int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
+        const int64_t max_blocks = slots_for(n) / kBlock;  // the scratch holds this many slots
+        if (blocks > max_blocks) blocks = (int)max_blocks;
+        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, order, n, cursor, simplex, *options, mtv, status, n_faces,
+                                         faces, static_cast<double*>(scratch), slot_doubles(*options));
+        rc = d3d::check_launch("d3d_epa");
+    }
+    d3d::scratch_free(block, st);
+    return rc;
+}

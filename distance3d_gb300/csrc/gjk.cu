@@ -1,0 +1,139 @@
+// gjk.cu -- the plain FP64 GJK drop-in: batched distance and intersection,
+// one thread per pair.  Compiled with -fmad=false so that the arithmetic is
+// the reference's rounding sequence (see d3d_device.cuh); the results are the
+// reference's bit for bit.
+#include "capi_util.h"
+#include "gjk_impl.h"
+#include "gjk_out.cuh"
+#include "persist.cuh"
+#include "scratch.h"
+#include "jolt.cuh"
+
+namespace {
+
+using namespace d3d;
+
+constexpr int kBlock = 128;
+constexpr int64_t kScheduleMin = 4096;  // below this, pairs run in input order
+
+// Persistent FP64 GJK distance: each lane runs the reference's loop for one
+// pair at a time (one iteration per round) and fetches the next pair, in the
+// type-sorted `order`, when its pair ends.  `n_dev` (if not null) holds the
+// pair count on the device (fallback lists of the mixed form).
+__global__ void __launch_bounds__(kBlock) k_gjk_distance_f64(d3d_store s, const int32_t* __restrict__ i1,
+                                                            const int32_t* __restrict__ i2,
+                                                            const int32_t* __restrict__ order, int64_t n,
+                                                            const unsigned long long* __restrict__ n_dev,
+                                                            unsigned long long* __restrict__ cursor,
+                                                            d3d_gjk_options opt, DistanceOut o) {
+    if (n_dev) n = (int64_t)*n_dev;
+    const JoltEps<double> E = reference_eps<double>();
+    const double tol_sq = opt.tolerance * opt.tolerance;
+    GjkLoop<double> g;
+    int64_t pid = 0;
+    int a = 0, b = 0;
+    bool need = true;
+    while (true) {
+        const long long slot = fetch_slot(cursor, need);
+        if (need) {
+            if (slot >= n) break;
+            pid = order ? order[slot] : slot;
+            a = i1[pid];
+            b = i2[pid];
+            simplex_clear(g.S);
+            const d3 dir = mk(1.0, 0.0, 0.0);
+            gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
+            need = false;
+        }
+        // collider records are re-read every round (L1-resident) so that
+        // they hold no registers across the simplex solve
+        Col<double> c1, c2;
+        load_col(s, a, c1);
+        load_col(s, b, c2);
+        if (gjk_step<double>(g, c1, c2, s, tol_sq, opt.max_distance_squared, opt.max_iterations, E)) {
+            GjkResult<double> r;
+            gjk_end(g, opt.sanity_check, E, r);
+            store_result(o, pid, r, g.S);
+            need = true;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_gjk_intersection_f64(d3d_store s, const int32_t* __restrict__ i1,
+                                                              const int32_t* __restrict__ i2, int64_t n,
+                                                              double tol_sq, int max_iter, int8_t* __restrict__ hit,
+                                                              int8_t* __restrict__ status) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    Col<double> c1, c2;
+    load_col(s, i1[k], c1);
+    load_col(s, i2[k], c2);
+    JoltEps<double> E = reference_eps<double>();
+    int st;
+    hit[k] = (int8_t)gjk_intersection_loop(c1, c2, s, tol_sq, max_iter, E, st);
+    status[k] = (int8_t)st;
+}
+
+}  // namespace
+
+extern "C" int d3d_gjk_distance(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                                const d3d_gjk_options* options, double* dist, double* cp1, double* cp2,
+                                double* simplex, int8_t* n_simplex, int8_t* status, int32_t* iterations,
+                                void* stream) {
+    int rc = d3d::check_store(store, "d3d_gjk_distance");
+    if (rc) return rc;
+    D3D_REQUIRE(options, "d3d_gjk_distance: null options");
+    D3D_REQUIRE(n >= 0, "d3d_gjk_distance: n < 0");
+    D3D_REQUIRE(options->max_iterations >= 1, "d3d_gjk_distance: max_iterations < 1");
+    D3D_REQUIRE(options->precision == D3D_PRECISION_FP64 || options->precision == D3D_PRECISION_MIXED,
+                "d3d_gjk_distance: unknown precision %d", options->precision);
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(i1 && i2 && dist && cp1 && cp2 && simplex && n_simplex && status,
+                "d3d_gjk_distance: null pointer");
+    if (options->precision == D3D_PRECISION_MIXED)
+        return d3d::gjk_distance_mixed(*store, i1, i2, n, *options, dist, cp1, cp2, simplex, n_simplex, status,
+                                       iterations, d3d::as_stream(stream));
+    cudaStream_t st = d3d::as_stream(stream);
+    const bool sched = n >= kScheduleMin;
+    const size_t order_bytes = sched ? ((sizeof(int32_t) * (size_t)n + 255) & ~size_t(255)) : 0;
+    const size_t temp_bytes = sched ? d3d::pair_order_temp_bytes(n) : 0;
+    void* block = nullptr;
+    rc = d3d::scratch_alloc(&block, 256 + order_bytes + temp_bytes, st);
+    if (rc) return rc;
+    unsigned long long* cursor = static_cast<unsigned long long*>(block);
+    int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(block) + 256) : nullptr;
+    cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
+    if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, static_cast<char*>(block) + 256 + order_bytes, temp_bytes, st);
+    if (!rc) {
+        DistanceOut o{dist, cp1, cp2, simplex, n_simplex, status, iterations};
+        rc = d3d::launch_gjk_f64(*store, i1, i2, order, n, nullptr, cursor, *options, o, st);
+    }
+    d3d::scratch_free(block, st);
+    return rc;
+}
+
+namespace d3d {
+
+int launch_gjk_f64(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
+                   const unsigned long long* n_dev, unsigned long long* cursor, const d3d_gjk_options& opt,
+                   const DistanceOut& o, cudaStream_t stream) {
+    const int blocks = persistent_blocks((const void*)k_gjk_distance_f64, kBlock, n);
+    k_gjk_distance_f64<<<blocks, kBlock, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+    return check_launch("d3d_gjk_distance");
+}
+
+}  // namespace d3d
+
+extern "C" int d3d_gjk_intersection(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                                    double tolerance, int32_t max_iterations, int8_t* hit, int8_t* status,
+                                    void* stream) {
+    int rc = d3d::check_store(store, "d3d_gjk_intersection");
+    if (rc) return rc;
+    D3D_REQUIRE(n >= 0, "d3d_gjk_intersection: n < 0");
+    D3D_REQUIRE(max_iterations >= 1, "d3d_gjk_intersection: max_iterations < 1");
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(i1 && i2 && hit && status, "d3d_gjk_intersection: null pointer");
+    k_gjk_intersection_f64<<<d3d::grid_for(n, 128), 128, 0, d3d::as_stream(stream)>>>(
+        *store, i1, i2, n, tolerance * tolerance, max_iterations, hit, status);
+    return d3d::check_launch("d3d_gjk_intersection");
+}

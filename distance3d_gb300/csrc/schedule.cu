@@ -1,0 +1,117 @@
+// schedule.cu -- pair scheduling (type-sorted order), the library's scratch
+// pool and persistent-launch sizing.
+#include <cub/cub.cuh>
+
+#include <mutex>
+
+#include "capi_util.h"
+#include "scratch.h"
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+
+inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+// key = ((type1 * 6 + type2) << 4) | size class of the larger hull
+__global__ void k_pair_keys(d3d_store s, const int32_t* __restrict__ i1, const int32_t* __restrict__ i2, int64_t n,
+                            uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int4 a = __ldg(reinterpret_cast<const int4*>(s.meta) + i1[k]);
+    int4 b = __ldg(reinterpret_cast<const int4*>(s.meta) + i2[k]);
+    int nv = max(a.x == D3D_HULL ? a.y : 0, b.x == D3D_HULL ? b.y : 0);
+    int cls = nv > 0 ? min(32 - __clz(nv), 15) : 0;
+    unsigned ta = (unsigned)min(max(a.x, 0), 5), tb = (unsigned)min(max(b.x, 0), 5);
+    keys[k] = ((ta * 6u + tb) << 4) | (unsigned)cls;
+    vals[k] = (int32_t)k;
+}
+
+}  // namespace
+
+namespace d3d {
+
+int scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        set_error("scratch: no current device (%s)", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        if (!g_pool[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            e = cudaMemPoolCreate(&g_pool[dev], &props);
+            if (e != cudaSuccess) {
+                g_pool[dev] = nullptr;
+                set_error("scratch: cudaMemPoolCreate: %s", cudaGetErrorString(e));
+                return D3D_ERR_CUDA;
+            }
+            uint64_t keep = uint64_t(1) << 30;
+            cudaMemPoolSetAttribute(g_pool[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool = g_pool[dev];
+    }
+    e = cudaMallocFromPoolAsync(p, bytes ? bytes : 1, pool, stream);
+    if (e != cudaSuccess) {
+        set_error("scratch: allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    return D3D_SUCCESS;
+}
+
+void scratch_free(void* p, cudaStream_t stream) {
+    if (p) cudaFreeAsync(p, stream);
+}
+
+int persistent_blocks(const void* kernel, int block, int64_t work_items) {
+    int dev = 0, sms = 1, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    int64_t want = (work_items + block - 1) / block;
+    int64_t full = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    int64_t b = want < full ? want : full;
+    return (int)(b > 0 ? b : 1);
+}
+
+size_t pair_order_temp_bytes(int64_t n) {
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (const int32_t*)nullptr, (int32_t*)nullptr, (int)n, 0, 10);
+    return 2 * align_up(sizeof(uint32_t) * (size_t)n) + align_up(sizeof(int32_t) * (size_t)n) + align_up(cub_bytes);
+}
+
+int pair_order(const d3d_store& s, const int32_t* i1, const int32_t* i2, int64_t n, int32_t* order, void* temp,
+               size_t temp_bytes, cudaStream_t stream) {
+    if (n <= 0) return D3D_SUCCESS;
+    if (temp_bytes < pair_order_temp_bytes(n)) {
+        set_error("pair_order: temporary storage too small");
+        return D3D_ERR_CAPACITY;
+    }
+    char* t = static_cast<char*>(temp);
+    uint32_t* keys = reinterpret_cast<uint32_t*>(t);
+    t += align_up(sizeof(uint32_t) * (size_t)n);
+    uint32_t* keys_out = reinterpret_cast<uint32_t*>(t);
+    t += align_up(sizeof(uint32_t) * (size_t)n);
+    int32_t* vals = reinterpret_cast<int32_t*>(t);
+    t += align_up(sizeof(int32_t) * (size_t)n);
+    size_t cub_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, keys, keys_out, vals, order, (int)n, 0, 10, stream);
+    k_pair_keys<<<grid_for(n, 256), 256, 0, stream>>>(s, i1, i2, n, keys, vals);
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(t, cub_bytes, keys, keys_out, vals, order, (int)n, 0, 10, stream);
+    if (e != cudaSuccess) {
+        set_error("pair_order: sort failed: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    return check_launch("pair_order");
+}
+
+}  // namespace d3d

@@ -1,0 +1,271 @@
+// store.cu -- the device collider store: packing, pose updates, support
+// points and axis-aligned bounding boxes.  Compiled with -fmad=false: every
+// value here must match the reference's FP64 rounding sequence.
+#include "capi_util.h"
+#include "d3d_device.cuh"
+
+namespace {
+
+using namespace d3d;
+
+// geometry.py:135,138-157 convert_box_to_vertices:
+// t + (BOX_COORDS * size) . R^T with BOX_COORDS in itertools.product order
+__device__ void write_box_vertices(const d3d_store& s, int off, const double* R, const double* t,
+                                   const double* size) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        double a0 = (((k >> 2) & 1) ? 0.5 : -0.5) * size[0];
+        double a1 = (((k >> 1) & 1) ? 0.5 : -0.5) * size[1];
+        double a2 = ((k & 1) ? 0.5 : -0.5) * size[2];
+        double v[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) v[i] = t[i] + dot012(a0, a1, a2, R[i * 3], R[i * 3 + 1], R[i * 3 + 2]);
+        double2* d = reinterpret_cast<double2*>(s.verts64) + (size_t)(off + k) * 2;
+        d[0] = make_double2(v[0], v[1]);
+        d[1] = make_double2(v[2], 0.0);
+        reinterpret_cast<float4*>(s.verts32)[off + k] =
+            make_float4(__double2float_rn(v[0]), __double2float_rn(v[1]), __double2float_rn(v[2]), 0.f);
+    }
+}
+
+__device__ void write_record(const d3d_store& s, int i, const double* R, const double* t, const double* p) {
+    double* r = s.rec64 + (size_t)i * 16;
+    float* f = s.rec32 + (size_t)i * 16;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        r[k] = R[k];
+        f[k] = __double2float_rn(R[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        r[9 + k] = t[k];
+        f[9 + k] = __double2float_rn(t[k]);
+        r[12 + k] = p[k];
+        f[12 + k] = __double2float_rn(p[k]);
+    }
+    r[15] = 0.0;
+    f[15] = 0.f;
+}
+
+__global__ void k_pack(d3d_store s, const int32_t* __restrict__ types, const double* __restrict__ poses,
+                       const double* __restrict__ params, const int64_t* __restrict__ hull_offset,
+                       const int32_t* __restrict__ hull_count, int64_t n, int* __restrict__ bad) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int type = types[i];
+    double R[9], t[3], p[3];
+    for (int k = 0; k < 9; ++k) R[k] = poses[i * 12 + k];
+    for (int k = 0; k < 3; ++k) {
+        t[k] = poses[i * 12 + 9 + k];
+        p[k] = params[i * 4 + k];
+    }
+    write_record(s, (int)i, R, t, p);
+    int count = 0, off = 0;
+    if (type == D3D_BOX) {
+        count = 8;
+        int64_t o = hull_offset[i];
+        if (o < 0 || o + 8 > s.n_vertices) {
+            atomicExch(bad, 1);
+            count = 0;
+        } else {
+            off = (int)o;
+            write_box_vertices(s, off, R, t, p);
+        }
+    } else if (type == D3D_HULL) {
+        int64_t o = hull_offset[i];
+        count = hull_count[i];
+        if (o < 0 || count < 1 || o + count > s.n_vertices) {
+            atomicExch(bad, 1);
+            count = 0;
+        } else {
+            off = (int)o;
+        }
+    } else if (type < 0 || type > D3D_HULL) {
+        atomicExch(bad, 1);
+    }
+    reinterpret_cast<int4*>(s.meta)[i] = make_int4(type, count, off, 0);
+}
+
+__global__ void k_hull_to_f32(d3d_store s, int64_t rows) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const double2* v = reinterpret_cast<const double2*>(s.verts64) + r * 2;
+    double2 a = v[0], b = v[1];
+    reinterpret_cast<float4*>(s.verts32)[r] =
+        make_float4(__double2float_rn(a.x), __double2float_rn(a.y), __double2float_rn(b.x), 0.f);
+}
+
+__global__ void k_set_poses(d3d_store s, const int32_t* __restrict__ idx, const double* __restrict__ poses,
+                            int64_t n) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int i = idx[k];
+    if (i < 0 || i >= s.n_colliders) return;
+    double R[9], t[3], p[3];
+    for (int j = 0; j < 9; ++j) R[j] = poses[k * 12 + j];
+    for (int j = 0; j < 3; ++j) {
+        t[j] = poses[k * 12 + 9 + j];
+        p[j] = s.rec64[(size_t)i * 16 + 12 + j];
+    }
+    int type, nv, off;
+    load_meta(s, i, type, nv, off);
+    if (type == D3D_HULL) return;
+    write_record(s, i, R, t, p);
+    if (type == D3D_BOX && nv == 8) write_box_vertices(s, off, R, t, p);
+}
+
+__global__ void k_support(d3d_store s, const int32_t* __restrict__ idx, const double* __restrict__ dirs,
+                          int64_t n, double* __restrict__ out) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    Col<double> c;
+    load_col(s, idx[k], c);
+    d3 r = support(c, s.verts64, mk(dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2]));
+    out[3 * k] = r.x;
+    out[3 * k + 1] = r.y;
+    out[3 * k + 2] = r.z;
+}
+
+// containment.py:6-148, one collider per thread; writes [axis][min,max]
+__global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n, double* __restrict__ out) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    Col<double> c;
+    load_col(s, idx ? idx[k] : (int)k, c);
+    const double* R = c.R;
+    const double* t = c.t;
+    double lo[3], hi[3];
+    switch (c.type) {
+    case D3D_SPHERE:  // :25-44
+        for (int i = 0; i < 3; ++i) {
+            lo[i] = t[i] - c.p[0];
+            hi[i] = t[i] + c.p[0];
+        }
+        break;
+    case D3D_CAPSULE:  // :99-122
+        for (int i = 0; i < 3; ++i) {
+            double e = 0.5 * c.p[1] * fabs(R[i * 3 + 2]) + c.p[0];
+            lo[i] = t[i] - e;
+            hi[i] = t[i] + e;
+        }
+        break;
+    case D3D_CYLINDER:  // :70-96
+        for (int i = 0; i < 3; ++i) {
+            double a = R[i * 3 + 2];
+            double e = 0.5 * c.p[1] * fabs(a) + c.p[0] * sqrt(1.0 - a * a);
+            lo[i] = t[i] - e;
+            hi[i] = t[i] + e;
+        }
+        break;
+    case D3D_ELLIPSOID: {  // :125-148
+        double E[9];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) E[i * 3 + j] = R[i * 3 + j] * c.p[j];
+        for (int j = 0; j < 3; ++j) {
+            double nn = sqrt((E[j] * E[j] + E[3 + j] * E[3 + j]) + E[6 + j] * E[6 + j]);
+            for (int i = 0; i < 3; ++i) E[i * 3 + j] = E[i * 3 + j] / nn;
+        }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) E[i * 3 + j] = E[i * 3 + j] * c.p[j];
+        for (int kk = 0; kk < 3; ++kk) {
+            double m = 0.0;
+            for (int i = 0; i < 3; ++i) {
+                double v = dot012(R[i * 3], R[i * 3 + 1], R[i * 3 + 2], E[kk * 3], E[kk * 3 + 1], E[kk * 3 + 2]);
+                if (i == 0 || v > m) m = v;
+            }
+            lo[kk] = t[kk] - m;
+            hi[kk] = t[kk] + m;
+        }
+        break;
+    }
+    default: {  // box :47-67, hull :6-22
+        if (c.nv < 1) {  // rejected by d3d_store_pack
+            for (int i = 0; i < 3; ++i) lo[i] = hi[i] = NAN;
+            break;
+        }
+        d3 v = load_vertex(s.verts64, c.off);
+        lo[0] = hi[0] = v.x;
+        lo[1] = hi[1] = v.y;
+        lo[2] = hi[2] = v.z;
+        for (int r = 1; r < c.nv; ++r) {
+            v = load_vertex(s.verts64, c.off + r);
+            if (v.x < lo[0]) lo[0] = v.x;
+            if (v.x > hi[0]) hi[0] = v.x;
+            if (v.y < lo[1]) lo[1] = v.y;
+            if (v.y > hi[1]) hi[1] = v.y;
+            if (v.z < lo[2]) lo[2] = v.z;
+            if (v.z > hi[2]) hi[2] = v.z;
+        }
+        break;
+    }
+    }
+    for (int i = 0; i < 3; ++i) {
+        out[6 * k + 2 * i] = lo[i];
+        out[6 * k + 2 * i + 1] = hi[i];
+    }
+}
+
+}  // namespace
+
+extern "C" int d3d_store_pack(const d3d_store* store, const int32_t* types, const double* poses,
+                              const double* params, const int64_t* hull_offset, const int32_t* hull_count,
+                              int64_t n_hull_vertices, void* stream) {
+    int rc = d3d::check_store(store, "d3d_store_pack");
+    if (rc) return rc;
+    const int64_t n = store->n_colliders;
+    D3D_REQUIRE(n == 0 || (types && poses && params && hull_offset && hull_count),
+                "d3d_store_pack: null input array");
+    D3D_REQUIRE(n_hull_vertices >= 0 && n_hull_vertices <= store->n_vertices,
+                "d3d_store_pack: n_hull_vertices %lld outside [0, %lld]", (long long)n_hull_vertices,
+                (long long)store->n_vertices);
+    cudaStream_t st = d3d::as_stream(stream);
+    int* bad = nullptr;
+    if (cudaMallocAsync(&bad, sizeof(int), st) != cudaSuccess || cudaMemsetAsync(bad, 0, sizeof(int), st) != cudaSuccess)
+        return d3d::check_launch("d3d_store_pack: flag");
+    if (n_hull_vertices > 0) k_hull_to_f32<<<d3d::grid_for(n_hull_vertices, 256), 256, 0, st>>>(*store, n_hull_vertices);
+    if (n > 0)
+        k_pack<<<d3d::grid_for(n, 128), 128, 0, st>>>(*store, types, poses, params, hull_offset, hull_count, n, bad);
+    int hbad = 0;
+    cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(bad, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        d3d::set_error("d3d_store_pack: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    D3D_REQUIRE(!hbad, "d3d_store_pack: a collider has an unknown type or a vertex range outside the pool");
+    return d3d::check_launch("d3d_store_pack");
+}
+
+extern "C" int d3d_store_set_poses(const d3d_store* store, const int32_t* idx, const double* poses, int64_t n,
+                                   void* stream) {
+    int rc = d3d::check_store(store, "d3d_store_set_poses");
+    if (rc) return rc;
+    D3D_REQUIRE(n >= 0, "d3d_store_set_poses: n < 0");
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(idx && poses, "d3d_store_set_poses: null pointer");
+    k_set_poses<<<d3d::grid_for(n, 128), 128, 0, d3d::as_stream(stream)>>>(*store, idx, poses, n);
+    return d3d::check_launch("d3d_store_set_poses");
+}
+
+extern "C" int d3d_support(const d3d_store* store, const int32_t* idx, const double* dirs, int64_t n, double* out,
+                           void* stream) {
+    int rc = d3d::check_store(store, "d3d_support");
+    if (rc) return rc;
+    D3D_REQUIRE(n >= 0, "d3d_support: n < 0");
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(idx && dirs && out, "d3d_support: null pointer");
+    k_support<<<d3d::grid_for(n, 128), 128, 0, d3d::as_stream(stream)>>>(*store, idx, dirs, n, out);
+    return d3d::check_launch("d3d_support");
+}
+
+extern "C" int d3d_aabbs(const d3d_store* store, const int32_t* idx, int64_t n, double* out, void* stream) {
+    int rc = d3d::check_store(store, "d3d_aabbs");
+    if (rc) return rc;
+    D3D_REQUIRE(n >= 0, "d3d_aabbs: n < 0");
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(out, "d3d_aabbs: null output");
+    D3D_REQUIRE(idx || n <= store->n_colliders, "d3d_aabbs: n > n_colliders");
+    k_aabbs<<<d3d::grid_for(n, 128), 128, 0, d3d::as_stream(stream)>>>(*store, idx, n, out);
+    return d3d::check_launch("d3d_aabbs");
+}

@@ -1,0 +1,159 @@
+/*
+ * d3d_gb300.h -- C ABI of libd3d_gb300.so, the GB300 (sm_103a) narrow and
+ * broad phase for distance3d.
+ *
+ * Conventions
+ * -----------
+ * - Every entry point returns an int status: D3D_SUCCESS (0) or a D3D_ERR_*
+ *   code; d3d_last_error() returns a message for the calling thread.  No entry
+ *   point aborts the process.
+ * - Every pointer argument except the d3d_store / options structs themselves
+ *   is a DEVICE pointer, caller allocated.  `stream` is a cudaStream_t passed as
+ *   void* (NULL = the legacy default stream).  Work is enqueued on that stream;
+ *   the call returns without synchronising unless stated otherwise.
+ * - Pair results are deterministic: one slot per pair, no atomics in result
+ *   slots, the same bits for the same inputs whatever the batch around them.
+ *
+ * Each entry point names the distance3d 0.9.0 interface it replaces
+ * (path:line inside that project).
+ */
+#ifndef D3D_GB300_H
+#define D3D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define D3D_ABI_VERSION 1
+
+/* return codes */
+#define D3D_SUCCESS 0
+#define D3D_ERR_INVALID 1   /* bad argument (null pointer, bad size, bad option) */
+#define D3D_ERR_CAPACITY 2  /* output or scratch capacity too small */
+#define D3D_ERR_CUDA 3      /* a CUDA runtime call failed */
+
+/* collider types (distance3d/colliders.py:109-440) */
+#define D3D_SPHERE 0
+#define D3D_CAPSULE 1
+#define D3D_BOX 2
+#define D3D_CYLINDER 3
+#define D3D_ELLIPSOID 4
+#define D3D_HULL 5          /* ConvexHullVertices */
+
+/* per-pair status codes */
+#define D3D_STATUS_OK 0
+#define D3D_STATUS_CLIPPED 1            /* separation > sqrt(max_distance_squared): dist = DBL_MAX, points NaN
+                                           (the reference returns (MAX_FLOAT, None, None, None), _gjk_jolt.py:209-210) */
+#define D3D_STATUS_SANITY 2             /* the reference's sanity assertion would fail (_gjk_jolt.py:215-216) */
+#define D3D_STATUS_MAX_ITER 3           /* iteration bound reached (the reference loops without bound) */
+#define D3D_STATUS_EPA_NOT_CONVERGED 4  /* EPA hit max_iter (epa.py:76-78, success = False) */
+#define D3D_STATUS_EPA_FACE_OVERFLOW 5  /* the reference raises AssertionError (epa.py:128) */
+#define D3D_STATUS_EPA_DEGENERATE 6     /* every face was removed (the reference raises in np.argmin) */
+
+#define D3D_PRECISION_FP64 0   /* plain FP64 drop-in: the reference's arithmetic, bit for bit */
+#define D3D_PRECISION_MIXED 1  /* FP32 iterations, FP64 final refinement */
+
+/*
+ * Device-resident collider store.  Built by d3d_store_pack from the packed
+ * host format (see distance3d_gb300/collider_set.py); all arrays are device
+ * memory owned by the caller.
+ *   rec64  [n][16] double : R row-major (9), t (3), params (3), 0
+ *   rec32  [n][16] float  : the same in FP32
+ *   meta   [n][4]  int32  : type, vertex count, vertex offset, 0
+ *   verts64 [V][4] double : hull vertices then 8 vertices per box (xyz, 0)
+ *   verts32 [V][4] float  : the same in FP32
+ */
+typedef struct d3d_store {
+    int64_t n_colliders;
+    int64_t n_vertices;
+    double* rec64;
+    float* rec32;
+    int32_t* meta;
+    double* verts64;
+    float* verts32;
+} d3d_store;
+
+typedef struct d3d_gjk_options {
+    double tolerance;             /* 1e-10 (_gjk_jolt.py:139) */
+    double max_distance_squared;  /* 1e5 */
+    double sanity_check;          /* 1e-8 */
+    int32_t max_iterations;       /* hard bound on GJK iterations, >= 1 */
+    int32_t precision;            /* D3D_PRECISION_* */
+} d3d_gjk_options;
+
+typedef struct d3d_epa_options {
+    int32_t max_iterations;   /* 64 (epa.py:9) */
+    int32_t max_loose_edges;  /* 32 */
+    int32_t max_faces;        /* 64 */
+    int32_t reserved;
+    double epsilon;           /* 1e-8 */
+} d3d_epa_options;
+
+int d3d_abi_version(void);
+const char* d3d_last_error(void);
+
+/* Pack a store.  Input arrays are the packed host format already copied to
+ * the device: types[n], poses[n][12], params[n][4], hull_offset[n] (int64;
+ * for a box: the row where its 8 derived vertices go, >= n_hull_vertices),
+ * hull_count[n]; the caller has copied the n_hull_vertices hull rows into
+ * store->verts64[0 : n_hull_vertices].  Box vertices follow
+ * geometry.py:138-157 (convert_box_to_vertices); FP32 mirrors are rounded from
+ * FP64.  Replaces collider construction, colliders.py:109-440. */
+int d3d_store_pack(const d3d_store* store, const int32_t* types, const double* poses,
+                   const double* params, const int64_t* hull_offset, const int32_t* hull_count,
+                   int64_t n_hull_vertices, void* stream);
+
+/* Set the poses of colliders idx[k] to poses[k][12] (R row-major, t) and
+ * re-derive box vertices.  Replaces ConvexCollider.update_pose
+ * (colliders.py:78-85, 172-176); a hull's pose cannot be set
+ * (colliders.py:137-138): D3D_ERR_INVALID is not detected on the device,
+ * so callers must not pass hull indices. */
+int d3d_store_set_poses(const d3d_store* store, const int32_t* idx, const double* poses,
+                        int64_t n, void* stream);
+
+/* Support points out[k] = support of collider idx[k] along dirs[k] (FP64).
+ * Replaces ConvexCollider.support_function (colliders.py:54-66). */
+int d3d_support(const d3d_store* store, const int32_t* idx, const double* dirs, int64_t n,
+                double* out, void* stream);
+
+/* Axis-aligned bounding boxes out[k][3][2] ([axis][min,max]) of colliders
+ * idx[k] (idx NULL: colliders 0..n-1).  Replaces ConvexCollider.aabb
+ * (colliders.py:88-95) and containment.py:6-148. */
+int d3d_aabbs(const d3d_store* store, const int32_t* idx, int64_t n, double* out, void* stream);
+
+/* Batched Jolt GJK distance for pairs (i1[k], i2[k]).  Outputs: dist[n],
+ * cp1[n][3], cp2[n][3], simplex[n][4][3] (rows >= n_simplex keep the
+ * reference's stale rows; rows never written are 0), n_simplex[n], status[n],
+ * iterations[n] (may be NULL).  Replaces gjk.gjk / gjk_distance /
+ * gjk_distance_jolt, gjk/_gjk_jolt.py:138-221 (aliases gjk/__init__.py:26-27). */
+int d3d_gjk_distance(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                     const d3d_gjk_options* options, double* dist, double* cp1, double* cp2,
+                     double* simplex, int8_t* n_simplex, int8_t* status, int32_t* iterations,
+                     void* stream);
+
+/* Batched Jolt GJK intersection test: hit[k] = 1 if the pair intersects.
+ * Replaces gjk.gjk_intersection / gjk_intersection_jolt, _gjk_jolt.py:29-135
+ * (alias gjk/__init__.py:28). */
+int d3d_gjk_intersection(const d3d_store* store, const int32_t* i1, const int32_t* i2,
+                         int64_t n, double tolerance, int32_t max_iterations, int8_t* hit,
+                         int8_t* status, void* stream);
+
+/* Scratch bytes d3d_epa needs for n pairs. */
+size_t d3d_epa_scratch_bytes(int64_t n, const d3d_epa_options* options);
+
+/* Batched EPA on GJK simplices simplex[n][4][3].  Outputs mtv[n][3],
+ * status[n], n_faces[n], faces[n][max_faces][4][3] (may be NULL).  `scratch`
+ * holds the polytopes (d3d_epa_scratch_bytes).  Replaces epa.epa, epa.py:9-78
+ * (Polytope :81-146, LooseEdges :149-202). */
+int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+            const double* simplex, const d3d_epa_options* options, double* mtv, int8_t* status,
+            int32_t* n_faces, double* faces, void* scratch, size_t scratch_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* D3D_GB300_H */

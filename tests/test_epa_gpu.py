@@ -1,0 +1,95 @@
+"""EPA on the GPU (through the C ABI) against the golden vectors and the
+oracle: status, MTV, face count and faces bit for bit."""
+import numpy as np
+import pytest
+
+from distance3d_gb300 import workloads
+from distance3d_gb300.epa import epa_batch, epa_scratch_bytes
+from distance3d_gb300.gjk import gjk_distance_batch
+from distance3d_gb300.store import ColliderStore
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def host(r):
+    return {k: v.cpu().numpy() for k, v in r.items()}
+
+
+@pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))])
+def test_epa_matches_reference_golden(golden, tag, kw):
+    g, cs = golden("gjk_mixed6")
+    e, _ = golden("epa_mixed6")
+    p = e["pair"]
+    r = host(epa_batch(ColliderStore(cs), g["i1"][p], g["i2"][p], g["simplex"][p], **kw))
+    st = e[f"status_{tag}"]
+    assert np.array_equal(r["status"], st)
+    ok = st == 0
+    assert np.array_equal(r["mtv"][ok], e[f"mtv_{tag}"][ok])
+    assert np.array_equal(r["n_faces"][ok], e[f"n_faces_{tag}"][ok])
+
+
+@pytest.mark.parametrize("max_faces,max_edges", [(64, 32), (256, 128)])
+def test_epa_matches_oracle_with_faces(max_faces, max_edges):
+    cs, i1, i2 = workloads.pairs_mixed_six(6000, seed=31, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    st = ColliderStore(cs)
+    g = host(gjk_distance_batch(st, i1, i2))
+    hit = np.flatnonzero(g["dist"] == 0.0)
+    assert len(hit) > 1000
+    kw = dict(max_faces=max_faces, max_loose_edges=max_edges)
+    r = host(epa_batch(st, i1[hit], i2[hit], g["simplex"][hit], return_faces=True, **kw))
+    ref = oracle.epa(cs, i1[hit], i2[hit], g["simplex"][hit], want_faces=True, **kw)
+    assert np.array_equal(r["status"], ref["status"])
+    assert np.array_equal(r["n_faces"], ref["n_faces"])
+    assert np.array_equal(r["mtv"], ref["mtv"], equal_nan=True)
+    for k in range(len(hit)):
+        nf = r["n_faces"][k]
+        assert np.array_equal(r["faces"][k, :nf], ref["faces"][k, :nf])
+
+
+def test_epa_many_pairs_reuse_slots():
+    """More pairs than scratch slots: every pair still gets its own answer."""
+    cs, i1, i2 = workloads.pairs_mixed_six(200000, seed=32, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    st = ColliderStore(cs)
+    g = host(gjk_distance_batch(st, i1, i2))
+    hit = np.flatnonzero(g["dist"] == 0.0)
+    assert len(hit) > 40000
+    r = host(epa_batch(st, i1[hit], i2[hit], g["simplex"][hit], max_faces=256, max_loose_edges=128))
+    sample = np.random.default_rng(1).choice(len(hit), 3000, replace=False)
+    ref = oracle.epa(cs, i1[hit][sample], i2[hit][sample], g["simplex"][hit][sample], max_faces=256,
+                     max_loose_edges=128)
+    assert np.array_equal(r["status"][sample], ref["status"])
+    assert np.array_equal(r["mtv"][sample], ref["mtv"], equal_nan=True)
+    assert epa_scratch_bytes(len(hit), max_faces=256, max_loose_edges=128) < 64 * len(hit) * 12 * 256 * 8
+
+
+def test_epa_edge_cases():
+    cs, i1, i2 = workloads.pairs_mixed_six(16, seed=2)
+    st = ColliderStore(cs)
+    r = epa_batch(st, [], [], np.zeros((0, 4, 3)))
+    assert r["mtv"].shape == (0, 3)
+    # zero iterations: the initial closest face, not converged
+    s = np.random.default_rng(0).normal(size=(4, 4, 3))
+    r = host(epa_batch(st, i1[:4], i2[:4], s, max_iter=0))
+    ref = oracle.epa(cs, i1[:4], i2[:4], s, max_iter=0)
+    assert np.array_equal(r["status"], ref["status"])
+    assert np.array_equal(r["mtv"], ref["mtv"], equal_nan=True)
+    # a degenerate (flat) simplex: whatever the reference does, the same status
+    flat = np.zeros((4, 4, 3))
+    flat[:, :, :2] = np.random.default_rng(1).normal(size=(4, 4, 2))
+    r = host(epa_batch(st, i1[:4], i2[:4], flat))
+    ref = oracle.epa(cs, i1[:4], i2[:4], flat)
+    assert np.array_equal(r["status"], ref["status"])
+    assert np.array_equal(r["mtv"], ref["mtv"], equal_nan=True)
+
+
+def test_drop_in_epa():
+    from distance3d_gb300 import colliders, epa, gjk
+    from tests.test_known_answers import EPA_V1, EPA_V2
+    c1, c2 = colliders.ConvexHullVertices(EPA_V1), colliders.ConvexHullVertices(EPA_V2)
+    d, _, _, simplex = gjk.gjk(c1, c2)
+    assert d == 0.0
+    mtv, faces, success = epa.epa(simplex, c1, c2)
+    assert success
+    assert faces.shape[1:] == (4, 3)
+    np.testing.assert_array_almost_equal(mtv, [-0.387287, 0.179576, -0.176204])

@@ -1,0 +1,190 @@
+"""GJK on the GPU (through the C ABI) against the golden vectors and the
+oracle.
+
+The FP64 form must equal the reference bit for bit: distance, closest
+points, simplex rows, n_simplex, iteration counts, flags.  The mixed form must
+stay within 1e-5 relative distance error of the FP64 oracle, with identical
+intersection flags wherever the distance exceeds 1e-6 (scenes are unit scale,
+so scale = 1).
+"""
+import numpy as np
+import pytest
+import torch
+
+from distance3d_gb300 import workloads
+from distance3d_gb300.gjk import gjk_distance_batch, gjk_intersection_batch
+from distance3d_gb300.store import ColliderStore
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+MIXED_REL_TOL = 1e-5
+FLAG_MARGIN = 1e-6
+
+
+def host(r):
+    return {k: v.cpu().numpy() for k, v in r.items()}
+
+
+def assert_bit_exact(g, ref, written=None):
+    assert np.array_equal(g["dist"], ref["dist"])
+    assert np.array_equal(g["cp1"], ref["cp1"], equal_nan=True)
+    assert np.array_equal(g["cp2"], ref["cp2"], equal_nan=True)
+    assert np.array_equal(g["n_simplex"], ref["n_simplex"])
+    if "iterations" in ref:
+        assert np.array_equal(g["iterations"], ref["iterations"])
+    if written is None:
+        assert np.array_equal(g["simplex"], ref["simplex"])
+    else:
+        assert np.array_equal(g["simplex"][written], ref["simplex"][written])
+
+
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb"])
+def test_fp64_matches_reference_golden(golden, name):
+    g, cs = golden(name)
+    st = ColliderStore(cs)
+    r = host(gjk_distance_batch(st, g["i1"], g["i2"]))
+    assert np.all(r["status"] == 0)
+    assert_bit_exact(r, g, written=~np.isnan(g["simplex"]))
+    h = gjk_intersection_batch(st, g["i1"], g["i2"])
+    assert np.array_equal(h["hit"].cpu().numpy(), g["intersect"])
+    assert np.all(h["status"].cpu().numpy() == 0)
+
+
+@pytest.mark.parametrize("maker,kw", [
+    (workloads.pairs_sphere_capsule_box, {}),
+    (workloads.pairs_mixed_six, {}),
+    (workloads.pairs_mixed_six, dict(center_half_width=workloads.INTERSECT30_HALF_WIDTH)),
+])
+def test_fp64_matches_oracle(maker, kw):
+    cs, i1, i2 = maker(20000, seed=11, **kw)
+    st = ColliderStore(cs)
+    r = host(gjk_distance_batch(st, i1, i2))
+    ref = oracle.gjk_distance(cs, i1, i2)
+    assert_bit_exact(r, ref)
+    assert np.array_equal(r["status"], ref["status"])
+    h = gjk_intersection_batch(st, i1, i2)["hit"].cpu().numpy()
+    assert np.array_equal(h, oracle.gjk_intersection(cs, i1, i2)["hit"])
+
+
+def reference_distance(ref):
+    """The reference's distance where it is self-consistent; where its
+    distance disagrees with its own closest points (Jolt's face-region
+    projection leaving the simplex on a sliver triangle, rare), the separation
+    of those closest points."""
+    sep = np.linalg.norm(ref["cp1"] - ref["cp2"], axis=1)
+    bad = np.abs(sep - ref["dist"]) > 1e-9 * np.maximum(1.0, ref["dist"])
+    return np.where(bad, sep, ref["dist"]), bad
+
+
+def mixed_check(r, ref):
+    want, inconsistent = reference_distance(ref)
+    assert inconsistent.mean() < 1e-3
+    rel = np.abs(r["dist"] - want) / np.maximum(1.0, np.abs(want))
+    assert rel.max() <= MIXED_REL_TOL, f"max rel err {rel.max()}"
+    sep = ref["dist"] > FLAG_MARGIN
+    assert np.array_equal(r["dist"][sep] > 0, ref["dist"][sep] > 0)
+    inter = ref["dist"] == 0.0
+    assert np.all(r["dist"][inter] <= FLAG_MARGIN)
+    # closest points realise the distance
+    gap = np.abs(np.linalg.norm(r["cp1"] - r["cp2"], axis=1) - r["dist"])
+    assert gap.max() <= 1e-6
+    return rel
+
+
+@pytest.mark.parametrize("maker,kw", [
+    (workloads.pairs_sphere_capsule_box, {}),
+    (workloads.pairs_mixed_six, {}),
+    (workloads.pairs_mixed_six, dict(center_half_width=workloads.INTERSECT30_HALF_WIDTH)),
+])
+def test_mixed_within_tolerance(maker, kw):
+    cs, i1, i2 = maker(20000, seed=12, **kw)
+    st = ColliderStore(cs)
+    r = host(gjk_distance_batch(st, i1, i2, precision="mixed"))
+    ref = oracle.gjk_distance(cs, i1, i2)
+    assert np.all(r["status"] == 0)
+    mixed_check(r, ref)
+
+
+def test_mixed_golden(golden):
+    g, cs = golden("gjk_mixed6")
+    r = host(gjk_distance_batch(ColliderStore(cs), g["i1"], g["i2"], precision="mixed"))
+    mixed_check(r, g)
+
+
+def test_edge_cases():
+    cs, i1, i2 = workloads.pairs_mixed_six(64, seed=3)
+    st = ColliderStore(cs)
+    empty = gjk_distance_batch(st, [], [])
+    assert empty["dist"].numel() == 0
+    assert gjk_intersection_batch(st, [], [])["hit"].numel() == 0
+    # every collider against itself: distance 0
+    same = np.arange(len(cs), dtype=np.int32)
+    r = host(gjk_distance_batch(st, same, same))
+    assert np.all(r["dist"] == 0.0)
+    ref = oracle.gjk_distance(cs, same, same)
+    assert_bit_exact(r, ref)
+    # iteration bound: the status says so and the oracle agrees
+    r = host(gjk_distance_batch(st, i1, i2, max_iterations=2))
+    ref = oracle.gjk_distance(cs, i1, i2, max_iter=2)
+    assert np.array_equal(r["status"], ref["status"])
+    assert np.any(r["status"] == 3)
+    assert np.array_equal(r["dist"], ref["dist"])
+
+
+def test_ragged_hulls():
+    """Hulls of 1, 2, 3 and 300 vertices, mixed with every other type."""
+    rng = np.random.default_rng(7)
+    from distance3d_gb300.collider_set import ColliderSet
+    base, _, _ = workloads.pairs_mixed_six(40, seed=8)
+    verts = [rng.normal(size=(n, 3)) * 0.2 for n in (1, 2, 3, 300)]
+    counts = np.array([len(v) for v in verts], np.int32)
+    offs = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    poses = np.tile(np.concatenate([np.eye(3).ravel(), np.zeros(3)]), (4, 1))
+    extra = ColliderSet(np.full(4, 5, np.int32), poses, np.zeros((4, 4)), offs, counts, np.concatenate(verts))
+    cs = ColliderSet.concatenate([base, extra])
+    n = len(cs)
+    i1 = np.repeat(np.arange(n - 4, n), n).astype(np.int32)
+    i2 = np.tile(np.arange(n), 4).astype(np.int32)
+    r = host(gjk_distance_batch(ColliderStore(cs), i1, i2))
+    ref = oracle.gjk_distance(cs, i1, i2)
+    assert_bit_exact(r, ref)
+
+
+def test_full_size_properties():
+    """1,048,576 six-type pairs: oracle-exact on a sample, deterministic, and
+    the closest points realise the distance everywhere."""
+    cs, i1, i2 = workloads.pairs_mixed_six(1 << 20, seed=21, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    st = ColliderStore(cs)
+    a = gjk_distance_batch(st, i1, i2)
+    b = gjk_distance_batch(st, i1, i2)
+    for k in a:
+        assert torch.equal(a[k], b[k]), k
+    r = host(a)
+    assert np.all(r["status"] == 0)
+    assert np.all(r["dist"] >= 0)
+    gap = np.abs(np.linalg.norm(r["cp1"] - r["cp2"], axis=1) - r["dist"])
+    assert gap.max() < 1e-7
+    sample = np.random.default_rng(0).choice(len(i1), 5000, replace=False)
+    ref = oracle.gjk_distance(cs, i1[sample], i2[sample])
+    assert_bit_exact({k: v[sample] for k, v in r.items()}, ref)
+    m = host(gjk_distance_batch(st, i1, i2, precision="mixed"))
+    mixed_check(m, r)
+
+
+def test_drop_in_api_matches_batch():
+    from distance3d_gb300 import colliders, gjk
+    rng = np.random.default_rng(5)
+    pose = np.eye(4)
+    pose[:3, 3] = [0.4, 0.1, -0.2]
+    c1 = colliders.Capsule(pose, 0.2, 0.5)
+    c2 = colliders.ConvexHullVertices(rng.normal(size=(20, 3)) * 0.3 + 1.0)
+    d, p1, p2, s = gjk.gjk(c1, c2)
+    from distance3d_gb300.collider_set import ColliderSet
+    ref = oracle.gjk_distance(ColliderSet.from_colliders([c1, c2]), [0], [1])
+    assert d == ref["dist"][0]
+    assert np.array_equal(p1, ref["cp1"][0]) and np.array_equal(p2, ref["cp2"][0])
+    assert s.shape == (4, 3)
+    assert gjk.gjk_intersection(c1, c2) == (d == 0.0)
+    far = colliders.ConvexHullVertices(np.array([[1e8, 0.0, 0.0]]))
+    assert gjk.gjk(c1, far) == (np.finfo(float).max, None, None, None)

@@ -33,6 +33,7 @@ UNITS = [
     ("epa.cu", ["-fmad=false"]),
     ("gjk_mixed.cu", ["-fmad=true"]),
     ("schedule.cu", []),
+    ("bvh.cu", []),
 ]
 
 

@@ -152,6 +152,40 @@ int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_
             const double* simplex, const d3d_epa_options* options, double* mtv, int8_t* status,
             int32_t* n_faces, double* faces, void* scratch, size_t scratch_bytes, void* stream);
 
+/* ------------------------------------------------------------------ broad phase
+ * A linear BVH over FP64 boxes aabbs[n][3][2] ([axis][min,max]).  The tree
+ * lives in a caller buffer of d3d_bvh_bytes(n) bytes (layout private) and
+ * refers to `aabbs`, which queries must pass again unchanged.  Pair sets equal
+ * the reference's AabbTree / brute-force sets exactly (closed intervals,
+ * aabb_tree.py:504-527). */
+
+size_t d3d_bvh_bytes(int64_t n_leaves);
+
+/* Build (stream-ordered).  Replaces AabbTree.insert_aabbs / insert_aabb
+ * (aabb_tree.py:31-115, insert_leaf :240-341) and the tree rebuild of
+ * BoundingVolumeHierarchy.update_collider_poses (broad_phase.py:144-151). */
+int d3d_bvh_build(const double* aabbs, int64_t n, void* tree, size_t tree_bytes, void* stream);
+
+/* Scratch bytes for a query with room for `capacity` pairs. */
+size_t d3d_bvh_query_bytes(int64_t capacity);
+
+/* All overlapping leaf pairs (i, j), i < j by input index, ascending, into
+ * pairs[capacity][2].  Synchronises the stream once; *n_pairs (host) is the
+ * pair count, and when it exceeds capacity the call returns D3D_ERR_CAPACITY
+ * so that the caller can retry with a larger buffer.  Replaces
+ * AabbTree.overlaps_aabb_tree(self) (aabb_tree.py:121-159, :344-378) as used
+ * by BoundingVolumeHierarchy.aabb_overlapping_with_self (broad_phase.py:229-252). */
+int d3d_bvh_self_pairs(const double* aabbs, int64_t n, const void* tree, int32_t* pairs, int64_t capacity,
+                       int64_t* n_pairs, void* scratch, size_t scratch_bytes, void* stream);
+
+/* All (leaf, query) pairs whose boxes overlap, for query boxes boxes[m][3][2],
+ * ascending by leaf then query.  Same capacity protocol as above.  Replaces
+ * AabbTree.overlaps_aabb (aabb_tree.py:161-181, query_overlap :381-403) and,
+ * with the other tree's boxes as queries, overlaps_aabb_tree(other) /
+ * BoundingVolumeHierarchy.aabb_overlapping_with_other_bvh (broad_phase.py:202-227). */
+int d3d_bvh_query(const double* aabbs, int64_t n, const void* tree, const double* boxes, int64_t m, int32_t* pairs,
+                  int64_t capacity, int64_t* n_pairs, void* scratch, size_t scratch_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

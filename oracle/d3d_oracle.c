@@ -820,3 +820,40 @@ int64_t orc_cross_pairs(const double* a, int64_t na, const double* b, int64_t nb
             }
     return m;
 }
+
+/* Sort-and-sweep restatement of all_aabbs_overlap restricted to i < j
+ * (aabb_tree.py:466-527): the same closed-interval pair set as the brute
+ * force, in O(n log n + candidates).  Pairs come out unsorted; count is
+ * returned, at most cap are written. */
+typedef struct { double lo; int64_t i; } sweep_key;
+
+static int sweep_cmp(const void* a, const void* b) {
+    const sweep_key* x = (const sweep_key*)a;
+    const sweep_key* y = (const sweep_key*)b;
+    if (x->lo < y->lo) return -1;
+    if (x->lo > y->lo) return 1;
+    return (x->i > y->i) - (x->i < y->i);
+}
+
+int64_t orc_self_pairs_sweep(const double* aabbs, int64_t n, int32_t* out, int64_t cap) {
+    sweep_key* k = (sweep_key*)malloc(sizeof(sweep_key) * (size_t)(n > 0 ? n : 1));
+    for (int64_t i = 0; i < n; ++i) { k[i].lo = aabbs[6 * i]; k[i].i = i; }
+    qsort(k, (size_t)n, sizeof(sweep_key), sweep_cmp);
+    int64_t m = 0;
+    for (int64_t a = 0; a < n; ++a) {
+        const int64_t i = k[a].i;
+        const double hx = aabbs[6 * i + 1];
+        for (int64_t b = a + 1; b < n && k[b].lo <= hx; ++b) {
+            const int64_t j = k[b].i;
+            if (aabb_overlap(aabbs + 6 * i, aabbs + 6 * j)) {
+                if (out && m < cap) {
+                    out[2 * m] = (int32_t)(i < j ? i : j);
+                    out[2 * m + 1] = (int32_t)(i < j ? j : i);
+                }
+                ++m;
+            }
+        }
+    }
+    free(k);
+    return m;
+}

@@ -39,6 +39,8 @@ def lib():
         _lib.orc_self_pairs.restype = ctypes.c_int64
         _lib.orc_cross_pairs.argtypes = [DP, ctypes.c_int64, DP, ctypes.c_int64, I32P, ctypes.c_int64]
         _lib.orc_cross_pairs.restype = ctypes.c_int64
+        _lib.orc_self_pairs_sweep.argtypes = [DP, ctypes.c_int64, I32P, ctypes.c_int64]
+        _lib.orc_self_pairs_sweep.restype = ctypes.c_int64
         _lib.orc_max_threads.restype = ctypes.c_int
         _lib.orc_box_vertices.argtypes = [DP, DP, DP]
     return _lib
@@ -142,3 +144,12 @@ def cross_pairs(a, b):
     out = np.empty((n, 2), np.int32)
     lib().orc_cross_pairs(_p(a, DP), len(a), _p(b, DP), len(b), _p(out, I32P), n)
     return out
+
+
+def self_pairs_sweep(aabbs_):
+    """Same pair set as self_pairs (i < j, sorted), by sort and sweep."""
+    a = np.ascontiguousarray(aabbs_, dtype=np.float64).reshape(-1, 3, 2)
+    n = lib().orc_self_pairs_sweep(_p(a, DP), len(a), None, 0)
+    out = np.empty((n, 2), np.int32)
+    lib().orc_self_pairs_sweep(_p(a, DP), len(a), _p(out, I32P), n)
+    return out[np.lexsort((out[:, 1], out[:, 0]))]

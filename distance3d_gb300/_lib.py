@@ -60,6 +60,8 @@ SIGNATURES = [
     ("d3d_epa_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(EpaOptions)]),
     ("d3d_epa", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(EpaOptions),
                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    ("d3d_epa_noalloc", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(EpaOptions),
+                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     ("d3d_bvh_bytes", c_size_t, [c_int64]),
     ("d3d_bvh_build", c_int, [c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
     ("d3d_bvh_query_bytes", c_size_t, [c_int64]),

@@ -17,6 +17,8 @@
 // next one.  Each thread owns one scratch slot of max_faces faces and
 // max_loose_edges edges (d3d_epa_scratch_bytes), reused across its pairs, so
 // the scratch is bounded by the slot count, not by n.
+#include <mutex>
+
 #include "capi_util.h"
 #include "d3d_device.cuh"
 #include "persist.cuh"
@@ -276,4 +278,99 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     }
     d3d::scratch_free(block, st);
     return rc;
+}
+
+// ----------------------------------------------------------------------------
+// EPA without any allocation.
+//
+// For callers that must not allocate device memory once they are running: a
+// control loop with a fixed memory budget, a plugin whose host application
+// owns every allocation on the GPU, or a process that pre-reserves all of its
+// memory at start-up.  d3d_epa needs a caller buffer plus a small temporary
+// from the library's pool; this variant instead keeps the polytope slots and
+// its work counter in one array that is part of the loaded library image, so
+// a call allocates nothing (no cudaMalloc, no pool, no sort temporaries:
+// pairs run in input order).
+//
+// The array is kNoAllocBytes = 16 MiB on every GPU that loads the library,
+// held until the process exits.  It bounds the per-pair polytope, not the
+// number of pairs: each of the array's slots is reused across pairs, and a
+// call fails with D3D_ERR_CAPACITY when a single slot of
+// (12 * max_faces + 6 * max_loose_edges) doubles leaves room for fewer than
+// 128 slots (with the defaults, 64 faces and 32 edges, there are 2,184).
+//
+// Every call shares the array, and the array keeps the previous call's
+// contents (the work counter is cleared on the stream at the start of each
+// call).  Calls whose work overlaps on the GPU -- concurrent streams, or
+// threads sharing a device -- race on it and must be serialised by the
+// caller.
+namespace {
+
+constexpr size_t kNoAllocBytes = size_t(16) << 20;
+constexpr int kMaxNoAllocDevices = 64;
+
+static __device__ __align__(256) unsigned char g_epa_noalloc[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxNoAllocDevices] = {};
+
+// The array's device address for the current device.  The first call on a
+// device (with that device current) looks it up with cudaGetSymbolAddress;
+// host code must never pass the symbol itself to a kernel.
+int noalloc_base(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxNoAllocDevices) {
+        d3d::set_error("d3d_epa_noalloc: no usable current device (%s)", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_epa_noalloc);
+        if (e != cudaSuccess || p == nullptr) {
+            d3d::set_error("d3d_epa_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return D3D_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return D3D_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                               const double* simplex, const d3d_epa_options* options, double* mtv, int8_t* status,
+                               int32_t* n_faces, double* faces, void* stream) {
+    int rc = d3d::check_store(store, "d3d_epa_noalloc");
+    if (rc) return rc;
+    D3D_REQUIRE(valid(options), "d3d_epa_noalloc: invalid options (need max_faces >= 4, limits >= 0, epsilon >= 0)");
+    D3D_REQUIRE(n >= 0, "d3d_epa_noalloc: n < 0");
+    const int64_t slot_bytes = slot_doubles(*options) * (int64_t)sizeof(double);
+    const int64_t slots = (int64_t)(kNoAllocBytes - 256) / slot_bytes;
+    if (slots < kBlock) {
+        d3d::set_error("d3d_epa_noalloc: max_faces=%d, max_loose_edges=%d need %lld bytes per pair; the static "
+                       "scratch of %zu bytes holds fewer than %d pairs at a time (use d3d_epa)",
+                       options->max_faces, options->max_loose_edges, (long long)slot_bytes, kNoAllocBytes, kBlock);
+        return D3D_ERR_CAPACITY;
+    }
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(i1 && i2 && simplex && mtv && status && n_faces, "d3d_epa_noalloc: null pointer");
+    void* base = nullptr;
+    rc = noalloc_base(&base);
+    if (rc) return rc;
+    cudaStream_t st = d3d::as_stream(stream);
+    unsigned long long* cursor = static_cast<unsigned long long*>(base);
+    double* slot_mem = reinterpret_cast<double*>(static_cast<char*>(base) + 256);
+    cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) {
+        d3d::set_error("d3d_epa_noalloc: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
+    if (blocks > slots / kBlock) blocks = (int)(slots / kBlock);
+    k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, nullptr, n, cursor, simplex, *options, mtv, status, n_faces, faces,
+                                     slot_mem, slot_doubles(*options));
+    return d3d::check_launch("d3d_epa_noalloc");
 }

@@ -32,7 +32,7 @@ class GjkOptions(ctypes.Structure):
 
 class EpaOptions(ctypes.Structure):
     _fields_ = [("max_iterations", c_int32), ("max_loose_edges", c_int32), ("max_faces", c_int32),
-                ("reserved", c_int32), ("epsilon", c_double)]
+                ("precision", c_int32), ("epsilon", c_double)]
 
 
 class D3DError(RuntimeError):

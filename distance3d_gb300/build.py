@@ -32,6 +32,7 @@ UNITS = [
     ("gjk.cu", ["-fmad=false"]),
     ("epa.cu", ["-fmad=false"]),
     ("gjk_mixed.cu", ["-fmad=true"]),
+    ("epa_mixed.cu", ["-fmad=true"]),
     ("schedule.cu", []),
     ("bvh.cu", []),
 ]

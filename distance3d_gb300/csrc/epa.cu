@@ -21,6 +21,7 @@
 
 #include "capi_util.h"
 #include "d3d_device.cuh"
+#include "epa_mixed.h"
 #include "persist.cuh"
 #include "scratch.h"
 
@@ -179,11 +180,13 @@ __device__ __forceinline__ int epa_step(EpaLoop& L, const Col<double>& c1, const
 
 __global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __restrict__ i1,
                                                 const int32_t* __restrict__ i2, const int32_t* __restrict__ order,
-                                                int64_t n, unsigned long long* __restrict__ cursor,
+                                                int64_t n, const unsigned long long* __restrict__ n_dev,
+                                                unsigned long long* __restrict__ cursor,
                                                 const double* __restrict__ simplex, d3d_epa_options o,
                                                 double* __restrict__ mtv, int8_t* __restrict__ status,
                                                 int32_t* __restrict__ n_faces, double* __restrict__ faces,
                                                 double* __restrict__ scratch, int64_t slot_doubles) {
+    if (n_dev) n = (int64_t)*n_dev;
     const int64_t slot = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double* F = scratch + slot * slot_doubles;
     double* E = F + 12 * (int64_t)o.max_faces;
@@ -226,20 +229,29 @@ int64_t slot_doubles(const d3d_epa_options& o) {
     return 12 * (int64_t)o.max_faces + 6 * (int64_t)o.max_loose_edges;
 }
 
+// the mixed form also runs the FP64 kernel on its fallback pairs
+int64_t slot_bytes_for(const d3d_epa_options& o) {
+    const int64_t f64 = slot_doubles(o) * (int64_t)sizeof(double);
+    if (o.precision != D3D_PRECISION_MIXED) return f64;
+    const int64_t mixed = d3d::epa_mixed_slot_bytes(o);
+    return mixed > f64 ? mixed : f64;
+}
+
 int64_t slots_for(int64_t n) {
     int64_t s = n < kMaxSlots ? n : kMaxSlots;
     return ((s + kBlock - 1) / kBlock) * kBlock;
 }
 
 bool valid(const d3d_epa_options* o) {
-    return o && o->max_iterations >= 0 && o->max_faces >= 4 && o->max_loose_edges >= 0 && o->epsilon >= 0.0;
+    return o && o->max_iterations >= 0 && o->max_faces >= 4 && o->max_loose_edges >= 0 && o->epsilon >= 0.0 &&
+           (o->precision == D3D_PRECISION_FP64 || o->precision == D3D_PRECISION_MIXED);
 }
 
 }  // namespace
 
 extern "C" size_t d3d_epa_scratch_bytes(int64_t n, const d3d_epa_options* options) {
     if (!valid(options) || n <= 0) return 0;
-    return (size_t)(slots_for(n) * slot_doubles(*options) * (int64_t)sizeof(double));
+    return (size_t)(slots_for(n) * slot_bytes_for(*options));
 }
 
 extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n, const double* simplex,
@@ -257,23 +269,32 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
         return D3D_ERR_CAPACITY;
     }
     cudaStream_t st = d3d::as_stream(stream);
+    const bool mixed = options->precision == D3D_PRECISION_MIXED;
     const bool sched = n >= kScheduleMin;
-    const size_t order_bytes = sched ? ((sizeof(int32_t) * (size_t)n + 255) & ~size_t(255)) : 0;
+    const size_t up_n = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
+    const size_t order_bytes = sched ? up_n : 0;
+    const size_t fb_bytes = mixed ? up_n : 0;
     const size_t temp_bytes = sched ? d3d::pair_order_temp_bytes(n) : 0;
     void* block = nullptr;
-    rc = d3d::scratch_alloc(&block, 256 + order_bytes + temp_bytes, st);
+    rc = d3d::scratch_alloc(&block, 256 + order_bytes + fb_bytes + temp_bytes, st);
     if (rc) return rc;
-    unsigned long long* cursor = static_cast<unsigned long long*>(block);
-    int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(block) + 256) : nullptr;
-    cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
-    if (sched)
-        rc = d3d::pair_order(*store, i1, i2, n, order, static_cast<char*>(block) + 256 + order_bytes, temp_bytes, st);
+    char* p = static_cast<char*>(block);
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(p);  // cursor, fallback cursor, fallback count
+    int32_t* order = sched ? reinterpret_cast<int32_t*>(p + 256) : nullptr;
+    int32_t* fallback = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes) : nullptr;
+    cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned long long), st);
+    if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, p + 256 + order_bytes + fb_bytes, temp_bytes, st);
+    if (!rc && mixed)
+        rc = d3d::epa_mixed_launch(*store, i1, i2, order, n, ctr, simplex, *options, mtv, status, n_faces, faces,
+                                   scratch, slots_for(n), fallback, ctr + 2, st);
     if (!rc) {
+        // the FP64 EPA: every pair, or the mixed form's fallback pairs
         int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
         const int64_t max_blocks = slots_for(n) / kBlock;  // the scratch holds this many slots
         if (blocks > max_blocks) blocks = (int)max_blocks;
-        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, order, n, cursor, simplex, *options, mtv, status, n_faces,
-                                         faces, static_cast<double*>(scratch), slot_doubles(*options));
+        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, mixed ? fallback : order, n, mixed ? ctr + 2 : nullptr,
+                                         mixed ? ctr + 1 : ctr, simplex, *options, mtv, status, n_faces, faces,
+                                         static_cast<double*>(scratch), slot_doubles(*options));
         rc = d3d::check_launch("d3d_epa");
     }
     d3d::scratch_free(block, st);
@@ -345,7 +366,8 @@ extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const 
                                int32_t* n_faces, double* faces, void* stream) {
     int rc = d3d::check_store(store, "d3d_epa_noalloc");
     if (rc) return rc;
-    D3D_REQUIRE(valid(options), "d3d_epa_noalloc: invalid options (need max_faces >= 4, limits >= 0, epsilon >= 0)");
+    D3D_REQUIRE(valid(options) && options->precision == D3D_PRECISION_FP64,
+                "d3d_epa_noalloc: invalid options (need the FP64 form, max_faces >= 4, limits >= 0, epsilon >= 0)");
     D3D_REQUIRE(n >= 0, "d3d_epa_noalloc: n < 0");
     const int64_t slot_bytes = slot_doubles(*options) * (int64_t)sizeof(double);
     const int64_t slots = (int64_t)(kNoAllocBytes - 256) / slot_bytes;
@@ -370,7 +392,7 @@ extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const 
     }
     int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
     if (blocks > slots / kBlock) blocks = (int)(slots / kBlock);
-    k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, nullptr, n, cursor, simplex, *options, mtv, status, n_faces, faces,
-                                     slot_mem, slot_doubles(*options));
+    k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, nullptr, n, nullptr, cursor, simplex, *options, mtv, status,
+                                     n_faces, faces, slot_mem, slot_doubles(*options));
     return d3d::check_launch("d3d_epa_noalloc");
 }

@@ -1,0 +1,25 @@
+// epa_mixed.h -- the mixed-precision EPA launcher (epa_mixed.cu), used by
+// d3d_epa when options->precision is D3D_PRECISION_MIXED.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "d3d_gb300.h"
+
+namespace d3d {
+
+// bytes of one polytope slot: (max_iterations + 4) vertices and max_faces
+// faces of 32 bytes, max_loose_edges edges of 8 bytes, a max_faces queue of
+// 4 bytes (rounded up to 16)
+int64_t epa_mixed_slot_bytes(const d3d_epa_options& o);
+
+// persistent launch over `order` (null: input order); at most max_slots
+// threads, each owning slot max_slots-aligned in `scratch`
+// Pairs whose FP32 polytope fails validation are appended to fallback[]
+// (count in *n_fallback) for the FP64 EPA.
+int epa_mixed_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
+                     unsigned long long* cursor, const double* simplex, const d3d_epa_options& o, double* mtv,
+                     int8_t* status, int32_t* n_faces, double* faces, void* scratch, int64_t max_slots,
+                     int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream);
+
+}  // namespace d3d

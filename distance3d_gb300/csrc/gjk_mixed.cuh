@@ -7,14 +7,39 @@
 
 namespace d3d {
 
-// FP64 support for phase B: polytopes choose their vertex by an FP32 argmax
-// and return the FP64 vertex; the smooth shapes use their FP64 functions.
+// FP64 support for the refinement phases.  Wherever the support function is
+// discontinuous -- the vertex of a polytope, the end of a capsule or a
+// cylinder (local z of the direction near 0) -- the choice is made in FP32,
+// exactly as the FP32 phase makes it (the FP32 record is the FP64 one
+// rounded, so its values are recomputed from the FP64 record here), and only
+// the point itself is evaluated in FP64.  A row re-evaluated along the
+// direction that produced it in FP32 therefore lands on the same feature; near
+// a discontinuity both features are supports to within the FP32 rounding of
+// the direction.
 struct RefineSupport {
     static __device__ __forceinline__ d3 eval(const Col<double>& c, const d3d_store& s, d3 d) {
+        const f3 df = mk(__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z));
         if (c.type == D3D_BOX || c.type == D3D_HULL) {
             if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
-            f3 df = mk(__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z));
             return load_vertex(s.verts64, c.off + hull_argmax(s.verts32, c.off, c.nv, df));
+        }
+        if (c.type == D3D_CAPSULE || c.type == D3D_CYLINDER) {
+            // local z of the direction as the FP32 support computes it
+            const float lz = dot102(__double2float_rn(c.R[2]), __double2float_rn(c.R[5]),
+                                    __double2float_rn(c.R[8]), df.x, df.y, df.z);
+            const bool up = c.type == D3D_CAPSULE ? lz > 0.f : !(lz < 0.f);
+            const d3 l = rt_mul(c.R, d);
+            d3 v;
+            if (c.type == D3D_CAPSULE) {
+                const double sn = sqrt(l.x * l.x + l.y * l.y + l.z * l.z);
+                v = sn == 0.0 ? mk(c.p[0], 0.0, 0.0) : l * (c.p[0] / sn);
+                v.z += up ? 0.5 * c.p[1] : -0.5 * c.p[1];
+            } else {
+                const double sn = sqrt(l.x * l.x + l.y * l.y);
+                const double z = up ? 0.5 * c.p[1] : -0.5 * c.p[1];
+                v = sn == 0.0 ? mk(c.p[0], 0.0, z) : mk(l.x * (c.p[0] / sn), l.y * (c.p[0] / sn), z);
+            }
+            return xform(c.R, c.t, v);
         }
         return support(c, s.verts64, d);
     }

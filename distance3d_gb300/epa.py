@@ -17,25 +17,33 @@ from .collider_set import ColliderSet
 from .store import ColliderStore, as_index, _ptr
 
 
-def _options(max_iter, max_loose_edges, max_faces, epsilon):
+_PRECISIONS = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}
+
+
+def _options(max_iter, max_loose_edges, max_faces, epsilon, precision="fp64"):
     if max_faces < 4:
         raise ValueError("max_faces must be >= 4")
-    return _lib.EpaOptions(int(max_iter), int(max_loose_edges), int(max_faces), 0, float(epsilon))
+    if precision not in _PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
+    return _lib.EpaOptions(int(max_iter), int(max_loose_edges), int(max_faces), _PRECISIONS[precision],
+                           float(epsilon))
 
 
 def epa_batch(store, i1, i2, simplex, *, max_iter=64, max_loose_edges=32, max_faces=64, epsilon=1e-8,
-              return_faces=False, scratch=None):
+              return_faces=False, scratch=None, precision="fp64"):
     """EPA for pairs (i1[k], i2[k]) starting from GJK simplices (n,4,3).
 
     Returns a dict of device tensors: ``mtv`` (n,3), ``status`` (n,) int8
     (0 converged, 4 max_iter, 5 face overflow, 6 degenerate), ``n_faces``
     (n,) int32 and, with ``return_faces``, ``faces`` (n,max_faces,4,3) whose
     first n_faces rows are valid.  ``scratch`` may pass a uint8 device tensor
-    of at least ``epa_scratch_bytes(n, ...)`` bytes.
+    of at least ``epa_scratch_bytes(n, ...)`` bytes.  ``precision="fp64"``
+    reproduces the reference bit for bit; ``"mixed"`` searches the polytope in
+    FP32 and refines the final face in FP64.
     """
     dev = store.device
     lib = _lib.load()
-    opt = _options(max_iter, max_loose_edges, max_faces, epsilon)
+    opt = _options(max_iter, max_loose_edges, max_faces, epsilon, precision)
     with torch.cuda.device(dev):
         a = as_index(i1, dev)
         b = as_index(i2, dev)
@@ -57,9 +65,9 @@ def epa_batch(store, i1, i2, simplex, *, max_iter=64, max_loose_edges=32, max_fa
         return out
 
 
-def epa_scratch_bytes(n, max_iter=64, max_loose_edges=32, max_faces=64, epsilon=1e-8):
+def epa_scratch_bytes(n, max_iter=64, max_loose_edges=32, max_faces=64, epsilon=1e-8, precision="fp64"):
     return int(_lib.load().d3d_epa_scratch_bytes(n, ctypes.byref(
-        _options(max_iter, max_loose_edges, max_faces, epsilon))))
+        _options(max_iter, max_loose_edges, max_faces, epsilon, precision))))
 
 
 def epa(simplex, collider1, collider2, max_iter=64, max_loose_edges=32, max_faces=64, epsilon=1e-8):

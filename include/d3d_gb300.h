@@ -88,7 +88,8 @@ typedef struct d3d_epa_options {
     int32_t max_iterations;   /* 64 (epa.py:9) */
     int32_t max_loose_edges;  /* 32 */
     int32_t max_faces;        /* 64 */
-    int32_t reserved;
+    int32_t precision;        /* D3D_PRECISION_FP64 (the reference, bit for bit) or D3D_PRECISION_MIXED
+                                 (FP32 polytope search, FP64 refinement of the final face) */
     double epsilon;           /* 1e-8 */
 } d3d_epa_options;
 
@@ -145,9 +146,10 @@ int d3d_gjk_intersection(const d3d_store* store, const int32_t* i1, const int32_
 size_t d3d_epa_scratch_bytes(int64_t n, const d3d_epa_options* options);
 
 /* Batched EPA on GJK simplices simplex[n][4][3].  Outputs mtv[n][3],
- * status[n], n_faces[n], faces[n][max_faces][4][3] (may be NULL).  `scratch`
- * holds the polytopes (d3d_epa_scratch_bytes).  Replaces epa.epa, epa.py:9-78
- * (Polytope :81-146, LooseEdges :149-202). */
+ * status[n], n_faces[n], faces[n][max_faces][4][3] (may be NULL; in the mixed
+ * form the FP32 polytope).  `scratch` holds the polytopes
+ * (d3d_epa_scratch_bytes).  Replaces epa.epa, epa.py:9-78 (Polytope :81-146,
+ * LooseEdges :149-202). */
 int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
             const double* simplex, const d3d_epa_options* options, double* mtv, int8_t* status,
             int32_t* n_faces, double* faces, void* scratch, size_t scratch_bytes, void* stream);

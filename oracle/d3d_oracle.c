@@ -857,3 +857,16 @@ int64_t orc_self_pairs_sweep(const double* aabbs, int64_t n, int32_t* out, int64
     free(k);
     return m;
 }
+
+/* Support points of colliders idx[k] along dirs[k] (FP64, the reference's
+ * support functions), in parallel. */
+void orc_support_batch(SET_ARGS, const int32_t* idx, const double* dirs, int64_t n, double* out, int nthreads) {
+    set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < n; ++k) {
+        collider c;
+        load_collider(&c, idx[k], SET_PASS);
+        v3 r = support(&c, mk(dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2]));
+        out[3 * k] = r.x; out[3 * k + 1] = r.y; out[3 * k + 2] = r.z;
+    }
+}

@@ -41,6 +41,7 @@ def lib():
         _lib.orc_cross_pairs.restype = ctypes.c_int64
         _lib.orc_self_pairs_sweep.argtypes = [DP, ctypes.c_int64, I32P, ctypes.c_int64]
         _lib.orc_self_pairs_sweep.restype = ctypes.c_int64
+        _lib.orc_support_batch.argtypes = _set_args + [I32P, DP, ctypes.c_int64, DP, ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
         _lib.orc_box_vertices.argtypes = [DP, DP, DP]
     return _lib
@@ -153,3 +154,32 @@ def self_pairs_sweep(aabbs_):
     out = np.empty((n, 2), np.int32)
     lib().orc_self_pairs_sweep(_p(a, DP), len(a), _p(out, I32P), n)
     return out[np.lexsort((out[:, 1], out[:, 0]))]
+
+
+def support_batch(cs, idx, directions, nthreads=0):
+    """(n,3) support points of colliders idx[k] along directions[k]."""
+    idx = _idx(idx)
+    d = np.ascontiguousarray(directions, dtype=np.float64).reshape(-1, 3)
+    out = np.empty((len(idx), 3))
+    lib().orc_support_batch(*_set(cs), _p(idx, I32P), _p(d, DP), len(idx), _p(out, DP), nthreads)
+    return out
+
+
+def distance_bracket(cs, i1, i2, cp1, cp2):
+    """Certified bracket of the GJK distance from a candidate pair of points:
+    ub = |cp1 - cp2| (the points are convex combinations of support points,
+    so inside the shapes) and lb = u . (s1(-u) - s2(u)) with u the unit
+    direction cp1 - cp2 (the support-function lower bound).  Returns (lb, ub)."""
+    v = np.asarray(cp1) - np.asarray(cp2)
+    ub = np.linalg.norm(v, axis=1)
+    u = v / np.maximum(ub, 1e-300)[:, None]
+    w = support_batch(cs, i1, -u) - support_batch(cs, i2, u)
+    return np.sum(u * w, axis=1), ub
+
+
+def depth_upper_bound(cs, i1, i2, normals):
+    """h(n) = n . (s1(n) - s2(-n)) for unit normals: an upper bound on the
+    penetration depth for every n (the depth is its minimum over n)."""
+    n = np.asarray(normals, dtype=np.float64)
+    w = support_batch(cs, i1, n) - support_batch(cs, i2, -n)
+    return np.sum(n * w, axis=1)

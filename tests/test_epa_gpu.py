@@ -93,3 +93,51 @@ def test_drop_in_epa():
     assert success
     assert faces.shape[1:] == (4, 3)
     np.testing.assert_array_almost_equal(mtv, [-0.387287, 0.179576, -0.176204])
+
+
+MIXED_DEPTH_TOL = 1e-5  # |depth_mixed - depth_fp64| / max(1, depth_fp64)
+
+
+def check_mixed_depths(cs, i1, i2, m, ref):
+    """Mixed EPA depths against the FP64 reference.
+
+    Both forms return h(n) = n . (s1(n) - s2(-n)) for their final normal n,
+    an upper bound on the true penetration depth for every n.  The mixed depth
+    must never exceed the reference's by more than the tolerance; where the
+    reference's exceeds the mixed one, h(n_mixed) -- recomputed here with the
+    oracle's exact supports -- proves that the reference's depth is not the
+    minimum (the reference's EPA keeps degenerate faces after its
+    orientation fix, epa.py:139-146, and can stop on a wrong face)."""
+    both = (m["status"] == 0) & (ref["status"] == 0)
+    dm = np.linalg.norm(m["mtv"][both], axis=1)
+    dr = np.linalg.norm(ref["mtv"][both], axis=1)
+    tol = MIXED_DEPTH_TOL * np.maximum(1.0, dr)
+    assert np.all(dm <= dr + tol), f"mixed deeper than the reference by {np.max(dm - dr)}"
+    wrong = dr > dm + tol
+    if wrong.any():
+        n = m["mtv"][both][wrong] / dm[wrong, None]
+        h = oracle.depth_upper_bound(cs, i1[both][wrong], i2[both][wrong], n)
+        assert np.all(np.abs(h - dm[wrong]) <= 1e-7 * np.maximum(1.0, dm[wrong]))
+        assert np.all(h < dr[wrong] - tol[wrong])
+    assert wrong.mean() < 2e-3
+    return both, wrong
+
+
+@pytest.mark.parametrize("max_faces,max_edges", [(64, 32), (256, 128)])
+def test_mixed_epa_within_tolerance(max_faces, max_edges):
+    cs, i1, i2 = workloads.pairs_mixed_six(30000, seed=33, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    st = ColliderStore(cs)
+    g = host(gjk_distance_batch(st, i1, i2))
+    hit = np.flatnonzero(g["dist"] == 0.0)
+    kw = dict(max_faces=max_faces, max_loose_edges=max_edges)
+    m = host(epa_batch(st, i1[hit], i2[hit], g["simplex"][hit], precision="mixed", **kw))
+    ref = oracle.epa(cs, i1[hit], i2[hit], g["simplex"][hit], **kw)
+    # exact topology (vertex ids) keeps the mixed search converging about as often
+    assert (m["status"] == 0).sum() >= 0.99 * (ref["status"] == 0).sum()
+    both, wrong = check_mixed_depths(cs, i1[hit], i2[hit], m, ref)
+    assert both.sum() > 0.9 * (ref["status"] == 0).sum()
+    dm = np.linalg.norm(m["mtv"][both], axis=1)
+    dr = np.linalg.norm(ref["mtv"][both], axis=1)
+    cosang = np.sum(m["mtv"][both] * ref["mtv"][both], axis=1) / np.maximum(dm * dr, 1e-300)
+    ok = ~wrong & (dr > 1e-3)
+    assert np.all(cosang[ok] > 1 - 1e-6)

@@ -43,6 +43,15 @@ EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 # status 1 = 154 B; EPA: mtv 24 + status 1 + face count 4 per intersecting pair.
 REC64, REC32, OUT_GJK, OUT_EPA = 124, 64, 154, 29
 
+# Flop model of one GJK iteration (FMA = 2), fixed before any flop rate was
+# measured and not tuned since: support function by collider type (sphere,
+# capsule, box as an 8-vertex hull, cylinder, ellipsoid; a hull costs 6 per
+# vertex) plus an average closest-point solve (line ~20, triangle ~80,
+# tetrahedron ~400, weighted by how often each occurs: 150).
+SUPPORT_FLOPS = [12, 50, 48, 50, 50]
+HULL_FLOPS_PER_VERTEX = 6
+SOLVE_FLOPS = 150
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -77,6 +86,34 @@ def algorithmic_bytes(cs, i1, n_epa, precision):
     n = len(i1)
     inputs = 2 * n * rec + per_vertex * float(nv[hull].sum()) + 8 * n  # + the two int32 indices
     return inputs + OUT_GJK * n + OUT_EPA * n_epa
+
+
+def measure_pipe_peaks(dev):
+    """FP64 and FP32 FMA throughput (FLOP/s) of this GPU, measured by the
+    probe library built beside libd3d_gb300 (8 independent FMA chains per
+    thread, SMs x 8 blocks of 256 threads)."""
+    import ctypes
+    import torch
+    from distance3d_gb300 import build as b
+    lib = ctypes.CDLL(b.PEAK_LIB)
+    lib.d3d_peak_fma_flops.restype = ctypes.c_double
+    lib.d3d_peak_fma_flops.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    st = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    fp64 = max(lib.d3d_peak_fma_flops(1, 4096, st) for _ in range(3))
+    fp32 = max(lib.d3d_peak_fma_flops(0, 65536, st) for _ in range(3))
+    return fp64, fp32
+
+
+def gjk_model_flops(cs, i1, i2, iterations):
+    """Model FLOPs of the plain GJK over all pairs, from the per-pair
+    iteration counts (exact: the FP64 kernel reports them)."""
+    cost = np.zeros(len(cs))
+    for t, f in enumerate(SUPPORT_FLOPS):
+        cost[cs.types == t] = f
+    hull = cs.types == 5
+    cost[hull] = HULL_FLOPS_PER_VERTEX * cs.hull_count[hull]
+    per_iter = cost[i1] + cost[i2] + SOLVE_FLOPS
+    return float(np.sum(per_iter * iterations))
 
 
 class ClockSampler:
@@ -353,13 +390,25 @@ def run_ours(args):
     fp64_value = world * n * args.steps / t_fp64
     e2e_value = world * n * args.steps / t_e2e
 
+    # compute roofline of the plain FP64 GJK kernel (one kernel per call):
+    # model FLOPs from its exact iteration counts / event-timed duration,
+    # against the measured FP64 FMA peak
+    peak64, peak32 = measure_pipe_peaks(dev)
+    gf = out_fp64[0]
+    flops64 = gjk_model_flops(cs, i1_np, i2_np, gf["iterations"].cpu().numpy())
+    compute_roofline = {"kernel": "k_gjk_distance_f64", "bound": "fp64 pipe",
+                        "model_flops_per_launch": flops64, "achieved_tflops": flops64 / gjk_fp64 / 1e12,
+                        "peak_tflops": peak64 / 1e12, "frac": flops64 / gjk_fp64 / peak64,
+                        "peak_source": "measured in this run (FMA chains, libd3d_peak)",
+                        "fp32_peak_tflops": peak32 / 1e12}
+
     # roofline: the dominant kernel of the mixed step
     gjk_bytes = algorithmic_bytes(cs, i1_np, 0, "mixed") - OUT_EPA * 0
     epa_bytes = n_epa * (2 * REC64 + OUT_EPA + 96)
     if gjk_mixed >= epa_mixed:
-        dom, t_dom, bytes_dom = "k_gjk_distance_mixed", gjk_mixed, gjk_bytes
+        dom, t_dom, bytes_dom = "d3d_gjk_distance mixed (k_gjk_mixed_a, k_gjk_mixed_b)", gjk_mixed, gjk_bytes
     else:
-        dom, t_dom, bytes_dom = "k_epa", epa_mixed, epa_bytes
+        dom, t_dom, bytes_dom = "d3d_epa mixed (k_epa_mixed)", epa_mixed, epa_bytes
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -391,6 +440,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": None,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
+            "compute_roofline": compute_roofline,
             "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{cpu_pairs} pairs ({cpu_s:.1f} s) of the same workload, "
                                        "GJK + EPA, C restatement with OpenMP"},

@@ -20,6 +20,9 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libd3d_gb300.so")
+# FMA-throughput probe used by bench.py to measure the FP64/FP32 pipe peaks
+PEAK_LIB = os.path.join(BUILD, "libd3d_peak.so")
+PEAK_SRC = os.path.join(CSRC, "bench", "peak.cu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
@@ -49,7 +52,7 @@ def nvcc():
 
 def _inputs_digest():
     h = hashlib.sha256()
-    for d in (CSRC, INCLUDE):
+    for d in (CSRC, INCLUDE, os.path.join(CSRC, "bench")):
         for name in sorted(os.listdir(d)):
             if name.endswith((".cu", ".cuh", ".h")):
                 with open(os.path.join(d, name), "rb") as f:
@@ -97,6 +100,11 @@ def build(force=False, verbose=False, ptxas_verbose=False):
     if p.returncode != 0:
         raise RuntimeError(f"link failed:\n{p.stdout}\n{p.stderr}")
     os.replace(tmp, LIB)
+    p = subprocess.run([cc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-cudart", "static",
+                        PEAK_SRC, "-o", PEAK_LIB + ".tmp"], capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {PEAK_SRC}:\n{p.stdout}\n{p.stderr}")
+    os.replace(PEAK_LIB + ".tmp", PEAK_LIB)
     with open(stamp, "w") as f:
         f.write(digest)
     return LIB

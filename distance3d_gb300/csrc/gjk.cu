@@ -26,10 +26,12 @@ __global__ void __launch_bounds__(kBlock) k_gjk_distance_f64(d3d_store s, const 
                                                             const unsigned long long* __restrict__ n_dev,
                                                             unsigned long long* __restrict__ cursor,
                                                             d3d_gjk_options opt, DistanceOut o) {
+    __shared__ double rows[24 * kBlock];  // the simplex P/Q rows of each lane
     if (n_dev) n = (int64_t)*n_dev;
     const JoltEps<double> E = reference_eps<double>();
     const double tol_sq = opt.tolerance * opt.tolerance;
-    GjkLoop<double> g;
+    GjkLoop<double, SmemRows<double, kBlock>> g;
+    g.S.R.base = rows + threadIdx.x;
     int64_t pid = 0;
     int a = 0, b = 0;
     bool need = true;
@@ -45,12 +47,7 @@ __global__ void __launch_bounds__(kBlock) k_gjk_distance_f64(d3d_store s, const 
             gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
             need = false;
         }
-        // collider records are re-read every round (L1-resident) so that
-        // they hold no registers across the simplex solve
-        Col<double> c1, c2;
-        load_col(s, a, c1);
-        load_col(s, b, c2);
-        if (gjk_step<double>(g, c1, c2, s, tol_sq, opt.max_distance_squared, opt.max_iterations, E)) {
+        if (gjk_step<double>(g, s, a, b, tol_sq, opt.max_distance_squared, opt.max_iterations, E)) {
             GjkResult<double> r;
             gjk_end(g, opt.sanity_check, E, r);
             store_result(o, pid, r, g.S);
@@ -65,12 +62,9 @@ __global__ void __launch_bounds__(128) k_gjk_intersection_f64(d3d_store s, const
                                                               int8_t* __restrict__ status) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    Col<double> c1, c2;
-    load_col(s, i1[k], c1);
-    load_col(s, i2[k], c2);
     JoltEps<double> E = reference_eps<double>();
     int st;
-    hit[k] = (int8_t)gjk_intersection_loop(c1, c2, s, tol_sq, max_iter, E, st);
+    hit[k] = (int8_t)gjk_intersection_loop(s, i1[k], i2[k], tol_sq, max_iter, E, st);
     status[k] = (int8_t)st;
 }
 

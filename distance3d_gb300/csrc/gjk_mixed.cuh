@@ -47,7 +47,7 @@ struct RefineSupport {
 
 // Relative duality gap at which phase B stops; it bounds the relative
 // distance error of the mixed form (apart from the FP32 vertex choice).
-constexpr double kMixedRelGap = 1e-9;
+constexpr double kMixedRelGap = 1e-8;
 
 __device__ __forceinline__ JoltEps<float> fp32_eps() {
     const float e = FLT_EPSILON;
@@ -68,7 +68,7 @@ struct __align__(16) Handoff {
 
 __device__ __forceinline__ int handoff_outcome(const Handoff& h) { return __float_as_int(h.v.w) & 0xff; }
 __device__ __forceinline__ int handoff_rows(const Handoff& h) { return (__float_as_int(h.v.w) >> 8) & 0xff; }
-__device__ __forceinline__ int handoff_iters(const Handoff& h) { return (__float_as_int(h.v.w) >> 16) & 0xffff; }
+__device__ __forceinline__ int handoff_iters(float4 v) { return (__float_as_int(v.w) >> 16) & 0xffff; }
 
 // ---------------------------------------------------------------- phase A
 // The Jolt loop (gjk_step) in FP32 on the FP32 mirror; row j of S.P holds
@@ -91,13 +91,13 @@ __device__ __forceinline__ void pa_begin(PhaseALoop& L) {
 }
 
 // one iteration; -1 while running, else a PhaseAOutcome
-__device__ __forceinline__ int pa_step(PhaseALoop& L, const Col<float>& c1, const Col<float>& c2, const d3d_store& s,
-                                       float tol_sq, float max_d2, int max_iter) {
+__device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a, int b, float tol_sq, float max_d2,
+                                       int max_iter) {
     const JoltEps<float> E = fp32_eps();
     if (L.it >= max_iter) return PA_FAILED;
     ++L.it;
-    f3 p = support(c1, s.verts32, L.dir);
-    f3 q = support(c2, s.verts32, -L.dir);
+    f3 p, q;
+    pair_supports<float, ExactSupport>(s, a, b, L.dir, p, q);
     f3 w = p - q;
     float dd = dot(L.dir, w);
     if (dd < 0.f && dd * dd > L.vl * max_d2) return PA_CLIPPED;
@@ -128,47 +128,72 @@ __device__ __forceinline__ Handoff pa_handoff(const PhaseALoop& L, int outcome) 
     int it = L.it < 0xffff ? L.it : 0xffff;
     h.v = make_float4(L.v.x, L.v.y, L.v.z, __int_as_float(outcome | (L.S.n << 8) | (it << 16)));
 #pragma unroll
-    for (int j = 0; j < 4; ++j) h.d[j] = make_float4(L.S.P[j].x, L.S.P[j].y, L.S.P[j].z, 0.f);
+    for (int j = 0; j < 4; ++j) h.d[j] = make_float4(L.S.R.P[j].x, L.S.R.P[j].y, L.S.R.P[j].z, 0.f);
     return h;
 }
 
 // ---------------------------------------------------------------- phase B
 enum PhaseBMode { PB_RUN = 0, PB_DONE = 1, PB_FALLBACK = 2 };
 
-// Start phase B for one pair.  Separated pairs: the reference's loop from the
-// FP32 closest point's direction instead of (1,0,0), stopped by the duality
-// gap.  Touching pairs: the FP32 simplex rows re-evaluated in FP64 along the
-// directions that produced them; if that simplex already encloses (or
-// touches) the origin the pair is done, otherwise the loop resumes there.
-__device__ __forceinline__ int pb_begin(const Handoff& h, const Col<double>& c1, const Col<double>& c2,
-                                        const d3d_store& s, double tol_sq, const JoltEps<double>& E,
-                                        GjkLoop<double>& g, GjkResult<double>& r) {
-    const int outcome = handoff_outcome(h);
+// Separated pairs: the reference's loop from the FP32 closest point's
+// direction instead of (1,0,0), with an empty simplex; pb_step stops it by the
+// duality gap.
+template <typename Rows>
+__device__ __forceinline__ void pb_begin(GjkLoop<double, Rows>& g, float4 v) {
     simplex_clear(g.S);
-    if (outcome == PA_SEPARATED) {
-        d3 dir = mk(-(double)h.v.x, -(double)h.v.y, -(double)h.v.z);
-        gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
-        return PB_RUN;
+    const d3 dir = mk(-(double)v.x, -(double)v.y, -(double)v.z);
+    gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
+}
+
+template <typename Rows>
+__device__ __forceinline__ bool pb_step(GjkLoop<double, Rows>& g, const d3d_store& s, int a, int b, double tol_sq,
+                                        const d3d_gjk_options& opt, const JoltEps<double>& E) {
+    return gjk_step<double, RefineSupport, true>(g, s, a, b, tol_sq, opt.max_distance_squared, opt.max_iterations,
+                                                 E, kMixedRelGap);
+}
+
+// Finish a pair after its loop.  The closest points use the scale-invariant
+// degeneracy test of bary_plane (the simplex built around an accurate FP32
+// direction is tiny).  Should they still disagree with |v| (a sliver
+// triangle), the pair, like any non-OK status, goes to the cold FP64
+// fallback.
+template <typename Rows>
+__device__ __forceinline__ int pb_end(const GjkLoop<double, Rows>& g, const d3d_gjk_options& opt,
+                                      const JoltEps<double>& E, GjkResult<double>& r) {
+    gjk_end<double, true>(g, opt.sanity_check, E, r);
+    if (r.status != D3D_STATUS_OK) return PB_FALLBACK;
+    const d3 ab = r.a - r.b;
+    if (abs_t(sqrt_t(dot(ab, ab)) - r.dist) > 1e-10 * (r.dist > 1.0 ? r.dist : 1.0)) return PB_FALLBACK;
+    return PB_DONE;
+}
+
+// Touching pairs: the FP32 simplex rows re-evaluated in FP64 along the
+// directions that produced them (h: the pair's handoff record in memory).  If that simplex encloses (or touches) the
+// origin the pair is done (r filled, PB_DONE); otherwise g is left ready for
+// the loop to resume there (PB_RUN).
+template <typename Rows>
+__device__ __forceinline__ int pt_replay(GjkLoop<double, Rows>& g, const d3d_store& s, int a, int b,
+                                         const Handoff* __restrict__ h, double tol_sq, const JoltEps<double>& E,
+                                         GjkResult<double>& r) {
+    simplex_clear(g.S);
+    g.it = 0;
+    const int rows = handoff_rows(*h);
+#pragma unroll 1
+    for (int j = 0; j < rows; ++j) {
+        const float4 f = h->d[j];
+        d3 p, q;
+        pair_supports<double, RefineSupport>(s, a, b, mk((double)f.x, (double)f.y, (double)f.z), p, q);
+        simplex_push(g.S, p - q, p, q);
     }
-    if (outcome != PA_TOUCHING) return PB_FALLBACK;
-    const int rows = handoff_rows(h);
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if (j < rows) {
-            d3 d = mk((double)h.d[j].x, (double)h.d[j].y, (double)h.d[j].z);
-            d3 p = RefineSupport::eval(c1, s, d);
-            d3 q = RefineSupport::eval(c2, s, -d);
-            simplex_push(g.S, p - q, p, q);
-        }
     d3 v;
     double vl;
     int set;
     if (g.S.n == 0 || !closest_to_origin(g.S, DBL_MAX, E, v, vl, set)) return PB_FALLBACK;
     if (set != 15) simplex_compact<double, true>(g.S, set);
     if (set == 15 || vl <= tol_sq || vl <= E.isect * max_y_len_sq(g.S)) {
-        d3 a, b;
-        closest_points(g.S, E, a, b);
-        d3 m = (a + b) * 0.5;
+        d3 ca, cb;
+        closest_points<double, true>(g.S, E, ca, cb);
+        const d3 m = (ca + cb) * 0.5;
         r.dist = 0.0;
         r.a = m;
         r.b = m;
@@ -178,64 +203,6 @@ __device__ __forceinline__ int pb_begin(const Handoff& h, const Col<double>& c1,
     }
     gjk_begin(g, -v, vl, vl);
     return PB_RUN;
-}
-
-__device__ __forceinline__ bool pb_step(GjkLoop<double>& g, const Col<double>& c1, const Col<double>& c2,
-                                        const d3d_store& s, double tol_sq, const d3d_gjk_options& opt,
-                                        const JoltEps<double>& E) {
-    return gjk_step<double, RefineSupport, true>(g, c1, c2, s, tol_sq, opt.max_distance_squared,
-                                                 opt.max_iterations, E, kMixedRelGap);
-}
-
-// Finish phase B.  Jolt's face-region projection can leave the simplex on a
-// sliver triangle; the barycentric closest points then disagree with |v|,
-// and such pairs (and any non-OK status) go to the cold FP64 fallback.
-__device__ __forceinline__ int pb_end(const GjkLoop<double>& g, const d3d_gjk_options& opt, const JoltEps<double>& E,
-                                      GjkResult<double>& r) {
-    gjk_end(g, opt.sanity_check, E, r);
-    if (r.status != D3D_STATUS_OK) return PB_FALLBACK;
-    d3 ab = r.a - r.b;
-    if (abs_t(sqrt_t(dot(ab, ab)) - r.dist) > 1e-10 * (r.dist > 1.0 ? r.dist : 1.0)) return PB_FALLBACK;
-    return PB_DONE;
-}
-
-// One pair end to end (phase A, phase B, cold fallback): the single-thread
-// form of the three kernels, used where a pair is computed in isolation.
-__device__ __forceinline__ void gjk_mixed_pair(const d3d_store& s, int a, int b, const d3d_gjk_options& opt,
-                                               GjkResult<double>& r, Simplex<double>& S) {
-    const JoltEps<double> E = reference_eps<double>();
-    const double tol_sq = opt.tolerance * opt.tolerance;
-    Handoff h;
-    {
-        Col<float> f1, f2;
-        load_col(s, a, f1);
-        load_col(s, b, f2);
-        PhaseALoop L;
-        pa_begin(L);
-        int o;
-        while ((o = pa_step(L, f1, f2, s, (float)tol_sq, (float)opt.max_distance_squared, opt.max_iterations)) < 0) {
-        }
-        h = pa_handoff(L, o);
-    }
-    Col<double> c1, c2;
-    load_col(s, a, c1);
-    load_col(s, b, c2);
-    GjkLoop<double> g;
-    int mode = pb_begin(h, c1, c2, s, tol_sq, E, g, r);
-    if (mode == PB_RUN) {
-        while (!pb_step(g, c1, c2, s, tol_sq, opt, E)) {
-        }
-        mode = pb_end(g, opt, E, r);
-    }
-    if (mode == PB_DONE) {
-        r.iters += handoff_iters(h);
-        S = g.S;
-        return;
-    }
-    simplex_clear(S);
-    const d3 dir = mk(1.0, 0.0, 0.0);
-    gjk_distance_loop(c1, c2, s, tol_sq, opt.max_distance_squared, opt.sanity_check, opt.max_iterations, E, S, dir,
-                      dot(dir, dir), DBL_MAX, r);
 }
 
 }  // namespace d3d

@@ -15,8 +15,9 @@ struct DistanceOut {
     int32_t* iterations;
 };
 
+template <typename Rows>
 __device__ __forceinline__ void store_result(const DistanceOut& o, int64_t k, const GjkResult<double>& r,
-                                             const Simplex<double>& S) {
+                                             const Simplex<double, Rows>& S) {
     if (r.status == D3D_STATUS_CLIPPED) {
         o.dist[k] = DBL_MAX;
 #pragma unroll

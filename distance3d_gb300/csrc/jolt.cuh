@@ -55,15 +55,19 @@ __device__ __forceinline__ void bary_line(V3<T> a, V3<T> b, const JoltEps<T>& E,
     }
 }
 
-// _gjk_jolt.py:316-372
-template <typename T>
+// _gjk_jolt.py:316-372.  The reference tests the determinant against an
+// absolute EPSILON, so a well-shaped triangle with edges below ~1e-8 counts as
+// degenerate and is reduced to an edge; SCALED makes the test relative to the
+// product of the squared edge lengths (the mixed form's final simplices are
+// that small, being built around an accurate FP32 direction).
+template <typename T, bool SCALED = false>
 __device__ __forceinline__ void bary_plane(V3<T> a, V3<T> b, V3<T> c, const JoltEps<T>& E, T& u, T& v, T& w) {
     V3<T> v0 = b - a, v1 = c - a, v2 = c - b;
     T d00 = dot(v0, v0), d11 = dot(v1, v1), d22 = dot(v2, v2);
     if (d00 <= d22) {
         T d01 = dot(v0, v1);
         T den = d00 * d11 - d01 * d01;
-        if (abs_t(den) < E.plane) {
+        if (abs_t(den) < (SCALED ? E.plane * (d00 * d11) : E.plane)) {
             if (d00 > d11) {
                 bary_line(a, b, E, u, v);
                 w = T(0);
@@ -80,7 +84,7 @@ __device__ __forceinline__ void bary_plane(V3<T> a, V3<T> b, V3<T> c, const Jolt
     } else {
         T d12 = dot(v1, v2);
         T den = d11 * d22 - d12 * d12;
-        if (abs_t(den) < E.plane) {
+        if (abs_t(den) < (SCALED ? E.plane * (d11 * d22) : E.plane)) {
             if (d11 > d22) {
                 bary_line(a, c, E, u, w);
                 v = T(0);
@@ -217,81 +221,81 @@ __device__ __forceinline__ int outside_planes(V3<T> a, V3<T> b, V3<T> c, V3<T> d
     return 15;
 }
 
-// _gjk_jolt.py:574-631
+// Where a simplex keeps its P and Q rows (the support points on each collider;
+// the solve reads only Y).  RegRows: registers, indexed by compile-time
+// constants after unrolling.  SmemRows: this lane's column of a shared-memory
+// block, six values per row strided by the block size, so that the FP64
+// kernels hold only Y in registers.
 template <typename T>
-__device__ __forceinline__ V3<T> cp_tetra(V3<T> a, V3<T> b, V3<T> c, V3<T> d, const JoltEps<T>& E, int& set) {
-    int s = 15, ns;
-    V3<T> cp = mk(T(0), T(0), T(0));
-    T best = maxf<T>();
-    int o = outside_planes(a, b, c, d, E);
-    if (o & 1) {
-        cp = cp_triangle(a, b, c, E, s);
-        best = dot(cp, cp);
+struct RegRows {
+    V3<T> P[4], Q[4];
+    __device__ __forceinline__ void put(int k, V3<T> p, V3<T> q) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j == k) {
+                P[j] = p;
+                Q[j] = q;
+            }
     }
-    if (o & 2) {
-        V3<T> q = cp_triangle(a, c, d, E, ns);
-        T d2 = dot(q, q);
-        if (d2 < best) {
-            best = d2;
-            cp = q;
-            s = (ns & 1) + ((ns & 6) << 1);
-        }
+    __device__ __forceinline__ void move(int dst, int src) {
+        P[dst] = P[src];
+        Q[dst] = Q[src];
     }
-    if (o & 4) {
-        V3<T> q = cp_triangle(a, d, b, E, ns);
-        T d2 = dot(q, q);
-        if (d2 < best) {
-            best = d2;
-            cp = q;
-            s = (ns & 1) + ((ns & 2) << 2) + ((ns & 4) >> 1);
-        }
-    }
-    if (o & 8) {
-        V3<T> q = cp_triangle(b, d, c, E, ns);
-        T d2 = dot(q, q);
-        if (d2 < best) {
-            cp = q;
-            s = ((ns & 1) << 1) + ((ns & 2) << 2) + (ns & 4);
-        }
-    }
-    set = s;
-    return cp;
-}
+    __device__ __forceinline__ V3<T> p(int k) const { return P[k]; }
+    __device__ __forceinline__ V3<T> q(int k) const { return Q[k]; }
+};
 
-// Register-resident simplex: rows 0..3 of Y, P, Q.
-template <typename T>
+template <typename T, int kStride>
+struct SmemRows {
+    T* base;  // element e (0..5: p.xyz, q.xyz) of row r at base[(6 r + e) kStride]
+    __device__ __forceinline__ T& at(int r, int e) const { return base[(6 * r + e) * kStride]; }
+    __device__ __forceinline__ void put(int k, V3<T> p, V3<T> q) {
+        at(k, 0) = p.x;
+        at(k, 1) = p.y;
+        at(k, 2) = p.z;
+        at(k, 3) = q.x;
+        at(k, 4) = q.y;
+        at(k, 5) = q.z;
+    }
+    __device__ __forceinline__ void move(int dst, int src) {
+#pragma unroll
+        for (int e = 0; e < 6; ++e) at(dst, e) = at(src, e);
+    }
+    __device__ __forceinline__ V3<T> p(int k) const { return mk(at(k, 0), at(k, 1), at(k, 2)); }
+    __device__ __forceinline__ V3<T> q(int k) const { return mk(at(k, 3), at(k, 4), at(k, 5)); }
+};
+
+// Simplex: rows 0..n-1 of Y (Minkowski-difference points, registers) and of
+// P, Q (in Rows).
+template <typename T, typename Rows = RegRows<T>>
 struct Simplex {
-    V3<T> Y[4], P[4], Q[4];
+    V3<T> Y[4];
+    Rows R;
     int n;
 };
 
-template <typename T>
-__device__ __forceinline__ void simplex_clear(Simplex<T>& S) {
+// Y rows cleared (rows GJK never writes are reported as zero); P and Q rows
+// are only read below n.
+template <typename T, typename Rows>
+__device__ __forceinline__ void simplex_clear(Simplex<T, Rows>& S) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        S.Y[k] = mk(T(0), T(0), T(0));
-        S.P[k] = S.Y[k];
-        S.Q[k] = S.Y[k];
-    }
+    for (int k = 0; k < 4; ++k) S.Y[k] = mk(T(0), T(0), T(0));
     S.n = 0;
 }
 
-template <typename T>
-__device__ __forceinline__ void simplex_push(Simplex<T>& S, V3<T> w, V3<T> p, V3<T> q) {
+template <typename T, typename Rows>
+__device__ __forceinline__ void simplex_push(Simplex<T, Rows>& S, V3<T> w, V3<T> p, V3<T> q) {
 #pragma unroll
     for (int k = 0; k < 4; ++k)
-        if (k == S.n) {
-            S.Y[k] = w;
-            S.P[k] = p;
-            S.Q[k] = q;
-        }
+        if (k == S.n) S.Y[k] = w;
+    S.R.put(S.n, p, q);
     ++S.n;
 }
 
 // keep the rows whose bit is set, in order (_gjk_jolt.py:655-664); rows at
 // and above the new count keep their old contents, as in the reference
-template <typename T, bool WITH_PQ>
-__device__ __forceinline__ void simplex_compact(Simplex<T>& S, int set) {
+template <typename T, bool WITH_PQ, typename Rows>
+__device__ __forceinline__ void simplex_compact(Simplex<T, Rows>& S, int set) {
     int m = 0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -300,10 +304,7 @@ __device__ __forceinline__ void simplex_compact(Simplex<T>& S, int set) {
             for (int j = 0; j <= i; ++j)
                 if (j == m && j != i) {
                     S.Y[j] = S.Y[i];
-                    if (WITH_PQ) {
-                        S.P[j] = S.P[i];
-                        S.Q[j] = S.Q[i];
-                    }
+                    if (WITH_PQ) S.R.move(j, i);
                 }
             ++m;
         }
@@ -311,26 +312,53 @@ __device__ __forceinline__ void simplex_compact(Simplex<T>& S, int set) {
     S.n = m;
 }
 
-// _gjk_jolt.py:691-711: closest point of the simplex to the origin; true iff
-// its squared length is below prev (NaN compares false)
+// Row k of a register-resident array (k < 4) without dynamic indexing.
 template <typename T>
-__device__ __forceinline__ bool closest_to_origin(const Simplex<T>& S, T prev, const JoltEps<T>& E, V3<T>& v,
+__device__ __forceinline__ V3<T> row_of(const V3<T>* Y, int k) {
+    V3<T> r = Y[0];
+    if (k == 1) r = Y[1];
+    if (k == 2) r = Y[2];
+    if (k == 3) r = Y[3];
+    return r;
+}
+
+// _gjk_jolt.py:691-711: closest point of the simplex to the origin; true iff
+// its squared length is below prev (NaN compares false).
+//
+// Triangles and tetrahedra share one face loop: a triangle is its own single
+// face, a tetrahedron contributes the faces whose plane has the origin on the
+// outside (_gjk_jolt.py:574-631: faces abc, acd, adb, bdc in that order, the
+// first tested face taken unconditionally, later ones only if strictly
+// closer).  Lanes of a warp holding simplices of 3 and 4 rows therefore run
+// cp_triangle together instead of in separate branches.
+template <typename T, typename Rows>
+__device__ __forceinline__ bool closest_to_origin(const Simplex<T, Rows>& S, T prev, const JoltEps<T>& E, V3<T>& v,
                                                   T& vl, int& set) {
-    V3<T> r;
+    V3<T> r = S.Y[0];
     int s = 1;
-    switch (S.n) {
-    case 1:
-        r = S.Y[0];
-        break;
-    case 2:
+    if (S.n == 2) {
         r = cp_line(S.Y[0], S.Y[1], E, s);
-        break;
-    case 3:
-        r = cp_triangle(S.Y[0], S.Y[1], S.Y[2], E, s);
-        break;
-    default:
-        r = cp_tetra(S.Y[0], S.Y[1], S.Y[2], S.Y[3], E, s);
-        break;
+    } else if (S.n >= 3) {
+        int faces = S.n == 3 ? 1 : outside_planes(S.Y[0], S.Y[1], S.Y[2], S.Y[3], E);
+        r = mk(T(0), T(0), T(0));
+        s = 15;
+        T best = maxf<T>();
+        while (faces) {
+            const int f = __ffs(faces) - 1;
+            faces &= faces - 1;
+            // corners of face f: (0,1,2) (0,2,3) (0,3,1) (1,3,2)
+            const int i0 = f == 3 ? 1 : 0;
+            const int i1 = f == 0 ? 1 : (f == 1 ? 2 : 3);
+            const int i2 = f == 0 ? 2 : (f == 1 ? 3 : (f == 2 ? 1 : 2));
+            int ns;
+            const V3<T> q = cp_triangle(row_of(S.Y, i0), row_of(S.Y, i1), row_of(S.Y, i2), E, ns);
+            const T d2 = dot(q, q);
+            if (f == 0 || d2 < best) {
+                best = d2;
+                r = q;
+                s = ((ns & 1) << i0) | (((ns >> 1) & 1) << i1) | (((ns >> 2) & 1) << i2);
+            }
+        }
     }
     T l = dot(r, r);
     if (l < prev) {
@@ -343,8 +371,8 @@ __device__ __forceinline__ bool closest_to_origin(const Simplex<T>& S, T prev, c
 }
 
 // _gjk_jolt.py:635-640
-template <typename T>
-__device__ __forceinline__ T max_y_len_sq(const Simplex<T>& S) {
+template <typename T, typename Rows>
+__device__ __forceinline__ T max_y_len_sq(const Simplex<T, Rows>& S) {
     T m = dot(S.Y[0], S.Y[0]);
 #pragma unroll
     for (int i = 1; i < 4; ++i)
@@ -355,33 +383,33 @@ __device__ __forceinline__ T max_y_len_sq(const Simplex<T>& S) {
     return m;
 }
 
-// _gjk_jolt.py:668-687
-template <typename T>
-__device__ __forceinline__ void closest_points(const Simplex<T>& S, const JoltEps<T>& E, V3<T>& a, V3<T>& b) {
+// _gjk_jolt.py:668-687 (SCALED: see bary_plane)
+template <typename T, bool SCALED = false, typename Rows>
+__device__ __forceinline__ void closest_points(const Simplex<T, Rows>& S, const JoltEps<T>& E, V3<T>& a, V3<T>& b) {
     switch (S.n) {
     case 1:
-        a = S.P[0];
-        b = S.Q[0];
+        a = S.R.p(0);
+        b = S.R.q(0);
         break;
     case 2: {
         T u, v;
         bary_line(S.Y[0], S.Y[1], E, u, v);
-        a = S.P[0] * u + S.P[1] * v;
-        b = S.Q[0] * u + S.Q[1] * v;
+        a = S.R.p(0) * u + S.R.p(1) * v;
+        b = S.R.q(0) * u + S.R.q(1) * v;
         break;
     }
     case 3: {
         T u, v, w;
-        bary_plane(S.Y[0], S.Y[1], S.Y[2], E, u, v, w);
-        a = (S.P[0] * u + S.P[1] * v) + S.P[2] * w;
-        b = (S.Q[0] * u + S.Q[1] * v) + S.Q[2] * w;
+        bary_plane<T, SCALED>(S.Y[0], S.Y[1], S.Y[2], E, u, v, w);
+        a = (S.R.p(0) * u + S.R.p(1) * v) + S.R.p(2) * w;
+        b = (S.R.q(0) * u + S.R.q(1) * v) + S.R.q(2) * w;
         break;
     }
     default: {
         T o[4];
         bary_tetra(S.Y[0], S.Y[1], S.Y[2], S.Y[3], o);
-        a = ((S.P[0] * o[0] + S.P[1] * o[1]) + S.P[2] * o[2]) + S.P[3] * o[3];
-        b = ((S.Q[0] * o[0] + S.Q[1] * o[1]) + S.Q[2] * o[2]) + S.Q[3] * o[3];
+        a = ((S.R.p(0) * o[0] + S.R.p(1) * o[1]) + S.R.p(2) * o[2]) + S.R.p(3) * o[3];
+        b = ((S.R.q(0) * o[0] + S.R.q(1) * o[1]) + S.R.q(2) * o[2]) + S.R.q(3) * o[3];
         break;
     }
     }
@@ -400,6 +428,24 @@ struct ExactSupport {
     }
 };
 
+// Support points p of collider a along d and q of collider b along -d.  The
+// records are read from the store (L1-resident) inside a two-trip loop, so
+// the support code exists once per kernel and holds no registers across the
+// simplex solve.
+template <typename T, typename Sup>
+__device__ __forceinline__ void pair_supports(const d3d_store& st, int a, int b, V3<T> d, V3<T>& p, V3<T>& q) {
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        Col<T> c;
+        load_col(st, k ? b : a, c);
+        const V3<T> x = Sup::eval(c, st, k ? -d : d);
+        if (k)
+            q = x;
+        else
+            p = x;
+    }
+}
+
 template <typename T>
 struct GjkResult {
     T dist;
@@ -410,9 +456,9 @@ struct GjkResult {
 
 // State of one pair's Jolt GJK distance loop between iterations.
 enum { GJK_RUNNING = -1 };
-template <typename T>
+template <typename T, typename Rows = RegRows<T>>
 struct GjkLoop {
-    Simplex<T> S;
+    Simplex<T, Rows> S;
     V3<T> dir;  // next search direction
     T vl;       // v_len_sq as the reference keeps it
     T prev;     // prev_v_len_sq
@@ -423,8 +469,8 @@ struct GjkLoop {
 
 // Start the loop.  S must already hold the starting simplex (n = 0 for the
 // reference's cold start, dir = (1,0,0), vl = 1, prev = MAX_FLOAT).
-template <typename T>
-__device__ __forceinline__ void gjk_begin(GjkLoop<T>& g, V3<T> dir, T vl, T prev) {
+template <typename T, typename Rows>
+__device__ __forceinline__ void gjk_begin(GjkLoop<T, Rows>& g, V3<T> dir, T vl, T prev) {
     g.dir = dir;
     g.vl = vl;
     g.prev = prev;
@@ -441,17 +487,17 @@ __device__ __forceinline__ void gjk_begin(GjkLoop<T>& g, V3<T> dir, T vl, T prev
 // support point along -v, |v|^2 - v.w <= rel_gap |v|^2 bounds the relative
 // error of |v| by rel_gap, and the loop stops there.  The FP64 drop-in is
 // compiled without it.
-template <typename T, typename Sup = ExactSupport, bool GAP = false>
-__device__ __forceinline__ bool gjk_step(GjkLoop<T>& g, const Col<T>& c1, const Col<T>& c2, const d3d_store& st,
-                                         T tol_sq, T max_d2, int max_iter, const JoltEps<T>& E, T rel_gap = T(0)) {
+template <typename T, typename Sup = ExactSupport, bool GAP = false, typename Rows>
+__device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
+                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0)) {
     if (g.it >= max_iter) {
         g.status = D3D_STATUS_MAX_ITER;
         g.state = GJK_NO_INTERSECTION;
         return true;
     }
     ++g.it;
-    V3<T> p = Sup::eval(c1, st, g.dir);
-    V3<T> q = Sup::eval(c2, st, -g.dir);
+    V3<T> p, q;
+    pair_supports<T, Sup>(st, a, b, g.dir, p, q);
     V3<T> w = p - q;
     T dd = dot(g.dir, w);
     if (dd < T(0) && dd * dd > g.vl * max_d2) {
@@ -496,8 +542,8 @@ __device__ __forceinline__ bool gjk_step(GjkLoop<T>& g, const Col<T>& c1, const 
 
 // After the loop: closest points, sanity check, distance
 // (_gjk_jolt.py:209-221).
-template <typename T>
-__device__ __forceinline__ void gjk_end(const GjkLoop<T>& g, T sanity, const JoltEps<T>& E, GjkResult<T>& out) {
+template <typename T, bool SCALED = false, typename Rows>
+__device__ __forceinline__ void gjk_end(const GjkLoop<T, Rows>& g, T sanity, const JoltEps<T>& E, GjkResult<T>& out) {
     out.iters = g.it;
     out.status = g.status;
     if (g.state == GJK_CLIPPED) {
@@ -505,7 +551,7 @@ __device__ __forceinline__ void gjk_end(const GjkLoop<T>& g, T sanity, const Jol
         return;
     }
     V3<T> a, b;
-    closest_points(g.S, E, a, b);
+    closest_points<T, SCALED>(g.S, E, a, b);
     T check = abs_t(dot(g.dir, g.dir) - g.vl);
     if (!(check < sanity) && out.status == D3D_STATUS_OK) out.status = D3D_STATUS_SANITY;
     T dist = sqrt_t(g.vl);
@@ -519,26 +565,21 @@ __device__ __forceinline__ void gjk_end(const GjkLoop<T>& g, T sanity, const Jol
     out.b = b;
 }
 
-// The whole loop for one pair: gjk_distance_jolt (_gjk_jolt.py:138-221).
-// On entry S holds the starting simplex; on exit it holds the final one.
-template <typename T, typename Sup = ExactSupport, bool GAP = false>
-__device__ __forceinline__ void gjk_distance_loop(const Col<T>& c1, const Col<T>& c2, const d3d_store& st, T tol_sq,
-                                                  T max_d2, T sanity, int max_iter, const JoltEps<T>& E,
-                                                  Simplex<T>& S, V3<T> dir, T vl, T prev, GjkResult<T>& out,
-                                                  T rel_gap = T(0)) {
-    GjkLoop<T> g;
-    g.S = S;
-    gjk_begin(g, dir, vl, prev);
-    while (!gjk_step<T, Sup, GAP>(g, c1, c2, st, tol_sq, max_d2, max_iter, E, rel_gap)) {
+// The rest of the loop for one pair, from the state gjk_begin (and any
+// starting simplex) left in g: gjk_distance_jolt (_gjk_jolt.py:138-221).
+template <typename T, typename Sup = ExactSupport, bool GAP = false, bool SCALED = false, typename Rows>
+__device__ __forceinline__ void gjk_run(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
+                                        T sanity, int max_iter, const JoltEps<T>& E, GjkResult<T>& out,
+                                        T rel_gap = T(0)) {
+    while (!gjk_step<T, Sup, GAP>(g, st, a, b, tol_sq, max_d2, max_iter, E, rel_gap)) {
     }
-    gjk_end(g, sanity, E, out);
-    S = g.S;
+    gjk_end<T, SCALED>(g, sanity, E, out);
 }
 
 // gjk_intersection_jolt, _gjk_jolt.py:29-135.  Returns 1 on intersection.
 template <typename T, typename Sup = ExactSupport>
-__device__ __forceinline__ int gjk_intersection_loop(const Col<T>& c1, const Col<T>& c2, const d3d_store& st, T tol_sq,
-                                                     int max_iter, const JoltEps<T>& E, int& status) {
+__device__ __forceinline__ int gjk_intersection_loop(const d3d_store& st, int a, int b, T tol_sq, int max_iter,
+                                                     const JoltEps<T>& E, int& status) {
     Simplex<T> S;
     simplex_clear(S);
     T prev = maxf<T>();
@@ -549,8 +590,8 @@ __device__ __forceinline__ int gjk_intersection_loop(const Col<T>& c1, const Col
             status = D3D_STATUS_MAX_ITER;
             return 0;
         }
-        V3<T> p = Sup::eval(c1, st, dir);
-        V3<T> q = Sup::eval(c2, st, -dir);
+        V3<T> p, q;
+        pair_supports<T, Sup>(st, a, b, dir, p, q);
         V3<T> w = p - q;
         if (dot(dir, w) < -E.conv) return 0;
         simplex_push(S, w, p, q);

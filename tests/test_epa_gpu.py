@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from distance3d_gb300 import workloads
+from distance3d_gb300.collider_set import BOX, HULL
 from distance3d_gb300.epa import epa_batch, epa_scratch_bytes
 from distance3d_gb300.gjk import gjk_distance_batch
 from distance3d_gb300.store import ColliderStore
@@ -139,5 +140,18 @@ def test_mixed_epa_within_tolerance(max_faces, max_edges):
     dm = np.linalg.norm(m["mtv"][both], axis=1)
     dr = np.linalg.norm(ref["mtv"][both], axis=1)
     cosang = np.sum(m["mtv"][both] * ref["mtv"][both], axis=1) / np.maximum(dm * dr, 1e-300)
-    ok = ~wrong & (dr > 1e-3)
-    assert np.all(cosang[ok] > 1 - 1e-6)
+    # Polytope pairs (box, hull): the final face of the Minkowski difference
+    # is the same face, so the directions agree to rounding.
+    t1, t2 = cs.types[i1[hit][both]], cs.types[i2[hit][both]]
+    poly = np.isin(t1, [BOX, HULL]) & np.isin(t2, [BOX, HULL]) & ~wrong & (dr > 1e-3)
+    assert poly.sum() > 100
+    assert np.all(cosang[poly] > 1 - 1e-9)
+    # Curved pairs: the depth is flat in the direction near its minimum, and
+    # both forms stop on a polytope face whose normal is within ~1e-3 rad of
+    # the optimum.  The mixed direction is certified instead: the exact
+    # support-function depth along it (the oracle's supports) equals the
+    # reported depth and is within the tolerance of the reference's depth.
+    n = m["mtv"][both] / dm[:, None]
+    h = oracle.depth_upper_bound(cs, i1[hit][both], i2[hit][both], n)
+    assert np.all(np.abs(h - dm) <= 1e-7 * np.maximum(1.0, dm))
+    assert np.all(h <= dr + MIXED_DEPTH_TOL * np.maximum(1.0, dr))

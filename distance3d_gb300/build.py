@@ -36,6 +36,7 @@ UNITS = [
     ("epa.cu", ["-fmad=false"]),
     ("gjk_mixed.cu", ["-fmad=true"]),
     ("epa_mixed.cu", ["-fmad=true"]),
+    ("epa_warp.cu", ["-fmad=true"]),
     ("schedule.cu", []),
     ("bvh.cu", []),
 ]

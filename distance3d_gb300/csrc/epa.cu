@@ -270,7 +270,8 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     }
     cudaStream_t st = d3d::as_stream(stream);
     const bool mixed = options->precision == D3D_PRECISION_MIXED;
-    const bool sched = n >= kScheduleMin;
+    const bool warp = mixed && d3d::epa_warp_supported(*options);
+    const bool sched = n >= kScheduleMin && !warp;
     const size_t up_n = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
     const size_t order_bytes = sched ? up_n : 0;
     const size_t fb_bytes = mixed ? up_n : 0;
@@ -284,7 +285,10 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     int32_t* fallback = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes) : nullptr;
     cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned long long), st);
     if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, p + 256 + order_bytes + fb_bytes, temp_bytes, st);
-    if (!rc && mixed)
+    if (!rc && warp)
+        rc = d3d::epa_warp_launch(*store, i1, i2, n, ctr, simplex, *options, mtv, status, n_faces, faces, fallback,
+                                  ctr + 2, st);
+    else if (!rc && mixed)
         rc = d3d::epa_mixed_launch(*store, i1, i2, order, n, ctr, simplex, *options, mtv, status, n_faces, faces,
                                    scratch, slots_for(n), fallback, ctr + 2, st);
     if (!rc) {

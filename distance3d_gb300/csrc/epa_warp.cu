@@ -1,0 +1,571 @@
+// epa_warp.cu -- mixed-precision EPA, one warp per pair.
+//
+// The search is the mixed EPA of epa_mixed.cu (FP32 polytope search on the
+// FP32 mirror, validation with an FP64 fallback); this file lays it out for
+// the GPU.  Each pair's polytope lives in its warp's slice of shared memory
+// and the 32 lanes share the work of every expansion (epa.py:59-74):
+//
+//   closest face      lanes scan strided face slots, warp min-reduction
+//   support           the two colliders on the two half warps; box / hull
+//                     argmax split across a half warp's lanes (first
+//                     maximum, as np.argmax)
+//   visible faces     breadth-first search from the closest face over the
+//                     face adjacency with the reference's visibility test
+//                     (epa.py:157-165)
+//   horizon           edges of visible faces whose neighbour is not visible,
+//                     gathered by a warp prefix sum (epa.py:167-187)
+//   validation        every horizon vertex starts and ends exactly one edge,
+//                     and the edges form one loop (pointer jumping): the
+//                     visible faces are a disk, so the new faces close the
+//                     surface again
+//   new faces         one per horizon edge, in the slots the visible faces
+//                     freed (then fresh slots), with their adjacency set from
+//                     the loop order (epa.py:126-146)
+//
+// Faces keep their three vertex ids, unit normal and offset, and the ids of
+// the faces across their three edges; winding is outward by construction, as
+// in epa_mixed.cu.  A pair whose polytope fails validation (degenerate face,
+// horizon not one loop, more horizon edges than max_loose_edges) goes to the
+// FP64 EPA's fallback list.  The converged face is refined along its FP32
+// normal with FP64 supports (refine_face).  Compiled with -fmad=true.
+#include "capi_util.h"
+#include "epa_mixed.cuh"
+#include "epa_mixed.h"
+#include "scratch.h"
+
+namespace {
+
+using namespace d3d;
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kWarps = 4;                // warps (pairs) per block
+constexpr unsigned kDead = 0xffffffffu;  // vertex word of a free face slot
+
+// Byte offsets of one warp's polytope in shared memory.
+struct Layout {
+    int vy, vd, fn, fv, adj, hz, freel, vis, se, ee, bytes;
+};
+
+__host__ __device__ inline Layout layout_for(const d3d_epa_options& o) {
+    const int nv = o.max_iterations + 4, F = o.max_faces, E = o.max_loose_edges > 0 ? o.max_loose_edges : 1;
+    Layout L;
+    int p = 0;
+    L.vy = p;
+    p += 16 * nv;
+    L.vd = p;
+    p += 16 * nv;
+    L.fn = p;
+    p += 16 * F;
+    L.adj = p;
+    p += 8 * F;
+    L.hz = p;
+    p += 8 * E;
+    L.fv = p;
+    p += 4 * F;
+    L.vis = p;
+    p += 4 * F;
+    L.freel = p;
+    p += 2 * F;
+    L.se = p;
+    p += nv;
+    L.ee = p;
+    p += nv;
+    L.bytes = (p + 15) & ~15;
+    return L;
+}
+
+struct Poly {
+    float4* vy;            // vertex y.xyz
+    float4* vd;            // search direction .xyz; w: input simplex row (0..3), -1 for found vertices
+    float4* fn;            // unit normal .xyz, w = offset n . y_a
+    ushort4* adj;          // faces across edges (a,b), (b,c), (c,a)
+    int2* hz;              // horizon edge e: x = a | b << 8 | k << 16 (edge k of g faces it), y = g
+    unsigned* fv;          // a | b << 8 | c << 16, kDead for a free slot
+    unsigned short* freel; // free face slots (stack)
+    int* vis;              // iteration stamp of the faces found visible
+    unsigned char* se;     // horizon edge that starts at vertex v
+    unsigned char* ee;     // horizon edge that ends at vertex v
+};
+
+__device__ __forceinline__ Poly poly_at(unsigned char* base, const Layout& L) {
+    Poly P;
+    P.vy = reinterpret_cast<float4*>(base + L.vy);
+    P.vd = reinterpret_cast<float4*>(base + L.vd);
+    P.fn = reinterpret_cast<float4*>(base + L.fn);
+    P.adj = reinterpret_cast<ushort4*>(base + L.adj);
+    P.hz = reinterpret_cast<int2*>(base + L.hz);
+    P.fv = reinterpret_cast<unsigned*>(base + L.fv);
+    P.freel = reinterpret_cast<unsigned short*>(base + L.freel);
+    P.vis = reinterpret_cast<int*>(base + L.vis);
+    P.se = base + L.se;
+    P.ee = base + L.ee;
+    return P;
+}
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ f3 yv(const Poly& P, int v) {
+    const float4 a = P.vy[v];
+    return mk(a.x, a.y, a.z);
+}
+
+// Index of the first maximum of V . d over a polytope's vertices, the 16
+// lanes of a half warp (mask hm) taking every 16th vertex (same products as
+// hull_argmax, same winner).
+template <typename T>
+__device__ __forceinline__ int half_argmax(const T* verts, int off, int nv, V3<T> d, unsigned hm) {
+    T best = T(0);
+    int bi = -1;
+    for (int k = lane_id() & 15; k < nv; k += 16) {
+        const V3<T> v = load_vertex(verts, off + k);
+        const T s = dot102(v.x, v.y, v.z, d.x, d.y, d.z);
+        if (bi < 0 || s > best) {
+            best = s;
+            bi = k;
+        }
+    }
+#pragma unroll
+    for (int m = 8; m; m >>= 1) {
+        const T ob = __shfl_xor_sync(hm, best, m);
+        const int oi = __shfl_xor_sync(hm, bi, m);
+        if (oi >= 0 && (bi < 0 || ob > best || (ob == best && oi < bi))) {
+            best = ob;
+            bi = oi;
+        }
+    }
+    return bi;
+}
+
+__device__ __forceinline__ unsigned half_mask() { return (lane_id() & 16) ? 0xffff0000u : 0x0000ffffu; }
+
+// w = s_a(d) - s_b(-d) in FP32: the lower half warp evaluates collider a, the
+// upper half collider b, together; every lane returns w.
+__device__ __forceinline__ f3 minkowski32(const d3d_store& st, int a, int b, f3 d) {
+    const bool up = lane_id() & 16;
+    Col<float> c;
+    load_col(st, up ? b : a, c);
+    const f3 dd = up ? -d : d;
+    f3 s;
+    if (c.type == D3D_BOX || c.type == D3D_HULL) {
+        if (c.nv < 1)
+            s = mk(NAN, NAN, NAN);
+        else
+            s = load_vertex(st.verts32, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, dd, half_mask())));
+    } else {
+        s = support(c, st.verts32, dd);
+    }
+    const f3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
+    return up ? o - s : s - o;
+}
+
+// The same in FP64 with RefineSupport (polytope vertex chosen by the FP32
+// argmax of the rounded direction).
+__device__ __forceinline__ d3 minkowski64(const d3d_store& st, int a, int b, d3 d) {
+    const bool up = lane_id() & 16;
+    Col<double> c;
+    load_col(st, up ? b : a, c);
+    const d3 dd = up ? -d : d;
+    d3 s;
+    if (c.type == D3D_BOX || c.type == D3D_HULL) {
+        if (c.nv < 1) {
+            s = mk(double(NAN), double(NAN), double(NAN));
+        } else {
+            const f3 df = mk(__double2float_rn(dd.x), __double2float_rn(dd.y), __double2float_rn(dd.z));
+            s = load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, df, half_mask())));
+        }
+    } else {
+        s = RefineSupport::eval(c, st, dd);
+    }
+    const d3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
+    return up ? o - s : s - o;
+}
+
+// exclusive prefix sum over lanes
+__device__ __forceinline__ int warp_excl(int x) {
+    int s = x;
+#pragma unroll
+    for (int m = 1; m < 32; m <<= 1) {
+        const int t = __shfl_up_sync(kFull, s, m);
+        if (lane_id() >= m) s += t;
+    }
+    return s - x;
+}
+
+// unit normal and offset of face (a, b, c); false if degenerate
+__device__ __forceinline__ bool plane_of(const Poly& P, int a, int b, int c, float4& out) {
+    const f3 ya = yv(P, a), yb = yv(P, b), yc = yv(P, c);
+    f3 n = cross(yb - ya, yc - ya);
+    const float l = sqrtf(dot(n, n));
+    if (!(l > 0.f)) return false;
+    n = n * (1.f / l);
+    out = make_float4(n.x, n.y, n.z, dot(ya, n));
+    return true;
+}
+
+__device__ __forceinline__ unsigned pack3(int a, int b, int c) { return (unsigned)a | ((unsigned)b << 8) | ((unsigned)c << 16); }
+__device__ __forceinline__ int vid(unsigned w, int j) { return (int)((w >> (8 * j)) & 0xffu); }
+__device__ __forceinline__ int adj_at(ushort4 g, int j) { return j == 0 ? g.x : (j == 1 ? g.y : g.z); }
+
+// Closest live face: (offset, slot), ties to the lower slot.
+__device__ __forceinline__ int closest_face(const Poly& P, int nslots) {
+    float bd = 0.f;
+    int bs = -1;
+    for (int f = lane_id(); f < nslots; f += 32) {
+        if (P.fv[f] == kDead) continue;
+        const float d = P.fn[f].w;
+        if (bs < 0 || d < bd) {
+            bd = d;
+            bs = f;
+        }
+    }
+#pragma unroll
+    for (int m = 16; m; m >>= 1) {
+        const float od = __shfl_xor_sync(kFull, bd, m);
+        const int os = __shfl_xor_sync(kFull, bs, m);
+        if (os >= 0 && (bs < 0 || od < bd || (od == bd && os < bs))) {
+            bd = od;
+            bs = os;
+        }
+    }
+    return bs;
+}
+
+// Outcome of the FP32 search for one pair.
+struct Search {
+    int status;   // a D3D status, or kEpaFallback
+    int closest;  // face slot refined for OK / NOT_CONVERGED
+    int nslots;
+    int live;
+};
+
+// The FP32 expanding-polytope search for one pair (uniform across the warp).
+__device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, const double* simplex,
+                              const d3d_epa_options& o) {
+    const int ln = lane_id();
+    Search R{kEpaFallback, 0, 0, 0};
+    // starting tetrahedron: the FP64 simplex rounded to FP32
+    float scale = 0.f;
+    if (ln < 4) {
+        const f3 y = mk((float)simplex[3 * ln], (float)simplex[3 * ln + 1], (float)simplex[3 * ln + 2]);
+        P.vy[ln] = make_float4(y.x, y.y, y.z, 0.f);
+        P.vd[ln] = make_float4(0.f, 0.f, 0.f, (float)ln);
+        scale = sqrtf(dot(y, y));
+    }
+#pragma unroll
+    for (int m = 16; m; m >>= 1) scale = fmaxf(scale, __shfl_xor_sync(kFull, scale, m));
+    __syncwarp();
+    // faces ABC, ACD, ADB, BDC, each wound away from the vertex it leaves out
+    bool bad = false;
+    if (ln < 4) {
+        const int t = ln == 0 ? 0x3210 : (ln == 1 ? 0x1320 : (ln == 2 ? 0x2130 : 0x0231));
+        int fa = t & 15, fb = (t >> 4) & 15;
+        const int fc = (t >> 8) & 15, fd = (t >> 12) & 15;
+        float4 pl;
+        if (!plane_of(P, fa, fb, fc, pl)) {
+            bad = true;
+        } else {
+            const f3 yd = yv(P, fd) - yv(P, fa);
+            if (pl.x * yd.x + pl.y * yd.y + pl.z * yd.z > 0.f) {
+                const int s = fa;
+                fa = fb;
+                fb = s;
+                pl = make_float4(-pl.x, -pl.y, -pl.z, -pl.w);
+            }
+            P.fv[ln] = pack3(fa, fb, fc);
+            P.fn[ln] = pl;
+            P.vis[ln] = 0;
+        }
+    }
+    if (__any_sync(kFull, bad)) return R;
+    __syncwarp();
+    // adjacency of the tetrahedron: the face across (u, v) holds (v, u)
+    if (ln < 12) {
+        const int f = ln / 3, j = ln % 3;
+        const unsigned w = P.fv[f];
+        const int u = vid(w, j), v = vid(w, (j + 1) % 3);
+        int g = -1;
+        for (int h = 0; h < 4; ++h) {
+            if (h == f) continue;
+            const unsigned x = P.fv[h];
+            for (int i = 0; i < 3; ++i)
+                if (vid(x, i) == v && vid(x, (i + 1) % 3) == u) g = h;
+        }
+        if (g < 0) {
+            bad = true;
+        } else {
+            unsigned short* ap = reinterpret_cast<unsigned short*>(&P.adj[f]);
+            ap[j] = (unsigned short)g;
+        }
+    }
+    if (__any_sync(kFull, bad)) return R;
+    __syncwarp();
+
+    const float vis_eps = (float)o.epsilon;  // the reference's visibility test
+    int nslots = 4, nfree = 0, live = 4, nv = 4, it = 0;
+    while (true) {
+        const int cf = closest_face(P, nslots);
+        R.closest = cf;
+        R.nslots = nslots;
+        R.live = live;
+        if (cf < 0) {
+            R.status = D3D_STATUS_EPA_DEGENERATE;
+            return R;
+        }
+        if (it >= o.max_iterations) {
+            R.status = D3D_STATUS_EPA_NOT_CONVERGED;
+            return R;
+        }
+        ++it;
+        const float4 cn = P.fn[cf];
+        const f3 sd = mk(cn.x, cn.y, cn.z);
+        const f3 w = minkowski32(st, a, b, sd);
+        scale = fmaxf(scale, sqrtf(dot(w, w)));
+        const float eps = fmaxf((float)o.epsilon, 8.f * FLT_EPSILON * scale);
+        if (dot(w, sd) - cn.w < eps) {
+            R.status = D3D_STATUS_OK;
+            return R;
+        }
+        if (nv >= o.max_iterations + 4) {
+            R.status = D3D_STATUS_EPA_NOT_CONVERGED;
+            return R;
+        }
+        const int vn = nv++;
+        const int stamp = it;
+        // Faces that see w: breadth first from the closest face over the
+        // adjacency.  The visible faces are listed where they are about to
+        // go, on the free list above its current top.
+        unsigned short* const vl = P.freel + nfree;
+        if (ln == 0) {
+            P.vy[vn] = make_float4(w.x, w.y, w.z, 0.f);
+            P.vd[vn] = make_float4(sd.x, sd.y, sd.z, -1.f);
+            P.vis[cf] = stamp;
+            vl[0] = (unsigned short)cf;
+        }
+        __syncwarp();
+        int head = 0, nvis = 1;
+        while (head < nvis) {
+            const int nc = 3 * (nvis - head);
+            int added = 0;
+            for (int i0 = 0; i0 < nc; i0 += 32) {
+                const int i = i0 + ln;
+                bool take = false;
+                int g = 0;
+                if (i < nc) {
+                    g = adj_at(P.adj[vl[head + i / 3]], i % 3);
+                    if (P.vis[g] != stamp) {
+                        const float4 pl = P.fn[g];
+                        if (dot(mk(pl.x, pl.y, pl.z), w - yv(P, vid(P.fv[g], 0))) > vis_eps)
+                            take = atomicExch(&P.vis[g], stamp) != stamp;
+                    }
+                }
+                const unsigned m = __ballot_sync(kFull, take);
+                if (take) vl[nvis + added + __popc(m & ((1u << ln) - 1u))] = (unsigned short)g;
+                added += __popc(m);
+            }
+            __syncwarp();
+            head = nvis;
+            nvis += added;
+        }
+        // horizon: edges of visible faces whose neighbour is not visible
+        int ne_l = 0;
+        for (int i = ln; i < 3 * nvis; i += 32) ne_l += P.vis[adj_at(P.adj[vl[i / 3]], i % 3)] != stamp;
+        int eb = warp_excl(ne_l);
+        const int ne = __shfl_sync(kFull, eb + ne_l, 31);
+        if (ne > o.max_loose_edges || ne < 3) return R;
+        for (int i = ln; i < 3 * nvis; i += 32) {
+            const int f = vl[i / 3], j = i % 3;
+            const int h = adj_at(P.adj[f], j);
+            if (P.vis[h] == stamp) continue;
+            const unsigned fw = P.fv[f];
+            const ushort4 gh = P.adj[h];
+            const int k = gh.x == f ? 0 : (gh.y == f ? 1 : 2);
+            P.hz[eb++] = make_int2(vid(fw, j) | (vid(fw, (j + 1) % 3) << 8) | (k << 16), h);
+        }
+        __syncwarp();
+        for (int i = ln; i < nvis; i += 32) P.fv[vl[i]] = kDead;
+        __syncwarp();
+        // The horizon must be one loop.  A single visible face gives its own
+        // three edges, in order.  Otherwise: unique start and end per vertex ...
+        if (nvis > 1) {
+            for (int e = ln; e < ne; e += 32) {
+                const int x = P.hz[e].x;
+                P.se[x & 0xff] = (unsigned char)e;
+                P.ee[(x >> 8) & 0xff] = (unsigned char)e;
+            }
+            __syncwarp();
+            bool ok = true;
+            for (int e = ln; e < ne; e += 32) {
+                const int x = P.hz[e].x;
+                const int nx = P.se[(x >> 8) & 0xff];
+                ok &= P.se[x & 0xff] == e && P.ee[(x >> 8) & 0xff] == e && nx < ne &&
+                      (P.hz[nx].x & 0xff) == ((x >> 8) & 0xff);
+            }
+            if (!__all_sync(kFull, ok)) return R;
+            // ... and following next(e) from edge 0 visits every edge once
+            if (ne <= 32) {
+                int nxt = ln < ne ? P.se[(P.hz[ln].x >> 8) & 0xff] : ln;
+                int lab = ln < ne ? ln : 0;
+#pragma unroll
+                for (int r = 0; r < 5; ++r) {
+                    lab = min(lab, __shfl_sync(kFull, lab, nxt));
+                    nxt = __shfl_sync(kFull, nxt, nxt);
+                }
+                ok = lab == 0;
+            } else {
+                int steps = 0, cur = 0;
+                if (ln == 0) {
+                    do {
+                        cur = P.se[(P.hz[cur].x >> 8) & 0xff];
+                        ++steps;
+                    } while (cur != 0 && steps <= ne);
+                }
+                ok = __shfl_sync(kFull, steps == ne && cur == 0, 0);
+            }
+            if (!__all_sync(kFull, ok)) return R;
+        }
+        const int nlive = live - nvis + ne;
+        if (nlive > o.max_faces) {
+            R.status = D3D_STATUS_EPA_FACE_OVERFLOW;
+            R.live = live - nvis;
+            return R;
+        }
+        // new faces (a, b, w): slots from the top of the free list, then fresh
+        const int nft = nfree + nvis;
+        for (int e = ln; e < ne; e += 32) {
+            const int2 h = P.hz[e];
+            const int ea = h.x & 0xff, eb2 = (h.x >> 8) & 0xff, k = (h.x >> 16) & 3;
+            const int nx = nvis == 1 ? (e == 2 ? 0 : e + 1) : P.se[eb2];
+            const int pv = nvis == 1 ? (e == 0 ? 2 : e - 1) : P.ee[ea];
+            const int s = e < nft ? P.freel[nft - 1 - e] : nslots + (e - nft);
+            const int sn = nx < nft ? P.freel[nft - 1 - nx] : nslots + (nx - nft);
+            const int sp = pv < nft ? P.freel[nft - 1 - pv] : nslots + (pv - nft);
+            float4 pl;
+            if (!plane_of(P, ea, eb2, vn, pl)) bad = true;
+            P.fn[s] = pl;
+            P.fv[s] = pack3(ea, eb2, vn);
+            P.adj[s] = make_ushort4((unsigned short)h.y, (unsigned short)sn, (unsigned short)sp, 0);
+            P.vis[s] = 0;
+            reinterpret_cast<unsigned short*>(&P.adj[h.y])[k] = (unsigned short)s;
+        }
+        if (__any_sync(kFull, bad)) return R;
+        nslots = ne > nft ? nslots + (ne - nft) : nslots;
+        nfree = ne < nft ? nft - ne : 0;
+        live = nlive;
+        __syncwarp();
+    }
+}
+
+// FP64 refinement of face f: its FP32 unit normal, renormalised in FP64,
+// n, and the depth along it from FP64 supports, mtv = n (n . w(n)) (the
+// reference's expression at convergence, epa.py:69).  n . w(n) is the support
+// depth h(n), an upper bound on the penetration depth for every n, and the
+// FP32 normal of the converged face is within the search's tolerance of the
+// optimal direction.
+__device__ __forceinline__ d3 refine_face(const Poly& P, const d3d_store& st, int a, int b, int f) {
+    const float4 fn = P.fn[f];
+    d3 n = mk((double)fn.x, (double)fn.y, (double)fn.z);
+    n = n * (1.0 / sqrt(dot(n, n)));
+    const d3 w = minkowski64(st, a, b, n);
+    return n * dot(w, n);
+}
+
+__global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
+                                                          const int32_t* __restrict__ i2, int64_t n,
+                                                          unsigned long long* __restrict__ cursor,
+                                                          const double* __restrict__ simplex, d3d_epa_options o,
+                                                          double* __restrict__ mtv, int8_t* __restrict__ status,
+                                                          int32_t* __restrict__ n_faces, double* __restrict__ faces,
+                                                          int32_t* __restrict__ fallback,
+                                                          unsigned long long* __restrict__ n_fallback) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const Layout L = layout_for(o);
+    const Poly P = poly_at(smem + (threadIdx.x >> 5) * L.bytes, L);
+    const int ln = lane_id();
+    while (true) {
+        long long k = 0;
+        if (ln == 0) k = (long long)atomicAdd(cursor, 1ull);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= n) break;
+        const int a = i1[k], b = i2[k];
+        const double* sx = simplex + 12 * k;
+        const Search R = search_pair(P, st, a, b, sx, o);
+        if (R.status == kEpaFallback) {
+            if (ln == 0) fallback[atomicAdd(n_fallback, 1ull)] = (int32_t)k;
+            __syncwarp();
+            continue;
+        }
+        d3 m = mk(double(NAN), double(NAN), double(NAN));
+        if (R.status == D3D_STATUS_OK || R.status == D3D_STATUS_EPA_NOT_CONVERGED) m = refine_face(P, st, a, b, R.closest);
+        const int nf = R.status == D3D_STATUS_EPA_DEGENERATE ? 0 : R.live;
+        if (ln == 0) {
+            mtv[3 * k] = m.x;
+            mtv[3 * k + 1] = m.y;
+            mtv[3 * k + 2] = m.z;
+            status[k] = (int8_t)R.status;
+            n_faces[k] = nf;
+        }
+        if (faces && nf > 0) {
+            // live faces in slot order: three vertices and the normal
+            double* out = faces + k * 12 * (int64_t)o.max_faces;
+            int base = 0;
+            for (int f0 = 0; f0 < R.nslots; f0 += 32) {
+                const int f = f0 + ln;
+                const bool live = f < R.nslots && P.fv[f] != kDead;
+                const unsigned mask = __ballot_sync(kFull, live);
+                if (live) {
+                    double* q = out + 12 * (base + __popc(mask & ((1u << ln) - 1u)));
+                    const unsigned fw = P.fv[f];
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        const float4 yy = P.vy[vid(fw, j)];
+                        q[3 * j] = yy.x;
+                        q[3 * j + 1] = yy.y;
+                        q[3 * j + 2] = yy.z;
+                    }
+                    const float4 pl = P.fn[f];
+                    q[9] = pl.x;
+                    q[10] = pl.y;
+                    q[11] = pl.z;
+                }
+                base += __popc(mask);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+namespace d3d {
+
+bool epa_warp_supported(const d3d_epa_options& o) {
+    if (o.max_iterations > 250 || o.max_loose_edges > 255 || o.max_faces > 65535) return false;
+    return (int64_t)layout_for(o).bytes * kWarps <= 227 * 1024;
+}
+
+int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n,
+                    unsigned long long* cursor, const double* simplex, const d3d_epa_options& o, double* mtv,
+                    int8_t* status, int32_t* n_faces, double* faces, int32_t* fallback,
+                    unsigned long long* n_fallback, cudaStream_t stream) {
+    const int smem = layout_for(o).bytes * kWarps;
+    cudaError_t e = cudaFuncSetAttribute(k_epa_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_epa_warp, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) {
+        set_error("d3d_epa (mixed): %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_epa_warp, 32 * kWarps, smem);
+    int64_t blocks = (int64_t)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    const int64_t need = (n + kWarps - 1) / kWarps;
+    if (blocks > need) blocks = need;
+    k_epa_warp<<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, n, cursor, simplex, o, mtv, status,
+                                                           n_faces, faces, fallback, n_fallback);
+    return check_launch("d3d_epa (mixed)");
+}
+
+}  // namespace d3d

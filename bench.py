@@ -35,6 +35,9 @@ SEED = 2024
 METRIC = "GJK+EPA pairs/s (mixed precision form; plain FP64 form alongside)"
 UNIT = "pairs/s"
 EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
+# this library's kernels per timed mixed step: k_pair_keys, k_gjk_mixed_a, _t, _b,
+# k_gjk_distance_f64 (fallback list); k_epa_warp, k_epa (fallback list)
+GJK_MIXED_LAUNCHES, EPA_MIXED_LAUNCHES = 5, 2
 
 # Algorithmic bytes per pair (counted once): two collider records, the hull
 # vertices of hull colliders, and the outputs.  FP64 record 120 B (pose 96 +
@@ -61,6 +64,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-seconds", type=float, default=2.0,
+                    help="seconds of Poisson arrivals per load level in the serving report (0: skip)")
     return ap.parse_args()
 
 
@@ -278,6 +283,45 @@ def run_reference(args):
     return 0
 
 
+def serve_report(store, i1_np, i2_np, seconds, seed=7):
+    """The continuous-batching server on the same resident store: peak pairs/s
+    with every request queued at once, then Poisson arrivals at 50/80/100% of
+    that peak, p50/p99 latency (arrival to results in host memory); mixed and
+    plain FP64 form.  Requests: lognormal pair counts (median 2,000, clipped
+    to [1, 50,000]) of pairs drawn from the batched workload."""
+    from distance3d_gb300.serve import CollisionServer, Request, latency_stats, request_sizes
+    rng = np.random.default_rng(seed)
+    mean_size = float(request_sizes(np.random.default_rng(seed + 1), 200000).mean())
+
+    def make(count):
+        sizes = request_sizes(rng, count)
+        reqs = []
+        for k, m in enumerate(sizes):
+            sel = rng.integers(0, len(i1_np), int(m))
+            reqs.append(Request(k, i1_np[sel], i2_np[sel], 0.0))
+        return reqs
+
+    out = {"request_pairs": {"median": 2000, "clip": [1, 50000], "mean": mean_size},
+           "latency": "arrival to results in host memory", "capacity": 65536, "slots": 2}
+    for precision in ("mixed", "fp64"):
+        srv = CollisionServer(store, capacity=65536, slots=2, precision=precision, epa_kw=EPA_KW)
+        warm = make(20)
+        srv.serve(warm, np.zeros(len(warm)))
+        burst = make(400 if precision == "mixed" else 60)
+        peak = latency_stats(srv.serve(burst, np.zeros(len(burst))))["pairs_per_s"]
+        res = {"peak_pairs_per_s": peak}
+        for load in (0.5, 0.8, 1.0):
+            rate = load * peak / mean_size
+            count = max(20, int(rate * seconds))
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+            st = latency_stats(srv.serve(make(count), arrivals))
+            res[f"load_{int(load * 100)}"] = {"offered_pairs_per_s": load * peak, "p50_ms": st["p50_ms"],
+                                              "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                                              "served_pairs_per_s": st["pairs_per_s"], "requests": count}
+        out[precision] = res
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -420,6 +464,7 @@ def run_ours(args):
 
     line = None
     if rank == 0:
+        serve = serve_report(store, i1_np, i2_np, args.serve_seconds) if args.serve_seconds > 0 else None
         cpu_value, cores, cpu_pairs, cpu_s = time_cpu(cs, i1_np, i2_np, args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -444,7 +489,8 @@ def run_ours(args):
             "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{cpu_pairs} pairs ({cpu_s:.1f} s) of the same workload, "
                                        "GJK + EPA, C restatement with OpenMP"},
-            "gpu_launches": 2 * args.steps,
+            "serve": serve,
+            "gpu_launches": GJK_MIXED_LAUNCHES * args.steps + EPA_MIXED_LAUNCHES * args.steps,
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -62,6 +62,9 @@ SIGNATURES = [
                         c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     ("d3d_epa_noalloc", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(EpaOptions),
                                 c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("d3d_collide_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions)]),
+    ("d3d_collide", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(GjkOptions),
+                            ctypes.POINTER(EpaOptions)] + [c_void_p] * 11 + [c_size_t, c_void_p]),
     ("d3d_bvh_bytes", c_size_t, [c_int64]),
     ("d3d_bvh_build", c_int, [c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
     ("d3d_bvh_query_bytes", c_size_t, [c_int64]),

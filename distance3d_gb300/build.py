@@ -38,6 +38,7 @@ UNITS = [
     ("epa_mixed.cu", ["-fmad=true"]),
     ("epa_warp.cu", ["-fmad=true"]),
     ("schedule.cu", []),
+    ("collide.cu", []),
     ("bvh.cu", []),
 ]
 

@@ -249,6 +249,27 @@ bool valid(const d3d_epa_options* o) {
 
 }  // namespace
 
+namespace d3d {
+
+int64_t epa_f64_slot_bytes(const d3d_epa_options& o) { return slot_doubles(o) * (int64_t)sizeof(double); }
+
+int epa_f64_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                   const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                   const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                   void* scratch, int64_t slots, cudaStream_t stream) {
+    int blocks = persistent_blocks((const void*)k_epa, kBlock, n);
+    if (blocks > slots / kBlock) blocks = (int)(slots / kBlock);
+    if (blocks < 1) {
+        set_error("d3d_epa: fewer than %d polytope slots", kBlock);
+        return D3D_ERR_CAPACITY;
+    }
+    k_epa<<<blocks, kBlock, 0, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces,
+                                         faces, static_cast<double*>(scratch), slot_doubles(o));
+    return check_launch("d3d_epa");
+}
+
+}  // namespace d3d
+
 extern "C" size_t d3d_epa_scratch_bytes(int64_t n, const d3d_epa_options* options) {
     if (!valid(options) || n <= 0) return 0;
     return (size_t)(slots_for(n) * slot_bytes_for(*options));
@@ -286,8 +307,8 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned long long), st);
     if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, p + 256 + order_bytes + fb_bytes, temp_bytes, st);
     if (!rc && warp)
-        rc = d3d::epa_warp_launch(*store, i1, i2, n, ctr, simplex, *options, mtv, status, n_faces, faces, fallback,
-                                  ctr + 2, st);
+        rc = d3d::epa_warp_launch(*store, i1, i2, nullptr, n, nullptr, ctr, simplex, *options, mtv, status, n_faces,
+                                  faces, fallback, ctr + 2, st);
     else if (!rc && mixed)
         rc = d3d::epa_mixed_launch(*store, i1, i2, order, n, ctr, simplex, *options, mtv, status, n_faces, faces,
                                    scratch, slots_for(n), fallback, ctr + 2, st);

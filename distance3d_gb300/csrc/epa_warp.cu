@@ -470,7 +470,9 @@ __device__ __forceinline__ d3 refine_face(const Poly& P, const d3d_store& st, in
 }
 
 __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
-                                                          const int32_t* __restrict__ i2, int64_t n,
+                                                          const int32_t* __restrict__ i2,
+                                                          const int32_t* __restrict__ list, int64_t n,
+                                                          const unsigned long long* __restrict__ n_dev,
                                                           unsigned long long* __restrict__ cursor,
                                                           const double* __restrict__ simplex, d3d_epa_options o,
                                                           double* __restrict__ mtv, int8_t* __restrict__ status,
@@ -481,11 +483,13 @@ __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const
     const Layout L = layout_for(o);
     const Poly P = poly_at(smem + (threadIdx.x >> 5) * L.bytes, L);
     const int ln = lane_id();
+    if (n_dev) n = (int64_t)*n_dev;
     while (true) {
-        long long k = 0;
-        if (ln == 0) k = (long long)atomicAdd(cursor, 1ull);
-        k = __shfl_sync(kFull, k, 0);
-        if (k >= n) break;
+        long long slot = 0;
+        if (ln == 0) slot = (long long)atomicAdd(cursor, 1ull);
+        slot = __shfl_sync(kFull, slot, 0);
+        if (slot >= n) break;
+        const int64_t k = list ? list[slot] : slot;
         const int a = i1[k], b = i2[k];
         const double* sx = simplex + 12 * k;
         const Search R = search_pair(P, st, a, b, sx, o);
@@ -543,10 +547,10 @@ bool epa_warp_supported(const d3d_epa_options& o) {
     return (int64_t)layout_for(o).bytes * kWarps <= 227 * 1024;
 }
 
-int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n,
-                    unsigned long long* cursor, const double* simplex, const d3d_epa_options& o, double* mtv,
-                    int8_t* status, int32_t* n_faces, double* faces, int32_t* fallback,
-                    unsigned long long* n_fallback, cudaStream_t stream) {
+int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                    const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                    const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
     const int smem = layout_for(o).bytes * kWarps;
     cudaError_t e = cudaFuncSetAttribute(k_epa_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
@@ -563,8 +567,8 @@ int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2
     int64_t blocks = (int64_t)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     const int64_t need = (n + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
-    k_epa_warp<<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, n, cursor, simplex, o, mtv, status,
-                                                           n_faces, faces, fallback, n_fallback);
+    k_epa_warp<<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv,
+                                                           status, n_faces, faces, fallback, n_fallback);
     return check_launch("d3d_epa (mixed)");
 }
 

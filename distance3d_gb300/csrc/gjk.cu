@@ -88,25 +88,42 @@ extern "C" int d3d_gjk_distance(const d3d_store* store, const int32_t* i1, const
         return d3d::gjk_distance_mixed(*store, i1, i2, n, *options, dist, cp1, cp2, simplex, n_simplex, status,
                                        iterations, d3d::as_stream(stream));
     cudaStream_t st = d3d::as_stream(stream);
-    const bool sched = n >= kScheduleMin;
-    const size_t order_bytes = sched ? ((sizeof(int32_t) * (size_t)n + 255) & ~size_t(255)) : 0;
-    const size_t temp_bytes = sched ? d3d::pair_order_temp_bytes(n) : 0;
     void* block = nullptr;
-    rc = d3d::scratch_alloc(&block, 256 + order_bytes + temp_bytes, st);
+    rc = d3d::scratch_alloc(&block, d3d::gjk_f64_scratch_bytes(n), st);
     if (rc) return rc;
-    unsigned long long* cursor = static_cast<unsigned long long*>(block);
-    int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(block) + 256) : nullptr;
-    cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
-    if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, static_cast<char*>(block) + 256 + order_bytes, temp_bytes, st);
-    if (!rc) {
-        DistanceOut o{dist, cp1, cp2, simplex, n_simplex, status, iterations};
-        rc = d3d::launch_gjk_f64(*store, i1, i2, order, n, nullptr, cursor, *options, o, st);
-    }
+    DistanceOut o{dist, cp1, cp2, simplex, n_simplex, status, iterations};
+    rc = d3d::gjk_f64_run(*store, i1, i2, n, nullptr, *options, o, block, st);
     d3d::scratch_free(block, st);
     return rc;
 }
 
 namespace d3d {
+
+size_t gjk_f64_scratch_bytes(int64_t capacity) {
+    if (capacity < kScheduleMin) return 256;
+    return 256 + ((sizeof(int32_t) * (size_t)capacity + 255) & ~size_t(255)) + pair_order_temp_bytes(capacity);
+}
+
+int gjk_f64_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n, const int64_t* n_dev,
+                const d3d_gjk_options& opt, const DistanceOut& o, void* scratch, cudaStream_t stream) {
+    const bool sched = n >= kScheduleMin;
+    unsigned long long* cursor = static_cast<unsigned long long*>(scratch);
+    int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + 256) : nullptr;
+    const size_t order_bytes = sched ? ((sizeof(int32_t) * (size_t)n + 255) & ~size_t(255)) : 0;
+    cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) {
+        set_error("d3d_gjk_distance: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    int rc = D3D_SUCCESS;
+    if (sched)
+        rc = pair_order(store, i1, i2, n, order, static_cast<char*>(scratch) + 256 + order_bytes,
+                        pair_order_temp_bytes(n), stream, n_dev);
+    if (!rc)
+        rc = launch_gjk_f64(store, i1, i2, order, n, reinterpret_cast<const unsigned long long*>(n_dev), cursor,
+                            opt, o, stream);
+    return rc;
+}
 
 int launch_gjk_f64(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
                    const unsigned long long* n_dev, unsigned long long* cursor, const d3d_gjk_options& opt,

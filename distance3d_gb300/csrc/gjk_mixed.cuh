@@ -45,15 +45,20 @@ struct RefineSupport {
     }
 };
 
-// Relative duality gap at which phase B stops; it bounds the relative
-// distance error of the mixed form (apart from the FP32 vertex choice).
-constexpr double kMixedRelGap = 1e-8;
+// Duality gap at which the FP64 refinement stops: the distance bracket
+// within 1e-7 of the distance, or within 1e-9 of the scene's scale
+// (max(1, |w|)) for nearly touching pairs, where the relative test would
+// chase FP32-resolution directions for dozens of FP64 iterations.  Both are
+// far below the form's 1e-5 tolerance on max(1, distance).
+constexpr double kMixedRelGap = 1e-7;
+constexpr double kMixedAbsGap2 = 1e-18;
 
 __device__ __forceinline__ JoltEps<float> fp32_eps() {
     const float e = FLT_EPSILON;
-    // plane/side tests and relative convergence at a few ulps; the touching
+    // plane/side tests at a few ulps, relative convergence at one ulp of
+    // |v|^2 (the FP64 refinement starts from this direction); the touching
     // test at the FP32 noise floor of |v|^2 relative to max|Y|^2
-    return JoltEps<float>{4.f * e, e * e, 4.f * e, 16.f * e * e, 0.f};
+    return JoltEps<float>{4.f * e, e * e, e, 16.f * e * e, 0.f};
 }
 
 enum PhaseAOutcome { PA_SEPARATED = 0, PA_TOUCHING = 1, PA_CLIPPED = 2, PA_FAILED = 3 };
@@ -133,23 +138,113 @@ __device__ __forceinline__ Handoff pa_handoff(const PhaseALoop& L, int outcome) 
 }
 
 // ---------------------------------------------------------------- phase B
-enum PhaseBMode { PB_RUN = 0, PB_DONE = 1, PB_FALLBACK = 2 };
+enum PhaseBMode { PB_RUN = 0, PB_DONE = 1, PB_FALLBACK = 2, PB_REPLAY = 3 };
 
-// Separated pairs: the reference's loop from the FP32 closest point's
-// direction instead of (1,0,0), with an empty simplex; pb_step stops it by the
-// duality gap.
+// FP64 refinement of one pair, a per-lane state machine.  REPLAY: A's final
+// simplex rows are re-evaluated in FP64 along the FP32 directions that
+// produced them, one row per round; after the last row the simplex is solved
+// as the loop's first iteration would (nothing to beat yet).  If it encloses
+// or touches the origin the pair is done; otherwise RUN continues the
+// reference's loop from there, stopped by the duality gap.
 template <typename Rows>
-__device__ __forceinline__ void pb_begin(GjkLoop<double, Rows>& g, float4 v) {
-    simplex_clear(g.S);
-    const d3 dir = mk(-(double)v.x, -(double)v.y, -(double)v.z);
-    gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
+struct PhaseB {
+    GjkLoop<double, Rows> g;
+    int mode;
+    int row, rows;
+};
+
+template <typename Rows>
+__device__ __forceinline__ void pb_begin(PhaseB<Rows>& B, float4 v) {
+    simplex_clear(B.g.S);
+    B.g.it = 0;
+    B.g.state = GJK_RUNNING;
+    B.g.status = D3D_STATUS_OK;
+    B.row = 0;
+    const int outcome = __float_as_int(v.w) & 0xff;
+    B.rows = (__float_as_int(v.w) >> 8) & 0xff;
+    B.mode = (outcome == PA_SEPARATED || outcome == PA_TOUCHING) && B.rows > 0 ? PB_REPLAY : PB_FALLBACK;
 }
 
+// One round for one lane: one pair of FP64 supports, along the next replayed
+// row direction (REPLAY, from `dirs`) or the loop's direction (RUN), then the
+// simplex update (_gjk_jolt.py:224-288).  Returns true once the loop has
+// ended: g.state is GJK_INTERSECTION or GJK_NO_INTERSECTION (pb_end finishes
+// the pair), or B.mode is PB_FALLBACK (clipped, iteration bound, failed
+// replay).
 template <typename Rows>
-__device__ __forceinline__ bool pb_step(GjkLoop<double, Rows>& g, const d3d_store& s, int a, int b, double tol_sq,
-                                        const d3d_gjk_options& opt, const JoltEps<double>& E) {
-    return gjk_step<double, RefineSupport, true>(g, s, a, b, tol_sq, opt.max_distance_squared, opt.max_iterations,
-                                                 E, kMixedRelGap);
+__device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, int a, int b,
+                                         const float4* __restrict__ dirs, double tol_sq, const d3d_gjk_options& opt,
+                                         const JoltEps<double>& E) {
+    GjkLoop<double, Rows>& g = B.g;
+    const bool replay = B.mode == PB_REPLAY;
+    d3 d = g.dir;
+    if (replay) {
+        const float4 f = dirs[B.row];
+        d = mk((double)f.x, (double)f.y, (double)f.z);
+    } else {
+        if (g.it >= opt.max_iterations) {
+            B.mode = PB_FALLBACK;
+            return true;
+        }
+        ++g.it;
+    }
+    d3 p, q;
+    pair_supports<double, RefineSupport>(s, a, b, d, p, q);
+    const d3 w = p - q;
+    if (!replay) {
+        const double dd = dot(g.dir, w);
+        if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
+            B.mode = PB_FALLBACK;  // clipped: the FP64 kernel reports it
+            return true;
+        }
+        if (g.S.n > 0) {
+            // duality gap: |v| - (|v|^2 - v.w) / |v| <= distance <= |v|
+            const double gap = g.vl + dd;
+            if (gap <= kMixedRelGap * g.vl || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl) {
+                g.dir = -g.dir;
+                g.state = GJK_NO_INTERSECTION;
+                return true;
+            }
+        }
+    }
+    simplex_push(g.S, w, p, q);
+    if (replay && ++B.row < B.rows) return false;
+    d3 nv;
+    double nl;
+    int set;
+    const double prev = replay ? DBL_MAX : g.prev;
+    if (closest_to_origin(g.S, prev, E, nv, nl, set)) {
+        g.dir = nv;
+        g.vl = nl;
+    } else if (replay) {
+        B.mode = PB_FALLBACK;
+        return true;
+    } else {
+        --g.S.n;
+        set = (1 << g.S.n) - 1;
+    }
+    if (replay) {
+        B.mode = PB_RUN;
+        g.prev = DBL_MAX;
+    }
+    if (set == 15) {
+        g.vl = 0.0;
+        g.state = GJK_INTERSECTION;
+        return true;
+    }
+    simplex_compact<double, true>(g.S, set);
+    if (g.vl <= tol_sq || g.vl <= E.isect * max_y_len_sq(g.S)) {
+        g.vl = 0.0;
+        g.state = GJK_INTERSECTION;
+        return true;
+    }
+    g.dir = -g.dir;
+    if (g.prev - g.vl <= E.conv * g.prev) {
+        g.state = GJK_NO_INTERSECTION;
+        return true;
+    }
+    g.prev = g.vl;
+    return false;
 }
 
 // Finish a pair after its loop.  The closest points use the scale-invariant
@@ -165,44 +260,6 @@ __device__ __forceinline__ int pb_end(const GjkLoop<double, Rows>& g, const d3d_
     const d3 ab = r.a - r.b;
     if (abs_t(sqrt_t(dot(ab, ab)) - r.dist) > 1e-10 * (r.dist > 1.0 ? r.dist : 1.0)) return PB_FALLBACK;
     return PB_DONE;
-}
-
-// Touching pairs: the FP32 simplex rows re-evaluated in FP64 along the
-// directions that produced them (h: the pair's handoff record in memory).  If that simplex encloses (or touches) the
-// origin the pair is done (r filled, PB_DONE); otherwise g is left ready for
-// the loop to resume there (PB_RUN).
-template <typename Rows>
-__device__ __forceinline__ int pt_replay(GjkLoop<double, Rows>& g, const d3d_store& s, int a, int b,
-                                         const Handoff* __restrict__ h, double tol_sq, const JoltEps<double>& E,
-                                         GjkResult<double>& r) {
-    simplex_clear(g.S);
-    g.it = 0;
-    const int rows = handoff_rows(*h);
-#pragma unroll 1
-    for (int j = 0; j < rows; ++j) {
-        const float4 f = h->d[j];
-        d3 p, q;
-        pair_supports<double, RefineSupport>(s, a, b, mk((double)f.x, (double)f.y, (double)f.z), p, q);
-        simplex_push(g.S, p - q, p, q);
-    }
-    d3 v;
-    double vl;
-    int set;
-    if (g.S.n == 0 || !closest_to_origin(g.S, DBL_MAX, E, v, vl, set)) return PB_FALLBACK;
-    if (set != 15) simplex_compact<double, true>(g.S, set);
-    if (set == 15 || vl <= tol_sq || vl <= E.isect * max_y_len_sq(g.S)) {
-        d3 ca, cb;
-        closest_points<double, true>(g.S, E, ca, cb);
-        const d3 m = (ca + cb) * 0.5;
-        r.dist = 0.0;
-        r.a = m;
-        r.b = m;
-        r.status = D3D_STATUS_OK;
-        r.iters = 0;
-        return PB_DONE;
-    }
-    gjk_begin(g, -v, vl, vl);
-    return PB_RUN;
 }
 
 }  // namespace d3d

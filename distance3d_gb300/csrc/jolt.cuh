@@ -12,6 +12,9 @@
 namespace d3d {
 
 template <typename T>
+__device__ __forceinline__ T maxf2(T a, T b) { return a > b ? a : b; }
+
+template <typename T>
 __device__ __forceinline__ T maxf();
 template <>
 __device__ __forceinline__ double maxf<double>() { return DBL_MAX; }
@@ -484,12 +487,13 @@ __device__ __forceinline__ void gjk_begin(GjkLoop<T, Rows>& g, V3<T> dir, T vl, 
 //
 // GAP adds the duality-gap termination of van den Bergen's GJK, which the
 // reference does not have: with v the current closest point and w the new
-// support point along -v, |v|^2 - v.w <= rel_gap |v|^2 bounds the relative
-// error of |v| by rel_gap, and the loop stops there.  The FP64 drop-in is
-// compiled without it.
+// support point along -v, |v| - (|v|^2 - v.w) / |v| <= distance <= |v|.  The
+// loop stops once that bracket is within rel_gap |v| (relative) or within
+// sqrt(abs_gap2) max(1, |w|) (absolute, on the scene's scale).  The FP64
+// drop-in is compiled without it.
 template <typename T, typename Sup = ExactSupport, bool GAP = false, typename Rows>
 __device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
-                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0)) {
+                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0), T abs_gap2 = T(0)) {
     if (g.it >= max_iter) {
         g.status = D3D_STATUS_MAX_ITER;
         g.state = GJK_NO_INTERSECTION;
@@ -504,10 +508,14 @@ __device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& s
         g.state = GJK_CLIPPED;
         return true;
     }
-    if (GAP && g.S.n > 0 && -dd >= g.vl * (T(1) - rel_gap)) {
-        g.dir = -g.dir;  // the state the reference leaves on convergence
-        g.state = GJK_NO_INTERSECTION;
-        return true;
+    if (GAP && g.S.n > 0) {
+        // gap = |v|^2 - v.w >= 0 (up to rounding): |v| - gap / |v| <= distance <= |v|
+        const T gap = g.vl + dd;
+        if (gap <= rel_gap * g.vl || gap * gap <= abs_gap2 * maxf2(T(1), dot(w, w)) * g.vl) {
+            g.dir = -g.dir;  // the state the reference leaves on convergence
+            g.state = GJK_NO_INTERSECTION;
+            return true;
+        }
     }
     simplex_push(g.S, w, p, q);
     V3<T> nv;
@@ -570,8 +578,8 @@ __device__ __forceinline__ void gjk_end(const GjkLoop<T, Rows>& g, T sanity, con
 template <typename T, typename Sup = ExactSupport, bool GAP = false, bool SCALED = false, typename Rows>
 __device__ __forceinline__ void gjk_run(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
                                         T sanity, int max_iter, const JoltEps<T>& E, GjkResult<T>& out,
-                                        T rel_gap = T(0)) {
-    while (!gjk_step<T, Sup, GAP>(g, st, a, b, tol_sq, max_d2, max_iter, E, rel_gap)) {
+                                        T rel_gap = T(0), T abs_gap2 = T(0)) {
+    while (!gjk_step<T, Sup, GAP>(g, st, a, b, tol_sq, max_d2, max_iter, E, rel_gap, abs_gap2)) {
     }
     gjk_end<T, SCALED>(g, sanity, E, out);
 }

@@ -15,18 +15,24 @@ cudaMemPool_t g_pool[kMaxDevices] = {};
 
 inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
-// key = ((type1 * 6 + type2) << 4) | size class of the larger hull
+// key = ((type1 * 6 + type2) << 4) | size class of the larger hull; slots at
+// and beyond the device-side count (if given) get the largest key
 __global__ void k_pair_keys(d3d_store s, const int32_t* __restrict__ i1, const int32_t* __restrict__ i2, int64_t n,
-                            uint32_t* __restrict__ keys, int32_t* __restrict__ vals) {
+                            const int64_t* __restrict__ n_dev, uint32_t* __restrict__ keys,
+                            int32_t* __restrict__ vals) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    vals[k] = (int32_t)k;
+    if (n_dev && k >= *n_dev) {
+        keys[k] = 0x7ffu;
+        return;
+    }
     int4 a = __ldg(reinterpret_cast<const int4*>(s.meta) + i1[k]);
     int4 b = __ldg(reinterpret_cast<const int4*>(s.meta) + i2[k]);
     int nv = max(a.x == D3D_HULL ? a.y : 0, b.x == D3D_HULL ? b.y : 0);
     int cls = nv > 0 ? min(32 - __clz(nv), 15) : 0;
     unsigned ta = (unsigned)min(max(a.x, 0), 5), tb = (unsigned)min(max(b.x, 0), 5);
     keys[k] = ((ta * 6u + tb) << 4) | (unsigned)cls;
-    vals[k] = (int32_t)k;
 }
 
 }  // namespace
@@ -85,12 +91,12 @@ int persistent_blocks(const void* kernel, int block, int64_t work_items) {
 size_t pair_order_temp_bytes(int64_t n) {
     size_t cub_bytes = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
-                                    (const int32_t*)nullptr, (int32_t*)nullptr, (int)n, 0, 10);
+                                    (const int32_t*)nullptr, (int32_t*)nullptr, (int)n, 0, 11);
     return 2 * align_up(sizeof(uint32_t) * (size_t)n) + align_up(sizeof(int32_t) * (size_t)n) + align_up(cub_bytes);
 }
 
 int pair_order(const d3d_store& s, const int32_t* i1, const int32_t* i2, int64_t n, int32_t* order, void* temp,
-               size_t temp_bytes, cudaStream_t stream) {
+               size_t temp_bytes, cudaStream_t stream, const int64_t* n_dev) {
     if (n <= 0) return D3D_SUCCESS;
     if (temp_bytes < pair_order_temp_bytes(n)) {
         set_error("pair_order: temporary storage too small");
@@ -104,9 +110,9 @@ int pair_order(const d3d_store& s, const int32_t* i1, const int32_t* i2, int64_t
     int32_t* vals = reinterpret_cast<int32_t*>(t);
     t += align_up(sizeof(int32_t) * (size_t)n);
     size_t cub_bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, keys, keys_out, vals, order, (int)n, 0, 10, stream);
-    k_pair_keys<<<grid_for(n, 256), 256, 0, stream>>>(s, i1, i2, n, keys, vals);
-    cudaError_t e = cub::DeviceRadixSort::SortPairs(t, cub_bytes, keys, keys_out, vals, order, (int)n, 0, 10, stream);
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, keys, keys_out, vals, order, (int)n, 0, 11, stream);
+    k_pair_keys<<<grid_for(n, 256), 256, 0, stream>>>(s, i1, i2, n, n_dev, keys, vals);
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(t, cub_bytes, keys, keys_out, vals, order, (int)n, 0, 11, stream);
     if (e != cudaSuccess) {
         set_error("pair_order: sort failed: %s", cudaGetErrorString(e));
         return D3D_ERR_CUDA;

@@ -170,6 +170,23 @@ int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const int32_t* i2
                     const double* simplex, const d3d_epa_options* options, double* mtv, int8_t* status,
                     int32_t* n_faces, double* faces, void* stream);
 
+/* GJK distance then EPA, for a batch whose pair count lives on the device.
+ * Replaces the reference's composition gjk() -> epa(simplex) on intersecting
+ * pairs (gjk/_gjk_jolt.py:138-221, epa.py:9-78) for a whole batch.  Pairs
+ * k < *n_dev of buffers sized `capacity`: GJK outputs as d3d_gjk_distance
+ * (precision gjk->precision); then EPA (precision epa->precision) on the
+ * pairs with dist == 0 and n_simplex == 4, found on the device.  Pairs without
+ * EPA get epa_status -1, NaN mtv and n_faces 0.  No host synchronisation and
+ * no allocation (scratch of d3d_collide_scratch_bytes bytes); the launch
+ * shapes depend on `capacity` only, so a CUDA graph captured around one call
+ * serves any *n_dev <= capacity when replayed. */
+size_t d3d_collide_scratch_bytes(int64_t capacity, const d3d_gjk_options* gjk, const d3d_epa_options* epa);
+int d3d_collide(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t capacity,
+                const int64_t* n_dev, const d3d_gjk_options* gjk, const d3d_epa_options* epa, double* dist,
+                double* cp1, double* cp2, double* simplex, int8_t* n_simplex, int8_t* status, int32_t* iterations,
+                double* mtv, int8_t* epa_status, int32_t* n_faces, void* scratch, size_t scratch_bytes,
+                void* stream);
+
 /* ------------------------------------------------------------------ broad phase
  * A linear BVH over FP64 boxes aabbs[n][3][2] ([axis][min,max]).  The tree
  * lives in a caller buffer of d3d_bvh_bytes(n) bytes (layout private) and

@@ -1,0 +1,84 @@
+"""The device-count batch (d3d_collide), its CUDA graphs and the
+continuous-batching server: same results as the separate calls, graph and
+eager identical, and every request's result identical alone and in the mix."""
+import numpy as np
+import pytest
+
+from distance3d_gb300 import workloads
+from distance3d_gb300.epa import epa_batch
+from distance3d_gb300.gjk import gjk_distance_batch
+from distance3d_gb300.serve import CollisionBatch, CollisionServer, Request, request_sizes
+from distance3d_gb300.store import ColliderStore
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
+
+
+def host(r):
+    return {k: v.cpu().numpy() for k, v in r.items()}
+
+
+@pytest.fixture(scope="module")
+def scene():
+    cs, i1, i2 = workloads.pairs_mixed_six(60000, seed=41, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    return cs, ColliderStore(cs), np.asarray(i1), np.asarray(i2)
+
+
+def separate_calls(st, i1, i2, precision):
+    g = host(gjk_distance_batch(st, i1, i2, precision=precision))
+    hit = np.flatnonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4))
+    e = host(epa_batch(st, i1[hit], i2[hit], g["simplex"][hit], precision=precision, **EPA_KW))
+    return g, hit, e
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_collide_equals_separate_calls(scene, precision):
+    cs, st, i1, i2 = scene
+    n = 20000
+    b = CollisionBatch(st, 32768, precision=precision, epa_kw=EPA_KW, graphs=True)
+    r = b.run(i1[:n], i2[:n])
+    g, hit, e = separate_calls(st, i1[:n], i2[:n], precision)
+    for k in ("dist", "cp1", "cp2", "simplex", "n_simplex", "status", "iterations"):
+        assert np.array_equal(r[k], g[k], equal_nan=True), k
+    assert np.array_equal(r["epa_status"][hit], e["status"])
+    assert np.array_equal(r["mtv"][hit], e["mtv"], equal_nan=True)
+    assert np.array_equal(r["n_faces"][hit], e["n_faces"])
+    rest = np.setdiff1d(np.arange(n), hit)
+    assert np.all(r["epa_status"][rest] == -1) and np.all(np.isnan(r["mtv"][rest]))
+    if precision == "fp64":
+        ref = oracle.gjk_distance(cs, i1[:n], i2[:n])
+        assert np.array_equal(r["dist"], ref["dist"]) and np.array_equal(r["simplex"], ref["simplex"])
+
+
+def test_graph_and_eager_identical_every_size(scene):
+    _, st, i1, i2 = scene
+    gb = CollisionBatch(st, 16384, precision="mixed", epa_kw=EPA_KW, graphs=True, classes=[1024, 16384])
+    eb = CollisionBatch(st, 16384, precision="mixed", epa_kw=EPA_KW, graphs=False, classes=[1024, 16384])
+    for n in (0, 1, 7, 1024, 1025, 9000, 16384):
+        a, b = gb.run(i1[:n], i2[:n]), eb.run(i1[:n], i2[:n])
+        for k in a:
+            assert np.array_equal(a[k], b[k], equal_nan=True), (n, k)
+
+
+def test_results_same_alone_and_in_the_mix(scene):
+    _, st, i1, i2 = scene
+    rng = np.random.default_rng(5)
+    sizes = list(request_sizes(rng, 24)) + [1, 70000 % 60000, 45000]
+    reqs, alone = [], []
+    ref = CollisionBatch(st, 65536, precision="mixed", epa_kw=EPA_KW, graphs=False)
+    for k, m in enumerate(sizes):
+        sel = rng.integers(0, len(i1), int(m))
+        reqs.append(Request(k, i1[sel].astype(np.int32), i2[sel].astype(np.int32), 0.0))
+        alone.append(ref.run(i1[sel], i2[sel]))
+    # small capacity: big requests are split over batches, batches overlap
+    srv = CollisionServer(st, capacity=16384, slots=3, precision="mixed", epa_kw=EPA_KW)
+    arrivals = np.sort(rng.uniform(0.0, 0.02, len(reqs)))
+    srv.serve(reqs, arrivals)
+    for r, a in zip(reqs, alone):
+        assert r.finished is not None and r.finished >= r.arrival
+        for k in a:
+            assert np.array_equal(r.result[k], a[k], equal_nan=True), (r.rid, k)
+
+

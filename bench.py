@@ -283,41 +283,46 @@ def run_reference(args):
     return 0
 
 
-def serve_report(store, i1_np, i2_np, seconds, seed=7):
-    """The continuous-batching server on the same resident store: peak pairs/s
-    with every request queued at once, then Poisson arrivals at 50/80/100% of
-    that peak, p50/p99 latency (arrival to results in host memory); mixed and
+def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=16384, slots=4):
+    """The continuous-batching server (the library's native server) on the
+    same resident store: peak pairs/s with a burst of requests all arriving
+    at once, then Poisson arrivals at 50/80/100% of that peak; latency from
+    each request's arrival to its results in host memory, p50/p99.  Mixed and
     plain FP64 form.  Requests: lognormal pair counts (median 2,000, clipped
     to [1, 50,000]) of pairs drawn from the batched workload."""
-    from distance3d_gb300.serve import CollisionServer, Request, latency_stats, request_sizes
+    from distance3d_gb300.serve import NativeCollisionServer, request_sizes
     rng = np.random.default_rng(seed)
     mean_size = float(request_sizes(np.random.default_rng(seed + 1), 200000).mean())
 
-    def make(count):
+    def trace(count):
         sizes = request_sizes(rng, count)
-        reqs = []
-        for k, m in enumerate(sizes):
-            sel = rng.integers(0, len(i1_np), int(m))
-            reqs.append(Request(k, i1_np[sel], i2_np[sel], 0.0))
-        return reqs
+        sel = rng.integers(0, len(i1_np), int(sizes.sum()))
+        return sizes, i1_np[sel], i2_np[sel]
 
     out = {"request_pairs": {"median": 2000, "clip": [1, 50000], "mean": mean_size},
-           "latency": "arrival to results in host memory", "capacity": 65536, "slots": 2}
+           "latency": "arrival to results in host memory", "server": "native (d3d_server), CUDA graphs",
+           "capacity": capacity, "slots": slots}
     for precision in ("mixed", "fp64"):
-        srv = CollisionServer(store, capacity=65536, slots=2, precision=precision, epa_kw=EPA_KW)
-        warm = make(20)
-        srv.serve(warm, np.zeros(len(warm)))
-        burst = make(400 if precision == "mixed" else 60)
-        peak = latency_stats(srv.serve(burst, np.zeros(len(burst))))["pairs_per_s"]
-        res = {"peak_pairs_per_s": peak}
-        for load in (0.5, 0.8, 1.0):
-            rate = load * peak / mean_size
-            count = max(20, int(rate * seconds))
-            arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
-            st = latency_stats(srv.serve(make(count), arrivals))
-            res[f"load_{int(load * 100)}"] = {"offered_pairs_per_s": load * peak, "p50_ms": st["p50_ms"],
-                                              "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
-                                              "served_pairs_per_s": st["pairs_per_s"], "requests": count}
+        srv = NativeCollisionServer(store, capacity=capacity, slots=slots, precision=precision, epa_kw=EPA_KW)
+        try:
+            sz, a, b = trace(20)
+            srv.replay(sz, a, b, np.zeros(len(sz)))
+            sz, a, b = trace(600 if precision == "mixed" else 60)
+            lat, span = srv.replay(sz, a, b, np.zeros(len(sz)))
+            peak = float(sz.sum()) / span
+            res = {"peak_pairs_per_s": peak}
+            for load in (0.5, 0.8, 1.0):
+                rate = load * peak / mean_size
+                count = max(20, int(rate * seconds))
+                sz, a, b = trace(count)
+                offsets = np.cumsum(rng.exponential(1.0 / rate, count))
+                lat, span = srv.replay(sz, a, b, offsets)
+                res[f"load_{int(load * 100)}"] = {
+                    "offered_pairs_per_s": load * peak, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                    "p99_ms": float(np.percentile(lat, 99) * 1e3), "max_ms": float(lat.max() * 1e3),
+                    "served_pairs_per_s": float(sz.sum()) / span, "requests": count}
+        finally:
+            srv.close()
         out[precision] = res
     return out
 

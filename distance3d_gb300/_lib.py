@@ -35,6 +35,16 @@ class EpaOptions(ctypes.Structure):
                 ("precision", c_int32), ("epsilon", c_double)]
 
 
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("capacity", ctypes.c_int64), ("slots", ctypes.c_int32), ("use_graphs", ctypes.c_int32),
+                ("hbm_budget", ctypes.c_int64)]
+
+
+class PairResults(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("dist", "cp1", "cp2", "simplex", "n_simplex", "status",
+                                               "iterations", "mtv", "epa_status", "n_faces")]
+
+
 class D3DError(RuntimeError):
     """A libd3d_gb300 entry point returned an error code."""
 
@@ -65,6 +75,14 @@ SIGNATURES = [
     ("d3d_collide_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions)]),
     ("d3d_collide", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(GjkOptions),
                             ctypes.POINTER(EpaOptions)] + [c_void_p] * 11 + [c_size_t, c_void_p]),
+    ("d3d_server_create", c_int, [_SP, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions),
+                                  ctypes.POINTER(ServerOptions), ctypes.POINTER(c_void_p)]),
+    ("d3d_server_destroy", None, [c_void_p]),
+    ("d3d_server_submit", c_int, [c_void_p, c_void_p, c_void_p, c_int64, ctypes.POINTER(c_int64)]),
+    ("d3d_server_wait", c_int, [c_void_p, c_int64, c_double]),
+    ("d3d_server_result", c_int, [c_void_p, c_int64, ctypes.POINTER(PairResults), ctypes.POINTER(c_double)]),
+    ("d3d_server_replay", c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                  ctypes.POINTER(c_double)]),
     ("d3d_bvh_bytes", c_size_t, [c_int64]),
     ("d3d_bvh_build", c_int, [c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
     ("d3d_bvh_query_bytes", c_size_t, [c_int64]),

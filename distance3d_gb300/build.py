@@ -39,6 +39,7 @@ UNITS = [
     ("epa_warp.cu", ["-fmad=true"]),
     ("schedule.cu", []),
     ("collide.cu", []),
+    ("server.cu", []),
     ("bvh.cu", []),
 ]
 

@@ -276,3 +276,77 @@ def latency_stats(requests):
 def request_sizes(rng, n, median=2000, sigma=1.0, lo=1, hi=50000):
     """Pairs per request: lognormal with the given median, clipped to [lo, hi]."""
     return np.clip(np.round(rng.lognormal(np.log(median), sigma, n)), lo, hi).astype(np.int64)
+
+
+class NativeCollisionServer:
+    """The C++ continuous-batching server (``d3d_server_*``): the same
+    admission and batching as ``CollisionServer``, run by a worker thread in
+    the library with one CUDA graph per capacity class and slot.  ``submit``
+    copies a request's host pairs and returns its id; ``result`` waits for it
+    and returns host arrays plus its latency; ``replay`` submits a whole
+    arrival trace from the library (so the arrival times are kept to the
+    microsecond) and returns the per-request latencies."""
+
+    def __init__(self, store, *, capacity=65536, slots=2, precision="mixed", epa_kw=None, gjk_kw=None, graphs=True,
+                 hbm_budget=0):
+        if precision not in _PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
+        ek = dict(max_iter=64, max_loose_edges=32, max_faces=64, epsilon=1e-8)
+        ek.update(epa_kw or {})
+        gk = dict(tolerance=1e-10, max_distance_squared=100000.0, sanity_check=1e-8, max_iterations=1024)
+        gk.update(gjk_kw or {})
+        self._gjk = _lib.GjkOptions(gk["tolerance"], gk["max_distance_squared"], gk["sanity_check"],
+                                    int(gk["max_iterations"]), _PRECISIONS[precision])
+        self._epa = _lib.EpaOptions(int(ek["max_iter"]), int(ek["max_loose_edges"]), int(ek["max_faces"]),
+                                    _PRECISIONS[precision], float(ek["epsilon"]))
+        self.store = store  # the server reads the store's device buffers
+        self._lib = _lib.load()
+        opt = _lib.ServerOptions(int(capacity), int(slots), 1 if graphs else 0, int(hbm_budget))
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(store.device):
+            torch.cuda.synchronize(store.device)
+            _lib.check(self._lib.d3d_server_create(store.view, ctypes.byref(self._gjk), ctypes.byref(self._epa),
+                                                   ctypes.byref(opt), ctypes.byref(handle)))
+        self._h = handle
+
+    def close(self):
+        if self._h:
+            self._lib.d3d_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, i1, i2):
+        a = np.ascontiguousarray(i1, dtype=np.int32)
+        b = np.ascontiguousarray(i2, dtype=np.int32)
+        rid = ctypes.c_int64()
+        _lib.check(self._lib.d3d_server_submit(self._h, a.ctypes.data, b.ctypes.data, len(a), ctypes.byref(rid)))
+        return rid.value, len(a)
+
+    def result(self, ticket, timeout=60.0):
+        rid, n = ticket
+        _lib.check(self._lib.d3d_server_wait(self._h, rid, float(timeout)))
+        out = {k: np.empty((n,) + tuple(s), dtype=torch.empty((), dtype=d).numpy().dtype) for k, d, s in _OUTPUTS}
+        pr = _lib.PairResults(*[out[k].ctypes.data for k, _, _ in _OUTPUTS])
+        lat = ctypes.c_double()
+        _lib.check(self._lib.d3d_server_result(self._h, rid, ctypes.byref(pr), ctypes.byref(lat)))
+        return out, lat.value
+
+    def replay(self, sizes, i1, i2, offsets):
+        """Requests of sizes[k] pairs (concatenated in i1/i2) arriving at
+        offsets[k] seconds; returns (latencies in seconds, span in seconds)."""
+        sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+        offs = np.ascontiguousarray(offsets, dtype=np.float64)
+        a = np.ascontiguousarray(i1, dtype=np.int32)
+        b = np.ascontiguousarray(i2, dtype=np.int32)
+        if a.size != sizes.sum() or b.size != a.size or offs.size != sizes.size:
+            raise ValueError("sizes, offsets and pair arrays disagree")
+        lat = np.empty(len(sizes))
+        span = ctypes.c_double()
+        _lib.check(self._lib.d3d_server_replay(self._h, len(sizes), offs.ctypes.data, sizes.ctypes.data,
+                                               a.ctypes.data, b.ctypes.data, lat.ctypes.data, ctypes.byref(span)))
+        return lat, span.value

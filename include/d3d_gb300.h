@@ -187,6 +187,48 @@ int d3d_collide(const d3d_store* store, const int32_t* i1, const int32_t* i2, in
                 double* mtv, int8_t* epa_status, int32_t* n_faces, void* scratch, size_t scratch_bytes,
                 void* stream);
 
+/* Continuous-batching collision server over one resident store (no
+ * counterpart in the reference, which answers one pair per call).  A worker
+ * thread batches submitted requests (host pair lists) into up to `slots`
+ * d3d_collide batches in flight, each within `capacity` pairs, all within
+ * `hbm_budget` bytes of pair slots (0: slots x capacity x 315 B); large
+ * requests are split over batches.  `use_graphs` replays one CUDA graph per
+ * capacity class.  Results per pair are d3d_collide's; latency runs from
+ * submission to the request's results being in host memory.  The store must
+ * outlive the server. */
+typedef struct d3d_server d3d_server;
+typedef struct {
+    int64_t capacity;
+    int32_t slots;
+    int32_t use_graphs;
+    int64_t hbm_budget;
+} d3d_server_options;
+/* host output arrays of one request (n pairs), any may be NULL */
+typedef struct {
+    double* dist;       /* n */
+    double* cp1;        /* n x 3 */
+    double* cp2;        /* n x 3 */
+    double* simplex;    /* n x 4 x 3 */
+    int8_t* n_simplex;  /* n */
+    int8_t* status;     /* n */
+    int32_t* iterations;
+    double* mtv;        /* n x 3 */
+    int8_t* epa_status; /* n, -1 where no EPA ran */
+    int32_t* n_faces;   /* n */
+} d3d_pair_results;
+int d3d_server_create(const d3d_store* store, const d3d_gjk_options* gjk, const d3d_epa_options* epa,
+                      const d3d_server_options* options, d3d_server** out);
+void d3d_server_destroy(d3d_server* server);
+int d3d_server_submit(d3d_server* server, const int32_t* i1, const int32_t* i2, int64_t n, int64_t* request_id);
+int d3d_server_wait(d3d_server* server, int64_t request_id, double timeout_s);
+int d3d_server_result(d3d_server* server, int64_t request_id, const d3d_pair_results* out, double* latency_s);
+/* Submit n_requests requests at offsets_s[k] seconds from the call (sizes[k]
+ * pairs each, concatenated in i1/i2), wait for all, return each one's
+ * latency (from its scheduled arrival) and the span from the call to the
+ * last finish; results are discarded. */
+int d3d_server_replay(d3d_server* server, int64_t n_requests, const double* offsets_s, const int64_t* sizes,
+                      const int32_t* i1, const int32_t* i2, double* latency_s, double* span_s);
+
 /* ------------------------------------------------------------------ broad phase
  * A linear BVH over FP64 boxes aabbs[n][3][2] ([axis][min,max]).  The tree
  * lives in a caller buffer of d3d_bvh_bytes(n) bytes (layout private) and

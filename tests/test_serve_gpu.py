@@ -82,3 +82,42 @@ def test_results_same_alone_and_in_the_mix(scene):
             assert np.array_equal(r.result[k], a[k], equal_nan=True), (r.rid, k)
 
 
+
+
+def test_native_server_same_alone_and_in_the_mix(scene):
+    from distance3d_gb300.serve import NativeCollisionServer
+    _, st, i1, i2 = scene
+    rng = np.random.default_rng(9)
+    sizes = [int(m) for m in request_sizes(rng, 30)] + [1, 40000, 0]
+    ref = CollisionBatch(st, 65536, precision="mixed", epa_kw=EPA_KW, graphs=False)
+    srv = NativeCollisionServer(st, capacity=16384, slots=3, precision="mixed", epa_kw=EPA_KW)
+    try:
+        sels = [rng.integers(0, len(i1), m) for m in sizes]
+        tickets = [srv.submit(i1[s], i2[s]) for s in sels]
+        for s, t in zip(sels, tickets):
+            out, lat = srv.result(t)
+            alone = ref.run(i1[s], i2[s])
+            assert lat >= 0.0
+            for k in alone:
+                assert np.array_equal(out[k], alone[k], equal_nan=True), (len(s), k)
+        # replayed arrival trace: every request answered, latencies positive
+        sz = request_sizes(rng, 50)
+        sel = rng.integers(0, len(i1), int(sz.sum()))
+        lat, span = srv.replay(sz, i1[sel], i2[sel], np.sort(rng.uniform(0, 0.05, len(sz))))
+        assert np.all(lat > 0) and span > 0
+    finally:
+        srv.close()
+
+
+def test_native_server_rejects_bad_pairs(scene):
+    from distance3d_gb300 import _lib
+    from distance3d_gb300.serve import NativeCollisionServer
+    _, st, i1, i2 = scene
+    srv = NativeCollisionServer(st, capacity=4096, slots=1, precision="mixed", epa_kw=EPA_KW, graphs=False)
+    try:
+        with pytest.raises(_lib.D3DError):
+            srv.submit([0, len(st)], [1, 2])
+        out, _ = srv.result(srv.submit(i1[:10], i2[:10]))
+        assert out["dist"].shape == (10,)
+    finally:
+        srv.close()

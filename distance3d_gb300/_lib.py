@@ -81,7 +81,7 @@ SIGNATURES = [
     ("d3d_server_submit", c_int, [c_void_p, c_void_p, c_void_p, c_int64, ctypes.POINTER(c_int64)]),
     ("d3d_server_wait", c_int, [c_void_p, c_int64, c_double]),
     ("d3d_server_result", c_int, [c_void_p, c_int64, ctypes.POINTER(PairResults), ctypes.POINTER(c_double)]),
-    ("d3d_server_replay", c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+    ("d3d_server_replay", c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                   ctypes.POINTER(c_double)]),
     ("d3d_bvh_bytes", c_size_t, [c_int64]),
     ("d3d_bvh_build", c_int, [c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),

@@ -23,8 +23,9 @@ constexpr int kBlock = 256;
 constexpr int64_t kF64Slots = 32768;      // FP64 EPA polytopes in flight (FP64 form)
 constexpr int64_t kFallbackSlots = 2048;  // FP64 EPA polytopes for the mixed form's fallback pairs
 
-// counters: EPA cursor, FP64 cursor, fallback count, EPA list length
-enum { kEpaCur = 0, kF64Cur, kNumFallback, kNumEpa, kCounters };
+// counters: EPA cursor, FP64 cursor, fallback count, EPA list length, FP64
+// warp cursor, second fallback count
+enum { kEpaCur = 0, kF64Cur, kNumFallback, kNumEpa, kW64Cur, kNumFallback2, kCounters };
 
 inline size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -67,7 +68,7 @@ __global__ void k_epa_select(int64_t cap, const int64_t* __restrict__ n_dev, con
 extern "C" size_t d3d_collide_scratch_bytes(int64_t capacity, const d3d_gjk_options* gjk,
                                             const d3d_epa_options* epa) {
     if (capacity <= 0 || !gjk || !epa || epa->max_faces < 4) return 0;
-    return 256 + 2 * up(sizeof(int32_t) * (size_t)capacity) + up(gjk_bytes(capacity, *gjk)) +
+    return 256 + 3 * up(sizeof(int32_t) * (size_t)capacity) + up(gjk_bytes(capacity, *gjk)) +
            (size_t)(f64_slots(capacity, *epa) * epa_f64_slot_bytes(*epa));
 }
 
@@ -103,6 +104,8 @@ extern "C" int d3d_collide(const d3d_store* store, const int32_t* i1, const int3
     p += up(sizeof(int32_t) * (size_t)capacity);
     int32_t* fallback = reinterpret_cast<int32_t*>(p);
     p += up(sizeof(int32_t) * (size_t)capacity);
+    int32_t* fallback2 = reinterpret_cast<int32_t*>(p);
+    p += up(sizeof(int32_t) * (size_t)capacity);
     void* gjk_scratch = p;
     p += up(gjk_bytes(capacity, *gjk));
     void* slots = p;
@@ -126,9 +129,15 @@ extern "C" int d3d_collide(const d3d_store* store, const int32_t* i1, const int3
     if (warp_form(*epa)) {
         rc = d3d::epa_warp_launch(*store, i1, i2, list, capacity, ctr + kNumEpa, ctr + kEpaCur, simplex, *epa, mtv,
                                   epa_status, n_faces, nullptr, fallback, ctr + kNumFallback, st);
+        const bool w64 = d3d::epa_warp_supported(*epa, true);
+        if (!rc && w64)
+            rc = d3d::epa_warp_launch(*store, i1, i2, fallback, capacity, ctr + kNumFallback, ctr + kW64Cur, simplex,
+                                      *epa, mtv, epa_status, n_faces, nullptr, fallback2, ctr + kNumFallback2, st,
+                                      true);
         if (!rc)
-            rc = d3d::epa_f64_launch(*store, i1, i2, fallback, capacity, ctr + kNumFallback, ctr + kF64Cur, simplex,
-                                     *epa, mtv, epa_status, n_faces, nullptr, slots, nslots, st);
+            rc = d3d::epa_f64_launch(*store, i1, i2, w64 ? fallback2 : fallback, capacity,
+                                     ctr + (w64 ? kNumFallback2 : kNumFallback), ctr + kF64Cur, simplex, *epa, mtv,
+                                     epa_status, n_faces, nullptr, slots, nslots, st);
     } else {
         rc = d3d::epa_f64_launch(*store, i1, i2, list, capacity, ctr + kNumEpa, ctr + kF64Cur, simplex, *epa, mtv,
                                  epa_status, n_faces, nullptr, slots, nslots, st);

@@ -295,21 +295,27 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     const bool sched = n >= kScheduleMin && !warp;
     const size_t up_n = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
     const size_t order_bytes = sched ? up_n : 0;
-    const size_t fb_bytes = mixed ? up_n : 0;
+    const size_t fb_bytes = mixed ? 2 * up_n : 0;  // fallback lists of the FP32 and FP64 warp searches
     const size_t temp_bytes = sched ? d3d::pair_order_temp_bytes(n) : 0;
     void* block = nullptr;
     rc = d3d::scratch_alloc(&block, 256 + order_bytes + fb_bytes + temp_bytes, st);
     if (rc) return rc;
     char* p = static_cast<char*>(block);
-    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(p);  // cursor, fallback cursor, fallback count
+    // counters: cursor, FP64 EPA cursor, fallback count, FP64 warp cursor, second fallback count
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(p);
     int32_t* order = sched ? reinterpret_cast<int32_t*>(p + 256) : nullptr;
     int32_t* fallback = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes) : nullptr;
-    cudaMemsetAsync(ctr, 0, 3 * sizeof(unsigned long long), st);
+    int32_t* fallback2 = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes + up_n) : nullptr;
+    const bool warp64 = warp && d3d::epa_warp_supported(*options, true);
+    cudaMemsetAsync(ctr, 0, 5 * sizeof(unsigned long long), st);
     if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, p + 256 + order_bytes + fb_bytes, temp_bytes, st);
-    if (!rc && warp)
+    if (!rc && warp) {
         rc = d3d::epa_warp_launch(*store, i1, i2, nullptr, n, nullptr, ctr, simplex, *options, mtv, status, n_faces,
                                   faces, fallback, ctr + 2, st);
-    else if (!rc && mixed)
+        if (!rc && warp64)
+            rc = d3d::epa_warp_launch(*store, i1, i2, fallback, n, ctr + 2, ctr + 3, simplex, *options, mtv, status,
+                                      n_faces, faces, fallback2, ctr + 4, st, true);
+    } else if (!rc && mixed)
         rc = d3d::epa_mixed_launch(*store, i1, i2, order, n, ctr, simplex, *options, mtv, status, n_faces, faces,
                                    scratch, slots_for(n), fallback, ctr + 2, st);
     if (!rc) {
@@ -317,9 +323,11 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
         int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
         const int64_t max_blocks = slots_for(n) / kBlock;  // the scratch holds this many slots
         if (blocks > max_blocks) blocks = (int)max_blocks;
-        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, mixed ? fallback : order, n, mixed ? ctr + 2 : nullptr,
-                                         mixed ? ctr + 1 : ctr, simplex, *options, mtv, status, n_faces, faces,
-                                         static_cast<double*>(scratch), slot_doubles(*options));
+        const int32_t* list = warp64 ? fallback2 : (mixed ? fallback : order);
+        const unsigned long long* count = warp64 ? ctr + 4 : (mixed ? ctr + 2 : nullptr);
+        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, list, n, count, mixed ? ctr + 1 : ctr, simplex, *options,
+                                         mtv, status, n_faces, faces, static_cast<double*>(scratch),
+                                         slot_doubles(*options));
         rc = d3d::check_launch("d3d_epa");
     }
     d3d::scratch_free(block, st);

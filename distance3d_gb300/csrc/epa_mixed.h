@@ -23,15 +23,17 @@ int epa_mixed_launch(const d3d_store& store, const int32_t* i1, const int32_t* i
                      int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream);
 
 // The warp-per-pair form (epa_warp.cu): one warp per pair, its polytope in
-// shared memory; supported when max_iterations <= 250, max_loose_edges <= 255
-// and four polytopes fit in a block's shared memory.  Runs pairs list[k] (or
-// k) for k < n, or k < *n_dev if n_dev is given (n then only sizes the
-// launch); fallback pairs as above.
-bool epa_warp_supported(const d3d_epa_options& o);
+// shared memory, FP32 (fp64 = false) or FP64 with the reference's supports
+// (fp64 = true, for the FP32 form's fallback pairs); supported when
+// max_iterations <= 250, max_loose_edges <= 255 and four polytopes fit in a
+// block's shared memory.  Runs pairs list[k] (or k) for k < n, or
+// k < *n_dev if n_dev is given (n then only sizes the launch); fallback pairs
+// as above.
+bool epa_warp_supported(const d3d_epa_options& o, bool fp64 = false);
 int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                     const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                     const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream);
+                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64 = false);
 
 // The FP64 EPA (epa.cu) over list[k] (or k) for k < n or < *n_dev, on
 // `slots` polytope slots of slot_bytes(o) in `scratch`.

@@ -26,8 +26,14 @@
 // the faces across their three edges; winding is outward by construction, as
 // in epa_mixed.cu.  A pair whose polytope fails validation (degenerate face,
 // horizon not one loop, more horizon edges than max_loose_edges) goes to the
-// FP64 EPA's fallback list.  The converged face is refined along its FP32
-// normal with FP64 supports (refine_face).  Compiled with -fmad=true.
+// fallback list.  The converged face is refined along its FP32 normal with
+// FP64 supports (refine_face).
+//
+// The same search is instantiated with an FP64 polytope and exact FP64
+// supports.  It takes the FP32 search's fallback pairs: the plane tests
+// behind a pinched horizon are FP32 noise on nearly coplanar faces, which
+// FP64 resolves.  Its own fallback pairs go to the serial FP64 EPA (the
+// reference's arithmetic).  Compiled with -fmad=true.
 #include "capi_util.h"
 #include "epa_mixed.cuh"
 #include "epa_mixed.h"
@@ -41,21 +47,41 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kWarps = 4;                // warps (pairs) per block
 constexpr unsigned kDead = 0xffffffffu;  // vertex word of a free face slot
 
+// xyz + w of the polytope's precision (16-byte aligned)
+template <typename T>
+struct alignas(16) Q4 {
+    T x, y, z, w;
+};
+
+template <typename T>
+__device__ __forceinline__ Q4<T> q4(T x, T y, T z, T w) {
+    return Q4<T>{x, y, z, w};
+}
+
+template <typename T>
+__device__ __forceinline__ T eps_of();
+template <>
+__device__ __forceinline__ float eps_of<float>() { return FLT_EPSILON; }
+template <>
+__device__ __forceinline__ double eps_of<double>() { return DBL_EPSILON; }
+
 // Byte offsets of one warp's polytope in shared memory.
 struct Layout {
     int vy, vd, fn, fv, adj, hz, freel, vis, se, ee, bytes;
 };
 
+template <typename T>
 __host__ __device__ inline Layout layout_for(const d3d_epa_options& o) {
     const int nv = o.max_iterations + 4, F = o.max_faces, E = o.max_loose_edges > 0 ? o.max_loose_edges : 1;
+    const int q = (int)sizeof(Q4<T>);
     Layout L;
     int p = 0;
     L.vy = p;
-    p += 16 * nv;
+    p += q * nv;
     L.vd = p;
-    p += 16 * nv;
+    p += q * nv;
     L.fn = p;
-    p += 16 * F;
+    p += q * F;
     L.adj = p;
     p += 8 * F;
     L.hz = p;
@@ -74,10 +100,11 @@ __host__ __device__ inline Layout layout_for(const d3d_epa_options& o) {
     return L;
 }
 
+template <typename T>
 struct Poly {
-    float4* vy;            // vertex y.xyz
-    float4* vd;            // search direction .xyz; w: input simplex row (0..3), -1 for found vertices
-    float4* fn;            // unit normal .xyz, w = offset n . y_a
+    Q4<T>* vy;             // vertex y.xyz
+    Q4<T>* vd;             // search direction .xyz; w: input simplex row (0..3), -1 for found vertices
+    Q4<T>* fn;             // unit normal .xyz, w = offset n . y_a
     ushort4* adj;          // faces across edges (a,b), (b,c), (c,a)
     int2* hz;              // horizon edge e: x = a | b << 8 | k << 16 (edge k of g faces it), y = g
     unsigned* fv;          // a | b << 8 | c << 16, kDead for a free slot
@@ -87,11 +114,12 @@ struct Poly {
     unsigned char* ee;     // horizon edge that ends at vertex v
 };
 
-__device__ __forceinline__ Poly poly_at(unsigned char* base, const Layout& L) {
-    Poly P;
-    P.vy = reinterpret_cast<float4*>(base + L.vy);
-    P.vd = reinterpret_cast<float4*>(base + L.vd);
-    P.fn = reinterpret_cast<float4*>(base + L.fn);
+template <typename T>
+__device__ __forceinline__ Poly<T> poly_at(unsigned char* base, const Layout& L) {
+    Poly<T> P;
+    P.vy = reinterpret_cast<Q4<T>*>(base + L.vy);
+    P.vd = reinterpret_cast<Q4<T>*>(base + L.vd);
+    P.fn = reinterpret_cast<Q4<T>*>(base + L.fn);
     P.adj = reinterpret_cast<ushort4*>(base + L.adj);
     P.hz = reinterpret_cast<int2*>(base + L.hz);
     P.fv = reinterpret_cast<unsigned*>(base + L.fv);
@@ -104,8 +132,9 @@ __device__ __forceinline__ Poly poly_at(unsigned char* base, const Layout& L) {
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
-__device__ __forceinline__ f3 yv(const Poly& P, int v) {
-    const float4 a = P.vy[v];
+template <typename T>
+__device__ __forceinline__ V3<T> yv(const Poly<T>& P, int v) {
+    const Q4<T> a = P.vy[v];
     return mk(a.x, a.y, a.z);
 }
 
@@ -158,6 +187,33 @@ __device__ __forceinline__ f3 minkowski32(const d3d_store& st, int a, int b, f3 
     return up ? o - s : s - o;
 }
 
+// w in FP64 with the reference's supports (the polytope argmax in FP64), for
+// the FP64 polytope.
+__device__ __forceinline__ d3 minkowski64_exact(const d3d_store& st, int a, int b, d3 d) {
+    const bool up = lane_id() & 16;
+    Col<double> c;
+    load_col(st, up ? b : a, c);
+    const d3 dd = up ? -d : d;
+    d3 s;
+    if (c.type == D3D_BOX || c.type == D3D_HULL) {
+        if (c.nv < 1)
+            s = mk(double(NAN), double(NAN), double(NAN));
+        else
+            s = load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts64, c.off, c.nv, dd, half_mask())));
+    } else {
+        s = support(c, st.verts64, dd);
+    }
+    const d3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
+    return up ? o - s : s - o;
+}
+
+// The polytope's precision: FP32 search on the FP32 mirror, or FP64 with the
+// reference's supports.
+__device__ __forceinline__ f3 minkowski_of(const d3d_store& st, int a, int b, f3 d);
+__device__ __forceinline__ d3 minkowski_of(const d3d_store& st, int a, int b, d3 d) {
+    return minkowski64_exact(st, a, b, d);
+}
+
 // The same in FP64 with RefineSupport (polytope vertex chosen by the FP32
 // argmax of the rounded direction).
 __device__ __forceinline__ d3 minkowski64(const d3d_store& st, int a, int b, d3 d) {
@@ -191,14 +247,17 @@ __device__ __forceinline__ int warp_excl(int x) {
     return s - x;
 }
 
+__device__ __forceinline__ f3 minkowski_of(const d3d_store& st, int a, int b, f3 d) { return minkowski32(st, a, b, d); }
+
 // unit normal and offset of face (a, b, c); false if degenerate
-__device__ __forceinline__ bool plane_of(const Poly& P, int a, int b, int c, float4& out) {
-    const f3 ya = yv(P, a), yb = yv(P, b), yc = yv(P, c);
-    f3 n = cross(yb - ya, yc - ya);
-    const float l = sqrtf(dot(n, n));
-    if (!(l > 0.f)) return false;
-    n = n * (1.f / l);
-    out = make_float4(n.x, n.y, n.z, dot(ya, n));
+template <typename T>
+__device__ __forceinline__ bool plane_of(const Poly<T>& P, int a, int b, int c, Q4<T>& out) {
+    const V3<T> ya = yv(P, a), yb = yv(P, b), yc = yv(P, c);
+    V3<T> n = cross(yb - ya, yc - ya);
+    const T l = sqrt_t(dot(n, n));
+    if (!(l > T(0))) return false;
+    n = n * (T(1) / l);
+    out = q4(n.x, n.y, n.z, dot(ya, n));
     return true;
 }
 
@@ -207,12 +266,13 @@ __device__ __forceinline__ int vid(unsigned w, int j) { return (int)((w >> (8 * 
 __device__ __forceinline__ int adj_at(ushort4 g, int j) { return j == 0 ? g.x : (j == 1 ? g.y : g.z); }
 
 // Closest live face: (offset, slot), ties to the lower slot.
-__device__ __forceinline__ int closest_face(const Poly& P, int nslots) {
-    float bd = 0.f;
+template <typename T>
+__device__ __forceinline__ int closest_face(const Poly<T>& P, int nslots) {
+    T bd = T(0);
     int bs = -1;
     for (int f = lane_id(); f < nslots; f += 32) {
         if (P.fv[f] == kDead) continue;
-        const float d = P.fn[f].w;
+        const T d = P.fn[f].w;
         if (bs < 0 || d < bd) {
             bd = d;
             bs = f;
@@ -220,7 +280,7 @@ __device__ __forceinline__ int closest_face(const Poly& P, int nslots) {
     }
 #pragma unroll
     for (int m = 16; m; m >>= 1) {
-        const float od = __shfl_xor_sync(kFull, bd, m);
+        const T od = __shfl_xor_sync(kFull, bd, m);
         const int os = __shfl_xor_sync(kFull, bs, m);
         if (os >= 0 && (bs < 0 || od < bd || (od == bd && os < bs))) {
             bd = od;
@@ -238,21 +298,23 @@ struct Search {
     int live;
 };
 
-// The FP32 expanding-polytope search for one pair (uniform across the warp).
-__device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, const double* simplex,
+// The expanding-polytope search for one pair in the polytope's precision T
+// (uniform across the warp).
+template <typename T>
+__device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int b, const double* simplex,
                               const d3d_epa_options& o) {
     const int ln = lane_id();
     Search R{kEpaFallback, 0, 0, 0};
-    // starting tetrahedron: the FP64 simplex rounded to FP32
-    float scale = 0.f;
+    // starting tetrahedron: the FP64 simplex (rounded to T)
+    T scale = T(0);
     if (ln < 4) {
-        const f3 y = mk((float)simplex[3 * ln], (float)simplex[3 * ln + 1], (float)simplex[3 * ln + 2]);
-        P.vy[ln] = make_float4(y.x, y.y, y.z, 0.f);
-        P.vd[ln] = make_float4(0.f, 0.f, 0.f, (float)ln);
-        scale = sqrtf(dot(y, y));
+        const V3<T> y = mk((T)simplex[3 * ln], (T)simplex[3 * ln + 1], (T)simplex[3 * ln + 2]);
+        P.vy[ln] = q4(y.x, y.y, y.z, T(0));
+        P.vd[ln] = q4(T(0), T(0), T(0), (T)ln);
+        scale = sqrt_t(dot(y, y));
     }
 #pragma unroll
-    for (int m = 16; m; m >>= 1) scale = fmaxf(scale, __shfl_xor_sync(kFull, scale, m));
+    for (int m = 16; m; m >>= 1) scale = maxf2(scale, (T)__shfl_xor_sync(kFull, scale, m));
     __syncwarp();
     // faces ABC, ACD, ADB, BDC, each wound away from the vertex it leaves out
     bool bad = false;
@@ -260,16 +322,16 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
         const int t = ln == 0 ? 0x3210 : (ln == 1 ? 0x1320 : (ln == 2 ? 0x2130 : 0x0231));
         int fa = t & 15, fb = (t >> 4) & 15;
         const int fc = (t >> 8) & 15, fd = (t >> 12) & 15;
-        float4 pl;
+        Q4<T> pl;
         if (!plane_of(P, fa, fb, fc, pl)) {
             bad = true;
         } else {
-            const f3 yd = yv(P, fd) - yv(P, fa);
-            if (pl.x * yd.x + pl.y * yd.y + pl.z * yd.z > 0.f) {
+            const V3<T> yd = yv(P, fd) - yv(P, fa);
+            if (pl.x * yd.x + pl.y * yd.y + pl.z * yd.z > T(0)) {
                 const int s = fa;
                 fa = fb;
                 fb = s;
-                pl = make_float4(-pl.x, -pl.y, -pl.z, -pl.w);
+                pl = q4(-pl.x, -pl.y, -pl.z, -pl.w);
             }
             P.fv[ln] = pack3(fa, fb, fc);
             P.fn[ln] = pl;
@@ -300,7 +362,7 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
     if (__any_sync(kFull, bad)) return R;
     __syncwarp();
 
-    const float vis_eps = (float)o.epsilon;  // the reference's visibility test
+    const T vis_eps = (T)o.epsilon;  // the reference's visibility test
     int nslots = 4, nfree = 0, live = 4, nv = 4, it = 0;
     while (true) {
         const int cf = closest_face(P, nslots);
@@ -316,11 +378,11 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
             return R;
         }
         ++it;
-        const float4 cn = P.fn[cf];
-        const f3 sd = mk(cn.x, cn.y, cn.z);
-        const f3 w = minkowski32(st, a, b, sd);
-        scale = fmaxf(scale, sqrtf(dot(w, w)));
-        const float eps = fmaxf((float)o.epsilon, 8.f * FLT_EPSILON * scale);
+        const Q4<T> cn = P.fn[cf];
+        const V3<T> sd = mk(cn.x, cn.y, cn.z);
+        const V3<T> w = minkowski_of(st, a, b, sd);
+        scale = maxf2(scale, sqrt_t(dot(w, w)));
+        const T eps = maxf2((T)o.epsilon, T(8) * eps_of<T>() * scale);
         if (dot(w, sd) - cn.w < eps) {
             R.status = D3D_STATUS_OK;
             return R;
@@ -336,8 +398,8 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
         // go, on the free list above its current top.
         unsigned short* const vl = P.freel + nfree;
         if (ln == 0) {
-            P.vy[vn] = make_float4(w.x, w.y, w.z, 0.f);
-            P.vd[vn] = make_float4(sd.x, sd.y, sd.z, -1.f);
+            P.vy[vn] = q4(w.x, w.y, w.z, T(0));
+            P.vd[vn] = q4(sd.x, sd.y, sd.z, T(-1));
             P.vis[cf] = stamp;
             vl[0] = (unsigned short)cf;
         }
@@ -353,7 +415,7 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
                 if (i < nc) {
                     g = adj_at(P.adj[vl[head + i / 3]], i % 3);
                     if (P.vis[g] != stamp) {
-                        const float4 pl = P.fn[g];
+                        const Q4<T> pl = P.fn[g];
                         if (dot(mk(pl.x, pl.y, pl.z), w - yv(P, vid(P.fv[g], 0))) > vis_eps)
                             take = atomicExch(&P.vis[g], stamp) != stamp;
                     }
@@ -439,7 +501,7 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
             const int s = e < nft ? P.freel[nft - 1 - e] : nslots + (e - nft);
             const int sn = nx < nft ? P.freel[nft - 1 - nx] : nslots + (nx - nft);
             const int sp = pv < nft ? P.freel[nft - 1 - pv] : nslots + (pv - nft);
-            float4 pl;
+            Q4<T> pl;
             if (!plane_of(P, ea, eb2, vn, pl)) bad = true;
             P.fn[s] = pl;
             P.fv[s] = pack3(ea, eb2, vn);
@@ -461,14 +523,23 @@ __device__ Search search_pair(const Poly& P, const d3d_store& st, int a, int b, 
 // depth h(n), an upper bound on the penetration depth for every n, and the
 // FP32 normal of the converged face is within the search's tolerance of the
 // optimal direction.
-__device__ __forceinline__ d3 refine_face(const Poly& P, const d3d_store& st, int a, int b, int f) {
-    const float4 fn = P.fn[f];
+__device__ __forceinline__ d3 refine_face(const Poly<float>& P, const d3d_store& st, int a, int b, int f) {
+    const Q4<float> fn = P.fn[f];
     d3 n = mk((double)fn.x, (double)fn.y, (double)fn.z);
     n = n * (1.0 / sqrt(dot(n, n)));
     const d3 w = minkowski64(st, a, b, n);
     return n * dot(w, n);
 }
 
+// The FP64 polytope's face: its own unit normal and the reference's supports.
+__device__ __forceinline__ d3 refine_face(const Poly<double>& P, const d3d_store& st, int a, int b, int f) {
+    const Q4<double> fn = P.fn[f];
+    const d3 n = mk(fn.x, fn.y, fn.z);
+    const d3 w = minkowski64_exact(st, a, b, n);
+    return n * dot(w, n);
+}
+
+template <typename T>
 __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
                                                           const int32_t* __restrict__ i2,
                                                           const int32_t* __restrict__ list, int64_t n,
@@ -480,8 +551,8 @@ __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const
                                                           int32_t* __restrict__ fallback,
                                                           unsigned long long* __restrict__ n_fallback) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const Layout L = layout_for(o);
-    const Poly P = poly_at(smem + (threadIdx.x >> 5) * L.bytes, L);
+    const Layout L = layout_for<T>(o);
+    const Poly<T> P = poly_at<T>(smem + (threadIdx.x >> 5) * L.bytes, L);
     const int ln = lane_id();
     if (n_dev) n = (int64_t)*n_dev;
     while (true) {
@@ -521,12 +592,12 @@ __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const
                     const unsigned fw = P.fv[f];
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
-                        const float4 yy = P.vy[vid(fw, j)];
+                        const Q4<T> yy = P.vy[vid(fw, j)];
                         q[3 * j] = yy.x;
                         q[3 * j + 1] = yy.y;
                         q[3 * j + 2] = yy.z;
                     }
-                    const float4 pl = P.fn[f];
+                    const Q4<T> pl = P.fn[f];
                     q[9] = pl.x;
                     q[10] = pl.y;
                     q[11] = pl.z;
@@ -542,19 +613,21 @@ __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const
 
 namespace d3d {
 
-bool epa_warp_supported(const d3d_epa_options& o) {
+bool epa_warp_supported(const d3d_epa_options& o, bool fp64) {
     if (o.max_iterations > 250 || o.max_loose_edges > 255 || o.max_faces > 65535) return false;
-    return (int64_t)layout_for(o).bytes * kWarps <= 227 * 1024;
+    const int bytes = fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes;
+    return (int64_t)bytes * kWarps <= 227 * 1024;
 }
 
 int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                     const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                     const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
-    const int smem = layout_for(o).bytes * kWarps;
-    cudaError_t e = cudaFuncSetAttribute(k_epa_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64) {
+    const void* fn = fp64 ? (const void*)k_epa_warp<double> : (const void*)k_epa_warp<float>;
+    const int smem = (fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes) * kWarps;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_epa_warp, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) {
         set_error("d3d_epa (mixed): %s", cudaGetErrorString(e));
@@ -563,12 +636,18 @@ int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_epa_warp, 32 * kWarps, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kWarps, smem);
     int64_t blocks = (int64_t)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
     const int64_t need = (n + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
-    k_epa_warp<<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv,
-                                                           status, n_faces, faces, fallback, n_fallback);
+    if (fp64)
+        k_epa_warp<double><<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex,
+                                                                       o, mtv, status, n_faces, faces, fallback,
+                                                                       n_fallback);
+    else
+        k_epa_warp<float><<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex,
+                                                                      o, mtv, status, n_faces, faces, fallback,
+                                                                      n_fallback);
     return check_launch("d3d_epa (mixed)");
 }
 

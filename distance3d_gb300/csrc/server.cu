@@ -47,9 +47,11 @@ constexpr size_t kPairBytes = 8 + 187 + 120;  // pair ids, outputs, scratch (app
 struct Request {
     int64_t id;
     std::vector<int32_t> i1, i2;
-    std::vector<unsigned char> out[kOutputs];
-    Clock::time_point arrival, finish;
+    std::vector<unsigned char> out[kOutputs];  // empty if the results are not kept
+    Clock::time_point arrival, launched, finish;
     int pieces_out = 0;
+    bool keep = true;
+    bool started = false;
     bool done = false;
 };
 
@@ -184,6 +186,7 @@ int init_slot(d3d_server* s, Slot& sl) {
 void collect(d3d_server* s, Slot& sl, Clock::time_point now) {
     for (const Piece& p : sl.pieces) {
         Request& r = *p.req;
+        if (!r.keep) continue;
         const int64_t len = p.hi - p.lo;
         for (int k = 0; k < kOutputs; ++k)
             std::memcpy(r.out[k].data() + p.lo * kOutBytes[k],
@@ -225,6 +228,12 @@ bool launch(d3d_server* s, Slot& sl) {
         }
         if (n == 0) return false;
         s->inflight_pairs += n;
+        const Clock::time_point now = Clock::now();
+        for (const Piece& p : sl.pieces)
+            if (!p.req->started) {
+                p.req->started = true;
+                p.req->launched = now;
+            }
     }
     for (const Piece& p : sl.pieces) {
         std::memcpy(sl.h_i1 + p.off, p.req->i1.data() + p.lo, sizeof(int32_t) * (p.hi - p.lo));
@@ -354,12 +363,16 @@ extern "C" void d3d_server_destroy(d3d_server* s) {
     delete s;
 }
 
-extern "C" int d3d_server_submit(d3d_server* s, const int32_t* i1, const int32_t* i2, int64_t n, int64_t* id) {
+namespace {
+
+int submit(d3d_server* s, const int32_t* i1, const int32_t* i2, int64_t n, int64_t* id, bool keep) {
     D3D_REQUIRE(s && id && n >= 0 && (n == 0 || (i1 && i2)), "d3d_server_submit: invalid argument");
     auto r = std::make_shared<Request>();
+    r->keep = keep;
     r->i1.assign(i1, i1 + n);
     r->i2.assign(i2, i2 + n);
-    for (int k = 0; k < kOutputs; ++k) r->out[k].resize(kOutBytes[k] * n);
+    if (keep)
+        for (int k = 0; k < kOutputs; ++k) r->out[k].resize(kOutBytes[k] * n);
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->error) return server_error(s);
     for (int64_t k = 0; k < n; ++k)
@@ -380,6 +393,12 @@ extern "C" int d3d_server_submit(d3d_server* s, const int32_t* i1, const int32_t
     *id = r->id;
     s->cv_work.notify_one();
     return D3D_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int d3d_server_submit(d3d_server* s, const int32_t* i1, const int32_t* i2, int64_t n, int64_t* id) {
+    return submit(s, i1, i2, n, id, true);
 }
 
 extern "C" int d3d_server_wait(d3d_server* s, int64_t id, double timeout_s) {
@@ -420,7 +439,7 @@ extern "C" int d3d_server_result(d3d_server* s, int64_t id, const d3d_pair_resul
         s->requests.erase(it);
     }
     if (latency_s) *latency_s = std::chrono::duration<double>(r->finish - r->arrival).count();
-    if (out) {
+    if (out && r->keep) {
         void* dst[kOutputs] = {out->dist, out->cp1, out->cp2, out->simplex, out->n_simplex,
                                out->status, out->iterations, out->mtv, out->epa_status, out->n_faces};
         for (int k = 0; k < kOutputs; ++k)
@@ -430,7 +449,8 @@ extern "C" int d3d_server_result(d3d_server* s, int64_t id, const d3d_pair_resul
 }
 
 extern "C" int d3d_server_replay(d3d_server* s, int64_t n_requests, const double* offsets_s, const int64_t* sizes,
-                                 const int32_t* i1, const int32_t* i2, double* latency_s, double* span_s) {
+                                 const int32_t* i1, const int32_t* i2, double* latency_s, double* wait_s,
+                                 double* span_s) {
     D3D_REQUIRE(s && n_requests >= 0 && (n_requests == 0 || (offsets_s && sizes && i1 && i2 && latency_s)),
                 "d3d_server_replay: invalid argument");
     std::vector<int64_t> ids(n_requests);
@@ -440,7 +460,7 @@ extern "C" int d3d_server_replay(d3d_server* s, int64_t n_requests, const double
         const auto at = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(offsets_s[k]));
         while (Clock::now() < at) {
         }
-        int rc = d3d_server_submit(s, i1 + base, i2 + base, sizes[k], &ids[k]);
+        int rc = submit(s, i1 + base, i2 + base, sizes[k], &ids[k], false);
         if (rc) return rc;
         {
             // latency counts from the scheduled arrival, so a late submission is not hidden
@@ -456,7 +476,9 @@ extern "C" int d3d_server_replay(d3d_server* s, int64_t n_requests, const double
         if (rc) return rc;
         {
             std::lock_guard<std::mutex> lock(s->mu);
-            if (s->requests[ids[k]]->finish > last) last = s->requests[ids[k]]->finish;
+            const Request& r = *s->requests[ids[k]];
+            if (r.finish > last) last = r.finish;
+            if (wait_s) wait_s[k] = std::chrono::duration<double>((r.started ? r.launched : r.finish) - r.arrival).count();
         }
         rc = d3d_server_result(s, ids[k], nullptr, &latency_s[k]);
         if (rc) return rc;

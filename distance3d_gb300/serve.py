@@ -346,7 +346,10 @@ class NativeCollisionServer:
         if a.size != sizes.sum() or b.size != a.size or offs.size != sizes.size:
             raise ValueError("sizes, offsets and pair arrays disagree")
         lat = np.empty(len(sizes))
+        wait = np.empty(len(sizes))
         span = ctypes.c_double()
         _lib.check(self._lib.d3d_server_replay(self._h, len(sizes), offs.ctypes.data, sizes.ctypes.data,
-                                               a.ctypes.data, b.ctypes.data, lat.ctypes.data, ctypes.byref(span)))
+                                               a.ctypes.data, b.ctypes.data, lat.ctypes.data, wait.ctypes.data,
+                                               ctypes.byref(span)))
+        self.last_wait = wait
         return lat, span.value

@@ -224,10 +224,11 @@ int d3d_server_wait(d3d_server* server, int64_t request_id, double timeout_s);
 int d3d_server_result(d3d_server* server, int64_t request_id, const d3d_pair_results* out, double* latency_s);
 /* Submit n_requests requests at offsets_s[k] seconds from the call (sizes[k]
  * pairs each, concatenated in i1/i2), wait for all, return each one's
- * latency (from its scheduled arrival) and the span from the call to the
- * last finish; results are discarded. */
+ * latency and its wait until its first batch launched (both from its
+ * scheduled arrival; wait_s may be NULL) and the span from the call to the
+ * last finish; the results are not kept. */
 int d3d_server_replay(d3d_server* server, int64_t n_requests, const double* offsets_s, const int64_t* sizes,
-                      const int32_t* i1, const int32_t* i2, double* latency_s, double* span_s);
+                      const int32_t* i1, const int32_t* i2, double* latency_s, double* wait_s, double* span_s);
 
 /* ------------------------------------------------------------------ broad phase
  * A linear BVH over FP64 boxes aabbs[n][3][2] ([axis][min,max]).  The tree

@@ -45,6 +45,11 @@ class PairResults(ctypes.Structure):
                                                "iterations", "mtv", "epa_status", "n_faces")]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("gjk_block", ctypes.c_int32), ("gjk_warps_per_sm", ctypes.c_int32), ("epa_warps", ctypes.c_int32),
+                ("sort_min", ctypes.c_int32)]
+
+
 class D3DError(RuntimeError):
     """A libd3d_gb300 entry point returned an error code."""
 
@@ -75,6 +80,10 @@ SIGNATURES = [
     ("d3d_collide_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions)]),
     ("d3d_collide", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(GjkOptions),
                             ctypes.POINTER(EpaOptions)] + [c_void_p] * 11 + [c_size_t, c_void_p]),
+    ("d3d_get_tuning", c_int, [ctypes.POINTER(Tuning)]),
+    ("d3d_set_tuning", c_int, [ctypes.POINTER(Tuning)]),
+    ("d3d_autotune", c_int, [_SP, c_void_p, c_void_p, c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions),
+                             ctypes.POINTER(Tuning), c_void_p]),
     ("d3d_server_create", c_int, [_SP, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions),
                                   ctypes.POINTER(ServerOptions), ctypes.POINTER(c_void_p)]),
     ("d3d_server_destroy", None, [c_void_p]),

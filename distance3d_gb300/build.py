@@ -40,6 +40,7 @@ UNITS = [
     ("schedule.cu", []),
     ("collide.cu", []),
     ("server.cu", []),
+    ("tune.cu", []),
     ("bvh.cu", []),
 ]
 

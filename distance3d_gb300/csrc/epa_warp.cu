@@ -44,7 +44,6 @@ namespace {
 using namespace d3d;
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kWarps = 4;                // warps (pairs) per block
 constexpr unsigned kDead = 0xffffffffu;  // vertex word of a free face slot
 
 // xyz + w of the polytope's precision (16-byte aligned)
@@ -539,8 +538,8 @@ __device__ __forceinline__ d3 refine_face(const Poly<double>& P, const d3d_store
     return n * dot(w, n);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
+template <typename T, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS, 16 / WARPS) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
                                                           const int32_t* __restrict__ i2,
                                                           const int32_t* __restrict__ list, int64_t n,
                                                           const unsigned long long* __restrict__ n_dev,
@@ -611,20 +610,15 @@ __global__ void __launch_bounds__(32 * kWarps, 4) k_epa_warp(d3d_store st, const
 
 }  // namespace
 
-namespace d3d {
+namespace {
 
-bool epa_warp_supported(const d3d_epa_options& o, bool fp64) {
-    if (o.max_iterations > 250 || o.max_loose_edges > 255 || o.max_faces > 65535) return false;
-    const int bytes = fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes;
-    return (int64_t)bytes * kWarps <= 227 * 1024;
-}
-
-int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
-                    const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
-                    const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64) {
-    const void* fn = fp64 ? (const void*)k_epa_warp<double> : (const void*)k_epa_warp<float>;
-    const int smem = (fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes) * kWarps;
+template <typename T, int WARPS>
+int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
+    const void* fn = (const void*)k_epa_warp<T, WARPS>;
+    const int smem = layout_for<T>(o).bytes * WARPS;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -633,22 +627,44 @@ int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2
         set_error("d3d_epa (mixed): %s", cudaGetErrorString(e));
         return D3D_ERR_CUDA;
     }
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * kWarps, smem);
-    int64_t blocks = (int64_t)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
-    const int64_t need = (n + kWarps - 1) / kWarps;
-    if (blocks > need) blocks = need;
-    if (fp64)
-        k_epa_warp<double><<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex,
-                                                                       o, mtv, status, n_faces, faces, fallback,
-                                                                       n_fallback);
-    else
-        k_epa_warp<float><<<(int)blocks, 32 * kWarps, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex,
-                                                                      o, mtv, status, n_faces, faces, fallback,
-                                                                      n_fallback);
+    const int blocks = persistent_blocks(fn, 32 * WARPS, n * 32, 0, smem);
+    k_epa_warp<T, WARPS><<<blocks, 32 * WARPS, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o,
+                                                               mtv, status, n_faces, faces, fallback, n_fallback);
     return check_launch("d3d_epa (mixed)");
+}
+
+}  // namespace
+
+namespace d3d {
+
+constexpr int64_t kSmemPerBlock = 227 * 1024;
+
+bool epa_warp_supported(const d3d_epa_options& o, bool fp64) {
+    if (o.max_iterations > 250 || o.max_loose_edges > 255 || o.max_faces > 65535) return false;
+    const int bytes = fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes;
+    return (int64_t)bytes * 2 <= kSmemPerBlock;
+}
+
+int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                    const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                    const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64) {
+    // pairs per block as tuned, fewer if their polytopes do not fit in one block
+    const int64_t bytes = fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes;
+    int w = tuning().epa_warps;
+    while (w > 2 && bytes * w > kSmemPerBlock) w /= 2;
+#define D3D_WARP_LAUNCH(T, W)                                                                                      \
+    return launch_warp<T, W>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces, fallback, \
+                             n_fallback, stream)
+    if (fp64) {
+        if (w == 2) D3D_WARP_LAUNCH(double, 2);
+        if (w == 8) D3D_WARP_LAUNCH(double, 8);
+        D3D_WARP_LAUNCH(double, 4);
+    }
+    if (w == 2) D3D_WARP_LAUNCH(float, 2);
+    if (w == 8) D3D_WARP_LAUNCH(float, 8);
+    D3D_WARP_LAUNCH(float, 4);
+#undef D3D_WARP_LAUNCH
 }
 
 }  // namespace d3d

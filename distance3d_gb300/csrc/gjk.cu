@@ -13,24 +13,23 @@ namespace {
 
 using namespace d3d;
 
-constexpr int kBlock = 128;
-constexpr int64_t kScheduleMin = 4096;  // below this, pairs run in input order
 
 // Persistent FP64 GJK distance: each lane runs the reference's loop for one
 // pair at a time (one iteration per round) and fetches the next pair, in the
 // type-sorted `order`, when its pair ends.  `n_dev` (if not null) holds the
 // pair count on the device (fallback lists of the mixed form).
-__global__ void __launch_bounds__(kBlock) k_gjk_distance_f64(d3d_store s, const int32_t* __restrict__ i1,
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_gjk_distance_f64(d3d_store s, const int32_t* __restrict__ i1,
                                                             const int32_t* __restrict__ i2,
                                                             const int32_t* __restrict__ order, int64_t n,
                                                             const unsigned long long* __restrict__ n_dev,
                                                             unsigned long long* __restrict__ cursor,
                                                             d3d_gjk_options opt, DistanceOut o) {
-    __shared__ double rows[24 * kBlock];  // the simplex P/Q rows of each lane
+    __shared__ double rows[24 * BLOCK];  // the simplex P/Q rows of each lane
     if (n_dev) n = (int64_t)*n_dev;
     const JoltEps<double> E = reference_eps<double>();
     const double tol_sq = opt.tolerance * opt.tolerance;
-    GjkLoop<double, SmemRows<double, kBlock>> g;
+    GjkLoop<double, SmemRows<double, BLOCK>> g;
     g.S.R.base = rows + threadIdx.x;
     int64_t pid = 0;
     int a = 0, b = 0;
@@ -100,16 +99,15 @@ extern "C" int d3d_gjk_distance(const d3d_store* store, const int32_t* i1, const
 namespace d3d {
 
 size_t gjk_f64_scratch_bytes(int64_t capacity) {
-    if (capacity < kScheduleMin) return 256;
     return 256 + ((sizeof(int32_t) * (size_t)capacity + 255) & ~size_t(255)) + pair_order_temp_bytes(capacity);
 }
 
 int gjk_f64_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n, const int64_t* n_dev,
                 const d3d_gjk_options& opt, const DistanceOut& o, void* scratch, cudaStream_t stream) {
-    const bool sched = n >= kScheduleMin;
+    const bool sched = n >= tuning().sort_min;
     unsigned long long* cursor = static_cast<unsigned long long*>(scratch);
     int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + 256) : nullptr;
-    const size_t order_bytes = sched ? ((sizeof(int32_t) * (size_t)n + 255) & ~size_t(255)) : 0;
+    const size_t order_bytes = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
     cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) {
         set_error("d3d_gjk_distance: %s", cudaGetErrorString(e));
@@ -128,8 +126,17 @@ int gjk_f64_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, in
 int launch_gjk_f64(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
                    const unsigned long long* n_dev, unsigned long long* cursor, const d3d_gjk_options& opt,
                    const DistanceOut& o, cudaStream_t stream) {
-    const int blocks = persistent_blocks((const void*)k_gjk_distance_f64, kBlock, n);
-    k_gjk_distance_f64<<<blocks, kBlock, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+    const d3d_tuning t = tuning();
+    if (t.gjk_block == 64) {
+        const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<64>, 64, n, blocks_per_sm(t, 64));
+        k_gjk_distance_f64<64><<<blocks, 64, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+    } else if (t.gjk_block == 256) {
+        const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<256>, 256, n, blocks_per_sm(t, 256));
+        k_gjk_distance_f64<256><<<blocks, 256, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+    } else {
+        const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<128>, 128, n, blocks_per_sm(t, 128));
+        k_gjk_distance_f64<128><<<blocks, 128, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+    }
     return check_launch("d3d_gjk_distance");
 }
 

@@ -38,10 +38,6 @@ namespace {
 
 using namespace d3d;
 
-constexpr int kBlock = 128;
-constexpr int64_t kScheduleMin = 4096;
-
-using Rows64 = SmemRows<double, kBlock>;
 
 // Per-call counters (one 256-byte block): cursors of A, B and C, then the
 // lengths of the refinement and fallback lists.
@@ -53,7 +49,8 @@ struct Lists {
     unsigned long long* ctr;
 };
 
-__global__ void __launch_bounds__(kBlock) k_gjk_mixed_a(d3d_store s, const int32_t* __restrict__ i1,
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_a(d3d_store s, const int32_t* __restrict__ i1,
                                                         const int32_t* __restrict__ i2,
                                                         const int32_t* __restrict__ order, int64_t n,
                                                         const int64_t* __restrict__ n_dev, float tol_sq,
@@ -86,14 +83,15 @@ __global__ void __launch_bounds__(kBlock) k_gjk_mixed_a(d3d_store s, const int32
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_gjk_mixed_b(d3d_store s, const int32_t* __restrict__ i1,
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_t* __restrict__ i1,
                                                         const int32_t* __restrict__ i2, d3d_gjk_options opt,
                                                         const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
-    __shared__ double rows[24 * kBlock];
+    __shared__ double rows[24 * BLOCK];
     const int64_t n = (int64_t)lists.ctr[kNumRefine];
     const JoltEps<double> E = reference_eps<double>();
     const double tol_sq = opt.tolerance * opt.tolerance;
-    PhaseB<Rows64> B;
+    PhaseB<SmemRows<double, BLOCK>> B;
     B.g.S.R.base = rows + threadIdx.x;
     int32_t pid = 0;
     int a = 0, b = 0;
@@ -131,16 +129,31 @@ inline size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 namespace d3d {
 
 size_t gjk_mixed_scratch_bytes(int64_t capacity) {
-    const bool sched = capacity >= kScheduleMin;
-    return 256 + (sched ? up(sizeof(int32_t) * (size_t)capacity) + pair_order_temp_bytes(capacity) : 0) +
+    return 256 + up(sizeof(int32_t) * (size_t)capacity) + pair_order_temp_bytes(capacity) +
            up(sizeof(Handoff) * (size_t)capacity) + 2 * up(sizeof(int32_t) * (size_t)capacity);
+}
+
+template <int BLOCK>
+int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
+                 const int64_t* n_dev, const d3d_gjk_options& opt, Handoff* hand, const DistanceOut& o,
+                 const Lists& lists, int per_sm, cudaStream_t stream) {
+    const float tol_sq = (float)(opt.tolerance * opt.tolerance);
+    k_gjk_mixed_a<BLOCK><<<persistent_blocks((const void*)k_gjk_mixed_a<BLOCK>, BLOCK, n, per_sm), BLOCK, 0,
+                           stream>>>(store, i1, i2, order, n, n_dev, tol_sq, (float)opt.max_distance_squared,
+                                     opt.max_iterations, hand, lists);
+    int rc = check_launch("d3d_gjk_distance (mixed, FP32 phase)");
+    if (rc) return rc;
+    k_gjk_mixed_b<BLOCK><<<persistent_blocks((const void*)k_gjk_mixed_b<BLOCK>, BLOCK, n, per_sm), BLOCK, 0,
+                           stream>>>(store, i1, i2, opt, hand, o, lists);
+    return check_launch("d3d_gjk_distance (mixed, FP64 phase)");
 }
 
 int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n, const int64_t* n_dev,
                   const d3d_gjk_options& opt, const DistanceOut& o, void* scratch, cudaStream_t stream) {
-    const bool sched = n >= kScheduleMin;
-    const size_t order_bytes = sched ? up(sizeof(int32_t) * (size_t)n) : 0;
-    const size_t temp_bytes = sched ? pair_order_temp_bytes(n) : 0;
+    const d3d_tuning t = tuning();
+    const bool sched = n >= t.sort_min;
+    const size_t order_bytes = up(sizeof(int32_t) * (size_t)n);
+    const size_t temp_bytes = pair_order_temp_bytes(n);
     const size_t list_bytes = up(sizeof(int32_t) * (size_t)n);
     char* p = static_cast<char*>(scratch);
     Lists lists;
@@ -161,16 +174,14 @@ int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, 
     }
     int rc = sched ? pair_order(store, i1, i2, n, order, temp, temp_bytes, stream, n_dev) : D3D_SUCCESS;
     if (!rc) {
-        const float tol_sq = (float)(opt.tolerance * opt.tolerance);
-        k_gjk_mixed_a<<<persistent_blocks((const void*)k_gjk_mixed_a, kBlock, n), kBlock, 0, stream>>>(
-            store, i1, i2, order, n, n_dev, tol_sq, (float)opt.max_distance_squared, opt.max_iterations, hand,
-            lists);
-        rc = check_launch("d3d_gjk_distance (mixed, FP32 phase)");
-    }
-    if (!rc) {
-        k_gjk_mixed_b<<<persistent_blocks((const void*)k_gjk_mixed_b, kBlock, n), kBlock, 0, stream>>>(
-            store, i1, i2, opt, hand, o, lists);
-        rc = check_launch("d3d_gjk_distance (mixed, FP64 phase)");
+        if (t.gjk_block == 64)
+            rc = launch_mixed<64>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, blocks_per_sm(t, 64), stream);
+        else if (t.gjk_block == 256)
+            rc = launch_mixed<256>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, blocks_per_sm(t, 256),
+                                   stream);
+        else
+            rc = launch_mixed<128>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, blocks_per_sm(t, 128),
+                                   stream);
     }
     if (!rc)
         rc = launch_gjk_f64(store, i1, i2, lists.fallback, n, lists.ctr + kNumFallback, lists.ctr + kCurC, opt, o,

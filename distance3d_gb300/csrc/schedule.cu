@@ -15,6 +15,9 @@ cudaMemPool_t g_pool[kMaxDevices] = {};
 
 inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
+std::mutex g_tune_mu;
+d3d_tuning g_tuning = {128, 0, 4, 4096};
+
 // key = ((type1 * 6 + type2) << 4) | size class of the larger hull; slots at
 // and beyond the device-side count (if given) get the largest key
 __global__ void k_pair_keys(d3d_store s, const int32_t* __restrict__ i1, const int32_t* __restrict__ i2, int64_t n,
@@ -77,15 +80,21 @@ void scratch_free(void* p, cudaStream_t stream) {
     if (p) cudaFreeAsync(p, stream);
 }
 
-int persistent_blocks(const void* kernel, int block, int64_t work_items) {
+int persistent_blocks(const void* kernel, int block, int64_t work_items, int max_per_sm, int smem) {
     int dev = 0, sms = 1, per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    if (max_per_sm > 0 && per_sm > max_per_sm) per_sm = max_per_sm;
     int64_t want = (work_items + block - 1) / block;
     int64_t full = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
     int64_t b = want < full ? want : full;
     return (int)(b > 0 ? b : 1);
+}
+
+d3d_tuning tuning() {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    return g_tuning;
 }
 
 size_t pair_order_temp_bytes(int64_t n) {
@@ -121,3 +130,21 @@ int pair_order(const d3d_store& s, const int32_t* i1, const int32_t* i2, int64_t
 }
 
 }  // namespace d3d
+
+extern "C" int d3d_get_tuning(d3d_tuning* out) {
+    D3D_REQUIRE(out, "d3d_get_tuning: null argument");
+    *out = d3d::tuning();
+    return D3D_SUCCESS;
+}
+
+extern "C" int d3d_set_tuning(const d3d_tuning* t) {
+    D3D_REQUIRE(t, "d3d_set_tuning: null argument");
+    D3D_REQUIRE(t->gjk_block == 64 || t->gjk_block == 128 || t->gjk_block == 256,
+                "d3d_set_tuning: gjk_block must be 64, 128 or 256");
+    D3D_REQUIRE(t->epa_warps == 2 || t->epa_warps == 4 || t->epa_warps == 8,
+                "d3d_set_tuning: epa_warps must be 2, 4 or 8");
+    D3D_REQUIRE(t->gjk_warps_per_sm >= 0 && t->sort_min >= 0, "d3d_set_tuning: negative value");
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuning = *t;
+    return D3D_SUCCESS;
+}

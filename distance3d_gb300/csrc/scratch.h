@@ -15,9 +15,20 @@ namespace d3d {
 int scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
 void scratch_free(void* p, cudaStream_t stream);
 
-// Blocks for a persistent launch of `kernel` with `block` threads:
-// resident blocks per SM x SMs, capped by the work.
-int persistent_blocks(const void* kernel, int block, int64_t work_items);
+// Blocks for a persistent launch of `kernel` with `block` threads and
+// `smem` bytes of dynamic shared memory: resident blocks per SM (at most
+// max_per_sm if > 0) x SMs, capped by the work.
+int persistent_blocks(const void* kernel, int block, int64_t work_items, int max_per_sm = 0, int smem = 0);
+
+// The current launch parameters (d3d_set_tuning / d3d_autotune).
+d3d_tuning tuning();
+
+// blocks per SM for a GJK grid of `block` threads under tuning t (0: no cap)
+inline int blocks_per_sm(const d3d_tuning& t, int block) {
+    if (t.gjk_warps_per_sm <= 0) return 0;
+    const int b = t.gjk_warps_per_sm / (block / 32);
+    return b > 0 ? b : 1;
+}
 
 // Processing order of n pairs (i1[k], i2[k]): pair indices sorted by
 // (type1, type2, hull-size class) so that a warp works on pairs that take the

@@ -187,6 +187,26 @@ int d3d_collide(const d3d_store* store, const int32_t* i1, const int32_t* i2, in
                 double* mtv, int8_t* epa_status, int32_t* n_faces, void* scratch, size_t scratch_bytes,
                 void* stream);
 
+/* Launch parameters of the batch kernels (process-wide, per library load).
+ * gjk_block: threads per block of the GJK kernels (64, 128 or 256);
+ * gjk_warps_per_sm: resident warps per SM of their persistent grids (0: as
+ * many as fit); epa_warps: pairs (warps) per block of the warp EPA (2, 4 or
+ * 8); sort_min: batches of at least this many pairs are sorted by collider
+ * types before GJK (larger than any batch: never). */
+typedef struct {
+    int32_t gjk_block;
+    int32_t gjk_warps_per_sm;
+    int32_t epa_warps;
+    int32_t sort_min;
+} d3d_tuning;
+int d3d_get_tuning(d3d_tuning* out);
+int d3d_set_tuning(const d3d_tuning* tuning);
+/* Time candidate tunings on the given pairs (GJK distance and EPA, both in
+ * options' precisions, on `stream`), set the fastest and return it in *out.
+ * Blocks until done. */
+int d3d_autotune(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                 const d3d_gjk_options* gjk, const d3d_epa_options* epa, d3d_tuning* out, void* stream);
+
 /* Continuous-batching collision server over one resident store (no
  * counterpart in the reference, which answers one pair per call).  A worker
  * thread batches submitted requests (host pair lists) into up to `slots`

@@ -293,8 +293,12 @@ def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=8192, slots=8):
     plain FP64 form.  Requests: lognormal pair counts (median 2,000, clipped
     to [1, 50,000]) of pairs drawn from the batched workload."""
     from distance3d_gb300.serve import NativeCollisionServer, request_sizes
+    from distance3d_gb300.tune import autotune, get_tuning, set_tuning
     rng = np.random.default_rng(seed)
     mean_size = float(request_sizes(np.random.default_rng(seed + 1), 200000).mean())
+    # the launch parameters for batches of the server's size (restored after)
+    before = get_tuning()
+    tuned = autotune(store, i1_np[:capacity], i2_np[:capacity], epa_kw=EPA_KW)
 
     def trace(count):
         sizes = request_sizes(rng, count)
@@ -303,7 +307,7 @@ def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=8192, slots=8):
 
     out = {"request_pairs": {"median": 2000, "clip": [1, 50000], "mean": mean_size},
            "latency": "arrival to results in host memory", "server": "native (d3d_server), CUDA graphs",
-           "capacity": capacity, "slots": slots}
+           "capacity": capacity, "slots": slots, "tuning": tuned}
     for precision in ("mixed", "fp64"):
         srv = NativeCollisionServer(store, capacity=capacity, slots=slots, precision=precision, epa_kw=EPA_KW)
         try:
@@ -326,6 +330,74 @@ def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=8192, slots=8):
         finally:
             srv.close()
         out[precision] = res
+    set_tuning(**before)
+    return out
+
+
+def broad_narrow_report(dev, n_colliders=131072, seed=3, reps=3):
+    """The broad+narrow workload: n colliders of the six types in
+    [-20,20]^3, FP64 AABBs, LBVH build, self-overlap query, then GJK + EPA on
+    the overlapping pairs (distance3d_gb300.pipeline.collide_scene).  Device
+    milliseconds per stage, best of `reps` after one warm-up, both forms."""
+    from distance3d_gb300 import workloads
+    from distance3d_gb300.pipeline import collide_scene
+    from distance3d_gb300.store import ColliderStore
+    cs = workloads.scene_mixed_six(n_colliders, seed=seed)
+    st = ColliderStore(cs, device=dev)
+    out = {"colliders": n_colliders, "box_half_width": 20.0, "seed": seed}
+    for precision in ("mixed", "fp64"):
+        collide_scene(st, precision=precision, epa_kw=EPA_KW)
+        best = None
+        for _ in range(reps):
+            pairs, r, t = collide_scene(st, precision=precision, epa_kw=EPA_KW, timings=True)
+            if best is None or sum(t.values()) < sum(best.values()):
+                best = t
+        total = sum(best.values())
+        out[precision] = {"ms": total, "stages_ms": best, "pairs": int(pairs.shape[0]),
+                          "epa_pairs": int((r["epa_status"] >= 0).sum().item()),
+                          "scenes_per_s": 1e3 / total, "narrow_pairs_per_s": pairs.shape[0] / best["gjk_epa"] * 1e3}
+    return out
+
+
+def robot_report(dev, n_configs=16384, seed=0, reps=3):
+    """Robot self-collision batch: n_configs joint configurations of a
+    synthetic 7-DoF arm (link lengths U[0.1,0.4] m, joint values
+    U[-pi,pi]) with 30 bodies (capsules r 0.04-0.08, boxes, cylinders);
+    every body pair on non-adjacent links tested per configuration
+    (forward kinematics, pose update, GJK + EPA in one CUDA graph).  Device
+    time per batch, best of `reps` after a warm-up, both forms; contact flags
+    compared between the forms."""
+    import torch
+    from distance3d_gb300.robot import SelfCollisionBatch, SerialArm
+    arm = SerialArm.synthetic(seed=seed)
+    q = torch.as_tensor(np.random.default_rng(seed + 1).uniform(-np.pi, np.pi, (n_configs, arm.dof)),
+                        dtype=torch.float64, device=dev)
+    out = {"configs": n_configs, "dof": arm.dof, "bodies": arm.n_bodies,
+           "pairs_per_config": int(len(arm.pair_table())), "seed": seed}
+    res = {}
+    for precision in ("mixed", "fp64"):
+        b = SelfCollisionBatch(arm, n_configs, precision=precision, graph=True, device=dev)
+        b.run(q)
+        stream = torch.cuda.current_stream(dev)
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = b.run(q, sync=False)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        res[precision] = {k: v.clone() for k, v in r.items()}
+        out[precision] = {"ms_per_batch": best, "configs_per_s": n_configs / best * 1e3,
+                          "pairs_per_s": b.n_pairs / best * 1e3,
+                          "configs_in_collision": float(r["any"].float().mean().item())}
+        del b
+    df, dm = res["fp64"]["dist"], res["mixed"]["dist"]
+    sep = df > 1e-6
+    out["contact_flags_identical_beyond_1e-6"] = bool(torch.equal(dm[sep] > 0, df[sep] > 0))
+    out["max_rel_dist_err"] = float(((dm - df).abs() / df.clamp(min=1.0)).max().item())
+    out["mixed_over_fp64"] = out["fp64"]["ms_per_batch"] / out["mixed"]["ms_per_batch"]
     return out
 
 
@@ -517,6 +589,8 @@ def run_ours(args):
     line = None
     if rank == 0:
         serve = serve_report(store, i1_np, i2_np, args.serve_seconds) if args.serve_seconds > 0 else None
+        broad = broad_narrow_report(dev)
+        robot = robot_report(dev)
         cpu_value, cores, cpu_pairs, cpu_s = time_cpu(cs, i1_np, i2_np, args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -542,6 +616,8 @@ def run_ours(args):
                              "sample": f"{cpu_pairs} pairs ({cpu_s:.1f} s) of the same workload, "
                                        "GJK + EPA, C restatement with OpenMP"},
             "serve": serve,
+            "broad_narrow": broad,
+            "robot_self_collision": robot,
             "tuning": tuned,
             "step": "one CUDA-graph replay of d3d_collide (GJK, EPA pair selection, EPA) over all pairs",
             "gpu_launches": MIXED_STEP_LAUNCHES * args.steps,

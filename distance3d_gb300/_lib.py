@@ -50,6 +50,11 @@ class Tuning(ctypes.Structure):
                 ("sort_min", ctypes.c_int32)]
 
 
+class Chain(ctypes.Structure):
+    _fields_ = [("n_joints", ctypes.c_int32), ("n_bodies", ctypes.c_int32), ("joint_axis", ctypes.c_void_p),
+                ("joint_origin", ctypes.c_void_p), ("body_link", ctypes.c_void_p), ("body_origin", ctypes.c_void_p)]
+
+
 class D3DError(RuntimeError):
     """A libd3d_gb300 entry point returned an error code."""
 
@@ -80,6 +85,7 @@ SIGNATURES = [
     ("d3d_collide_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions)]),
     ("d3d_collide", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(GjkOptions),
                             ctypes.POINTER(EpaOptions)] + [c_void_p] * 11 + [c_size_t, c_void_p]),
+    ("d3d_chain_fk", c_int, [ctypes.POINTER(Chain), c_void_p, c_int64, c_void_p, c_void_p]),
     ("d3d_get_tuning", c_int, [ctypes.POINTER(Tuning)]),
     ("d3d_set_tuning", c_int, [ctypes.POINTER(Tuning)]),
     ("d3d_autotune", c_int, [_SP, c_void_p, c_void_p, c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions),

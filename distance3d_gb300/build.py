@@ -41,6 +41,7 @@ UNITS = [
     ("collide.cu", []),
     ("server.cu", []),
     ("tune.cu", []),
+    ("robot.cu", ["-fmad=false"]),
     ("bvh.cu", []),
 ]
 

@@ -187,6 +187,25 @@ int d3d_collide(const d3d_store* store, const int32_t* i1, const int32_t* i2, in
                 double* mtv, int8_t* epa_status, int32_t* n_faces, void* scratch, size_t scratch_bytes,
                 void* stream);
 
+/* A serial kinematic chain with collision bodies (device pointers).  Link 0
+ * is the base; revolute joint j at the fixed transform joint_origin[j] of
+ * link j turns link j+1 about the unit axis joint_axis[j]; body b is fixed
+ * to link body_link[b] (0..n_joints) at body_origin[b].  Transforms are 12
+ * doubles, R row-major then t. */
+typedef struct {
+    int32_t n_joints;
+    int32_t n_bodies;
+    const double* joint_axis;    /* [n_joints][3] */
+    const double* joint_origin;  /* [n_joints][12] */
+    const int32_t* body_link;    /* [n_bodies] */
+    const double* body_origin;   /* [n_bodies][12] */
+} d3d_chain;
+/* Forward kinematics: poses[c][b][12] of every body for joint values
+ * q[c][n_joints] of configurations c < n_configs.  Feeds
+ * d3d_store_set_poses for batched self-collision checks (the pose updates
+ * self_collision.detect relies on, self_collision.py:5-64). */
+int d3d_chain_fk(const d3d_chain* chain, const double* q, int64_t n_configs, double* poses, void* stream);
+
 /* Launch parameters of the batch kernels (process-wide, per library load).
  * gjk_block: threads per block of the GJK kernels (64, 128 or 256);
  * gjk_warps_per_sm: resident warps per SM of their persistent grids (0: as

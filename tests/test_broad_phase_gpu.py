@@ -173,3 +173,24 @@ def test_deterministic_output():
     a = LBVH(aabbs).self_pairs().cpu().numpy()
     b = LBVH(aabbs).self_pairs().cpu().numpy()
     assert np.array_equal(a, b)
+
+
+def test_collide_scene_broad_then_narrow():
+    """The broad+narrow workload path: pair set bit-exact against the sweep
+    oracle, FP64 narrow phase bit-exact against the oracle's GJK on those
+    pairs, mixed form within tolerance and with the same intersection flags."""
+    from distance3d_gb300.pipeline import collide_scene
+    cs = workloads.scene_mixed_six(131072, seed=7)
+    st = ColliderStore(cs)
+    pairs, r = collide_scene(st, precision="fp64")
+    want = oracle.self_pairs_sweep(st.aabbs().cpu().numpy())
+    p = pairs.cpu().numpy()
+    assert np.array_equal(p, want) and len(p) > 1000
+    ref = oracle.gjk_distance(cs, p[:, 0], p[:, 1])
+    assert np.array_equal(r["dist"].cpu().numpy(), ref["dist"])
+    assert np.array_equal(r["simplex"].cpu().numpy(), ref["simplex"])
+    _, m = collide_scene(st, precision="mixed")
+    # the mixed form against the reference, certified where the reference's
+    # own distance disagrees with its closest points (see test_gjk_gpu)
+    from tests.test_gjk_gpu import mixed_check
+    mixed_check({k: v.cpu().numpy() for k, v in m.items()}, ref, cs, p[:, 0], p[:, 1])

@@ -35,6 +35,11 @@ SEED = 2024
 METRIC = "GJK+EPA pairs/s (mixed precision form; plain FP64 form alongside)"
 UNIT = "pairs/s"
 EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
+# DRAM bytes per pair of the mixed kernels from one ncu capture of the
+# 131,072-pair workload (k_gjk_mixed_a + k_gjk_mixed_b per pair; k_epa_warp
+# per EPA pair, 38,718 of them); traffic grows in proportion to the pairs
+NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78149376 + 3651840 + 139727616 + 12017664) / 131072,
+                           "epa_mixed": (46287616 + 118784) / 38718}
 # this library's kernels per timed mixed step (one graph replay): k_pair_keys,
 # k_gjk_mixed_a, k_gjk_mixed_b, k_gjk_distance_f64 (fallback list),
 # k_epa_select, k_epa_warp<float>, k_epa_warp<double> (fallback list), k_epa
@@ -68,6 +73,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--serve-seconds", type=float, default=2.0,
                     help="seconds of Poisson arrivals per load level in the serving report (0: skip)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch parameters (profiling runs)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the broad+narrow and robot sections (profiling runs)")
     return ap.parse_args()
 
 
@@ -469,7 +477,9 @@ def run_ours(args):
     # EPA) per precision is replayed per step, inputs resident
     from distance3d_gb300.serve import CollisionBatch
     from distance3d_gb300.tune import autotune
-    tuned = autotune(store, i1, i2, epa_kw=EPA_KW)  # on the workload itself, outside the timed region
+    from distance3d_gb300.tune import get_tuning
+    # on the workload itself, outside the timed region
+    tuned = get_tuning() if args.no_tune else autotune(store, i1, i2, epa_kw=EPA_KW)
     batches = {}
     for precision in ("mixed", "fp64"):
         b = CollisionBatch(store, n, precision=precision, epa_kw=EPA_KW, graphs=False, classes=[n])
@@ -575,8 +585,10 @@ def run_ours(args):
     epa_bytes = n_epa * (2 * REC64 + OUT_EPA + 96)
     if gjk_mixed >= epa_mixed:
         dom, t_dom, bytes_dom = "d3d_gjk_distance mixed (k_gjk_mixed_a, k_gjk_mixed_b)", gjk_mixed, gjk_bytes
+        traffic = NCU_DRAM_BYTES_PER_PAIR["gjk_mixed"] * n
     else:
-        dom, t_dom, bytes_dom = "d3d_epa mixed (k_epa_mixed)", epa_mixed, epa_bytes
+        dom, t_dom, bytes_dom = "d3d_epa mixed (k_epa_warp)", epa_mixed, epa_bytes
+        traffic = NCU_DRAM_BYTES_PER_PAIR["epa_mixed"] * n_epa
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -589,8 +601,8 @@ def run_ours(args):
     line = None
     if rank == 0:
         serve = serve_report(store, i1_np, i2_np, args.serve_seconds) if args.serve_seconds > 0 else None
-        broad = broad_narrow_report(dev)
-        robot = robot_report(dev)
+        broad = None if args.no_extras else broad_narrow_report(dev)
+        robot = None if args.no_extras else robot_report(dev)
         cpu_value, cores, cpu_pairs, cpu_s = time_cpu(cs, i1_np, i2_np, args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -609,7 +621,9 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": None,
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 131,072 pairs, "
+                                           "scaled by the pair count",
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
             "compute_roofline": compute_roofline,
             "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",

@@ -414,8 +414,9 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
                 if (i < nc) {
                     g = adj_at(P.adj[vl[head + i / 3]], i % 3);
                     if (P.vis[g] != stamp) {
+                        // w above the face's plane: n . w - n . y_a (the offset kept with the normal)
                         const Q4<T> pl = P.fn[g];
-                        if (dot(mk(pl.x, pl.y, pl.z), w - yv(P, vid(P.fv[g], 0))) > vis_eps)
+                        if (dot(mk(pl.x, pl.y, pl.z), w) - pl.w > vis_eps)
                             take = atomicExch(&P.vis[g], stamp) != stamp;
                     }
                 }
@@ -427,20 +428,33 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
             head = nvis;
             nvis += added;
         }
-        // horizon: edges of visible faces whose neighbour is not visible
-        int ne_l = 0;
-        for (int i = ln; i < 3 * nvis; i += 32) ne_l += P.vis[adj_at(P.adj[vl[i / 3]], i % 3)] != stamp;
-        int eb = warp_excl(ne_l);
-        const int ne = __shfl_sync(kFull, eb + ne_l, 31);
-        if (ne > o.max_loose_edges || ne < 3) return R;
-        for (int i = ln; i < 3 * nvis; i += 32) {
-            const int f = vl[i / 3], j = i % 3;
-            const int h = adj_at(P.adj[f], j);
-            if (P.vis[h] == stamp) continue;
-            const unsigned fw = P.fv[f];
-            const ushort4 gh = P.adj[h];
-            const int k = gh.x == f ? 0 : (gh.y == f ? 1 : 2);
-            P.hz[eb++] = make_int2(vid(fw, j) | (vid(fw, (j + 1) % 3) << 8) | (k << 16), h);
+        // horizon: edges of visible faces whose neighbour is not visible (a
+        // single visible face: its own three edges, in order)
+        int ne = 3;
+        if (nvis == 1) {
+            if (3 > o.max_loose_edges) return R;
+            if (ln < 3) {
+                const unsigned fw = P.fv[cf];
+                const int h = adj_at(P.adj[cf], ln);
+                const ushort4 gh = P.adj[h];
+                const int k = gh.x == cf ? 0 : (gh.y == cf ? 1 : 2);
+                P.hz[ln] = make_int2(vid(fw, ln) | (vid(fw, (ln + 1) % 3) << 8) | (k << 16), h);
+            }
+        } else {
+            int ne_l = 0;
+            for (int i = ln; i < 3 * nvis; i += 32) ne_l += P.vis[adj_at(P.adj[vl[i / 3]], i % 3)] != stamp;
+            int eb = warp_excl(ne_l);
+            ne = __shfl_sync(kFull, eb + ne_l, 31);
+            if (ne > o.max_loose_edges || ne < 3) return R;
+            for (int i = ln; i < 3 * nvis; i += 32) {
+                const int f = vl[i / 3], j = i % 3;
+                const int h = adj_at(P.adj[f], j);
+                if (P.vis[h] == stamp) continue;
+                const unsigned fw = P.fv[f];
+                const ushort4 gh = P.adj[h];
+                const int k = gh.x == f ? 0 : (gh.y == f ? 1 : 2);
+                P.hz[eb++] = make_int2(vid(fw, j) | (vid(fw, (j + 1) % 3) << 8) | (k << 16), h);
+            }
         }
         __syncwarp();
         for (int i = ln; i < nvis; i += 32) P.fv[vl[i]] = kDead;

@@ -23,25 +23,39 @@ struct RefineSupport {
             if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
             return load_vertex(s.verts64, c.off + hull_argmax(s.verts32, c.off, c.nv, df));
         }
-        if (c.type == D3D_CAPSULE || c.type == D3D_CYLINDER) {
-            // local z of the direction as the FP32 support computes it
+        // the curved supports normalise with one reciprocal square root (the
+        // reference divides by the norm; equal up to the last bits)
+        if (c.type == D3D_SPHERE) {
+            const double n2 = dot(d, d);
+            const d3 ctr = mk(c.t[0], c.t[1], c.t[2]);
+            if (n2 == 0.0) return ctr + mk(0.0, 0.0, c.p[0]);
+            return ctr + d * (c.p[0] * rsqrt(n2));
+        }
+        const d3 l = rt_mul(c.R, d);
+        d3 v;
+        if (c.type == D3D_ELLIPSOID) {
+            const d3 a = mk(l.x * c.p[0], l.y * c.p[1], l.z * c.p[2]);
+            const double n2 = dot(a, a);
+            const double f = n2 != 0.0 ? rsqrt(n2) : 1.0;
+            v = mk(a.x * f * c.p[0], a.y * f * c.p[1], a.z * f * c.p[2]);
+        } else {
+            // capsule / cylinder: the end is chosen by the FP32 sign of local z,
+            // as the FP32 support chooses it
             const float lz = dot102(__double2float_rn(c.R[2]), __double2float_rn(c.R[5]),
                                     __double2float_rn(c.R[8]), df.x, df.y, df.z);
             const bool up = c.type == D3D_CAPSULE ? lz > 0.f : !(lz < 0.f);
-            const d3 l = rt_mul(c.R, d);
-            d3 v;
+            const double z = up ? 0.5 * c.p[1] : -0.5 * c.p[1];
             if (c.type == D3D_CAPSULE) {
-                const double sn = sqrt(l.x * l.x + l.y * l.y + l.z * l.z);
-                v = sn == 0.0 ? mk(c.p[0], 0.0, 0.0) : l * (c.p[0] / sn);
-                v.z += up ? 0.5 * c.p[1] : -0.5 * c.p[1];
+                const double n2 = dot(l, l);
+                v = n2 == 0.0 ? mk(c.p[0], 0.0, 0.0) : l * (c.p[0] * rsqrt(n2));
+                v.z += z;
             } else {
-                const double sn = sqrt(l.x * l.x + l.y * l.y);
-                const double z = up ? 0.5 * c.p[1] : -0.5 * c.p[1];
-                v = sn == 0.0 ? mk(c.p[0], 0.0, z) : mk(l.x * (c.p[0] / sn), l.y * (c.p[0] / sn), z);
+                const double n2 = l.x * l.x + l.y * l.y;
+                const double f = n2 == 0.0 ? 0.0 : c.p[0] * rsqrt(n2);
+                v = n2 == 0.0 ? mk(c.p[0], 0.0, z) : mk(l.x * f, l.y * f, z);
             }
-            return xform(c.R, c.t, v);
         }
-        return support(c, s.verts64, d);
+        return xform(c.R, c.t, v);
     }
 };
 
@@ -110,7 +124,7 @@ __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a,
     f3 nv;
     float nl;
     int set;
-    if (closest_to_origin(L.S, L.prev, E, nv, nl, set)) {
+    if (closest_to_origin<float, RegRows<float>, true>(L.S, L.prev, E, nv, nl, set)) {
         L.dir = nv;
         L.vl = nl;
     } else {
@@ -213,7 +227,7 @@ __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, in
     double nl;
     int set;
     const double prev = replay ? DBL_MAX : g.prev;
-    if (closest_to_origin(g.S, prev, E, nv, nl, set)) {
+    if (closest_to_origin<double, Rows, true>(g.S, prev, E, nv, nl, set)) {
         g.dir = nv;
         g.vl = nl;
     } else if (replay) {

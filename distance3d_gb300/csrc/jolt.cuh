@@ -140,8 +140,9 @@ __device__ __forceinline__ V3<T> cp_line(V3<T> a, V3<T> b, const JoltEps<T>& E, 
     return a * u + b * v;
 }
 
-// _gjk_jolt.py:416-523
-template <typename T>
+// _gjk_jolt.py:416-523.  FAST (the mixed form only) divides once in the face
+// projection instead of per component.
+template <typename T, bool FAST = false>
 __device__ __forceinline__ V3<T> cp_triangle(V3<T> a, V3<T> b, V3<T> c, const JoltEps<T>& E, int& set) {
     V3<T> ab = b - a, ac = c - a, bc = c - b;
     V3<T> n = (dot(bc, bc) < dot(ac, ac)) ? cross(ab, bc) : cross(ab, ac);
@@ -207,6 +208,10 @@ __device__ __forceinline__ V3<T> cp_triangle(V3<T> a, V3<T> b, V3<T> c, const Jo
     // n * (a + b + c).dot(n) / (3.0 * n_len_sq), left to right
     T s = dot((a + b) + c, n);
     T den = T(3) * nl;
+    if (FAST) {
+        const T f = s / den;
+        return mk(n.x * f, n.y * f, n.z * f);
+    }
     return mk(n.x * s / den, n.y * s / den, n.z * s / den);
 }
 
@@ -334,7 +339,7 @@ __device__ __forceinline__ V3<T> row_of(const V3<T>* Y, int k) {
 // first tested face taken unconditionally, later ones only if strictly
 // closer).  Lanes of a warp holding simplices of 3 and 4 rows therefore run
 // cp_triangle together instead of in separate branches.
-template <typename T, typename Rows>
+template <typename T, typename Rows, bool FAST = false>
 __device__ __forceinline__ bool closest_to_origin(const Simplex<T, Rows>& S, T prev, const JoltEps<T>& E, V3<T>& v,
                                                   T& vl, int& set) {
     V3<T> r = S.Y[0];
@@ -354,7 +359,7 @@ __device__ __forceinline__ bool closest_to_origin(const Simplex<T, Rows>& S, T p
             const int i1 = f == 0 ? 1 : (f == 1 ? 2 : 3);
             const int i2 = f == 0 ? 2 : (f == 1 ? 3 : (f == 2 ? 1 : 2));
             int ns;
-            const V3<T> q = cp_triangle(row_of(S.Y, i0), row_of(S.Y, i1), row_of(S.Y, i2), E, ns);
+            const V3<T> q = cp_triangle<T, FAST>(row_of(S.Y, i0), row_of(S.Y, i1), row_of(S.Y, i2), E, ns);
             const T d2 = dot(q, q);
             if (f == 0 || d2 < best) {
                 best = d2;

@@ -100,6 +100,7 @@ SIGNATURES = [
                                   ctypes.POINTER(c_double)]),
     ("d3d_bvh_bytes", c_size_t, [c_int64]),
     ("d3d_bvh_build", c_int, [c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
+    ("d3d_bvh_refit", c_int, [c_void_p, c_int64, c_void_p, c_size_t, c_void_p]),
     ("d3d_bvh_query_bytes", c_size_t, [c_int64]),
     ("d3d_bvh_self_pairs", c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_int64, ctypes.POINTER(c_int64),
                                    c_void_p, c_size_t, c_void_p]),

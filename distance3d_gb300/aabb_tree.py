@@ -51,6 +51,16 @@ class AabbTree:
         self.root = 0
         self._bvh = None
 
+    def update_aabbs(self, aabbs):
+        """Move every leaf to a new box (same count and order): the built
+        tree is refit, not rebuilt (d3d_bvh_refit)."""
+        boxes = np.asarray(aabbs, dtype=np.float64).reshape(-1, 3, 2)
+        if len(boxes) != self.filled_len:
+            raise ValueError(f"update_aabbs needs {self.filled_len} boxes, got {len(boxes)}")
+        self.aabbs = boxes.copy()
+        if self._bvh is not None and self.filled_len:
+            self._bvh.refit(self.aabbs)
+
     def insert_aabb(self, aabb, external_data=None):
         self.insert_aabbs([aabb], [external_data])
 

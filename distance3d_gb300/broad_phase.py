@@ -54,13 +54,19 @@ class BoundingVolumeHierarchy:
             self._pending = []
 
     def update_collider_poses(self):
-        """Read every collider's pose from ``tm`` and rebuild the tree
-        (broad_phase.py:144-151)."""
-        self.aabbtree_ = AabbTree(device=self.device)
-        self._pending = []
+        """Read every collider's pose from ``tm`` (broad_phase.py:144-151).
+        The reference rebuilds its tree; here the boxes are recomputed on
+        the GPU and the tree is refit when its leaves are the same colliders
+        (same pair sets, no rebuild)."""
+        self._flush()
         for frame, collider in self.colliders_.items():
             collider.update_pose(self.tm.get_transform(frame, "origin"))
-            self._pending.append((frame, collider))
+        leaves = [c for _, c in self.aabbtree_.external_data_list]
+        if len(leaves) == len(self.colliders_) and all(a is b for a, b in zip(leaves, self.colliders_.values())):
+            self.aabbtree_.update_aabbs(collider_aabbs(leaves, self.device))
+            return
+        self.aabbtree_ = AabbTree(device=self.device)
+        self._pending = list(self.colliders_.items())
         self._flush()
 
     def get_colliders(self):

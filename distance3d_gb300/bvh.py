@@ -60,6 +60,18 @@ class LBVH:
             return pairs[:count.value]
         raise _lib.D3DError(_lib.D3D_ERR_CAPACITY, "pair count kept growing")
 
+    def refit(self, aabbs):
+        """Move the leaves to new boxes (same count and order of leaves),
+        keeping the tree's topology (d3d_bvh_refit)."""
+        with torch.cuda.device(self.device):
+            b = as_boxes(aabbs, self.device)
+            if b.shape[0] != self.n:
+                raise ValueError(f"refit needs {self.n} boxes, got {b.shape[0]}")
+            self.aabbs = b
+            _lib.check(_lib.load().d3d_bvh_refit(_ptr(self.aabbs), self.n, _ptr(self.tree), self.tree.numel(),
+                                                 _stream(self.device)))
+        return self
+
     def self_pairs(self):
         """(P,2) int32 device tensor of overlapping pairs (i, j), i < j, sorted."""
         with torch.cuda.device(self.device):

@@ -471,6 +471,28 @@ extern "C" int d3d_bvh_build(const double* aabbs, int64_t n, void* tree, size_t 
     return d3d::check_launch("d3d_bvh_build");
 }
 
+extern "C" int d3d_bvh_refit(const double* aabbs, int64_t n, void* tree, size_t tree_bytes, void* stream) {
+    D3D_REQUIRE(n >= 0 && n < (int64_t(1) << 31), "d3d_bvh_refit: n out of range");
+    D3D_REQUIRE(tree, "d3d_bvh_refit: null tree buffer");
+    size_t need = layout(nullptr, n, nullptr);
+    if (tree_bytes < need) {
+        d3d::set_error("d3d_bvh_refit: tree buffer of %zu bytes < %zu", tree_bytes, need);
+        return D3D_ERR_CAPACITY;
+    }
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(aabbs, "d3d_bvh_refit: null aabbs");
+    Tree t;
+    layout(tree, n, &t);
+    cudaStream_t st = d3d::as_stream(stream);
+    // same leaf order and topology; the boxes of leaves and nodes are redone
+    k_leaf_boxes<<<d3d::grid_for(n, kBlock), kBlock, 0, st>>>(aabbs, n, t.sorted, t.leafbox);
+    if (n > 1) {
+        cudaMemsetAsync(t.visits, 0, sizeof(int32_t) * (size_t)(n - 1), st);
+        k_refit<<<d3d::grid_for(n, kBlock), kBlock, 0, st>>>(t);
+    }
+    return d3d::check_launch("d3d_bvh_refit");
+}
+
 extern "C" size_t d3d_bvh_query_bytes(int64_t capacity) {
     if (capacity < 0) return 0;
     return 256 + 2 * up(sizeof(uint64_t) * (size_t)(capacity > 0 ? capacity : 1)) + up(query_cub_bytes(capacity));

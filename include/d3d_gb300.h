@@ -283,6 +283,13 @@ size_t d3d_bvh_bytes(int64_t n_leaves);
  * BoundingVolumeHierarchy.update_collider_poses (broad_phase.py:144-151). */
 int d3d_bvh_build(const double* aabbs, int64_t n, void* tree, size_t tree_bytes, void* stream);
 
+/* Refit a built tree to new boxes aabbs[n][3][2] of the same leaves (same
+ * Morton order and topology, boxes of leaves and nodes redone): the pose
+ * update of BoundingVolumeHierarchy.update_collider_poses
+ * (broad_phase.py:144-151) without the rebuild.  Pair sets stay exact; the
+ * tree's pruning degrades only as the leaves move far from their order. */
+int d3d_bvh_refit(const double* aabbs, int64_t n, void* tree, size_t tree_bytes, void* stream);
+
 /* Scratch bytes for a query with room for `capacity` pairs. */
 size_t d3d_bvh_query_bytes(int64_t capacity);
 

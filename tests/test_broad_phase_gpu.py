@@ -194,3 +194,59 @@ def test_collide_scene_broad_then_narrow():
     # own distance disagrees with its closest points (see test_gjk_gpu)
     from tests.test_gjk_gpu import mixed_check
     mixed_check({k: v.cpu().numpy() for k, v in m.items()}, ref, cs, p[:, 0], p[:, 1])
+
+
+def test_refit_after_moving_the_leaves():
+    """Refit keeps the pair sets exact after every leaf moves."""
+    rng = np.random.default_rng(3)
+    cs = workloads.scene_mixed_six(20000, seed=11, half_width=8.0)
+    st = ColliderStore(cs)
+    a = st.aabbs().cpu().numpy()
+    tree = LBVH(a)
+    for step in range(3):
+        shift = rng.normal(scale=0.5, size=(len(a), 3, 1))
+        b = a + shift
+        tree.refit(b)
+        assert np.array_equal(tree.self_pairs().cpu().numpy(), oracle.self_pairs_sweep(b))
+        q = b[rng.integers(0, len(b), 300)] + rng.normal(scale=0.2, size=(300, 3, 1))
+        got = tree.query(q).cpu().numpy()
+        want = oracle.cross_pairs(b, q)
+        assert np.array_equal(got, want)
+    import pytest
+    with pytest.raises(ValueError):
+        tree.refit(a[:10])
+
+
+def test_bvh_pose_update_refits():
+    """update_collider_poses moves the colliders and refits the tree: the
+    pairs equal those of a BVH built from scratch at the new poses."""
+    from distance3d_gb300 import colliders as C
+    rng = np.random.default_rng(8)
+
+    def scene(tm, centers, offsets):
+        bvh = BoundingVolumeHierarchy(tm, "base")
+        for i, c in enumerate(centers):
+            pose = np.eye(4)
+            pose[:3, 3] = c + offsets[i]
+            tm.add_transform(i, "origin", pose)
+            col = C.Box(pose, np.array([0.4, 0.3, 0.5])) if i % 2 else C.Capsule(pose, 0.2, 0.4)
+            bvh.add_collider(i, col)
+        return bvh
+
+    n = 400
+    centers = rng.uniform(-4, 4, (n, 3))
+    tm = _TM()
+    bvh = scene(tm, centers, np.zeros((n, 3)))
+    before = sorted((a[0], b[0]) for a, b in bvh.aabb_overlapping_with_self())
+    tree_id = id(bvh.aabbtree_)
+    moves = rng.normal(scale=0.3, size=(n, 3))
+    for i in range(n):
+        pose = np.eye(4)
+        pose[:3, 3] = centers[i] + moves[i]
+        tm.add_transform(i, "origin", pose)
+    bvh.update_collider_poses()
+    assert id(bvh.aabbtree_) == tree_id  # refit, not rebuilt
+    after = sorted((a[0], b[0]) for a, b in bvh.aabb_overlapping_with_self())
+    fresh = scene(_TM(), centers, moves)
+    assert after == sorted((a[0], b[0]) for a, b in fresh.aabb_overlapping_with_self())
+    assert after != before

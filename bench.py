@@ -304,9 +304,10 @@ def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=8192, slots=8):
     from distance3d_gb300.tune import autotune, get_tuning, set_tuning
     rng = np.random.default_rng(seed)
     mean_size = float(request_sizes(np.random.default_rng(seed + 1), 200000).mean())
-    # the launch parameters for batches of the server's size (restored after)
+    # the launch parameters for the server's saturated regime, every slot's
+    # batch in flight: tuned on capacity * slots pairs (restored after)
     before = get_tuning()
-    tuned = autotune(store, i1_np[:capacity], i2_np[:capacity], epa_kw=EPA_KW)
+    tuned = autotune(store, i1_np[:capacity * slots], i2_np[:capacity * slots], epa_kw=EPA_KW)
 
     def trace(count):
         sizes = request_sizes(rng, count)

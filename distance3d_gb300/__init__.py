@@ -1,7 +1,8 @@
 """distance3d_gb300: distance3d's narrow and broad phase on one GB300.
 
 Batched Jolt GJK distance and intersection, EPA, the Sphere / Capsule / Box /
-Cylinder / Ellipsoid / ConvexHullVertices support functions and AABB queries,
+Cylinder / Ellipsoid / ConvexHullVertices / Disk / Ellipse / Cone support
+functions (each optionally wrapped in Margin) and AABB queries,
 as hand-written sm_103a CUDA kernels behind the C ABI of libd3d_gb300.so
 (include/d3d_gb300.h).  The modules mirror distance3d's call surface:
 
@@ -13,6 +14,7 @@ as hand-written sm_103a CUDA kernels behind the C ABI of libd3d_gb300.so
 """
 from ._lib import (STATUS_OK, STATUS_CLIPPED, STATUS_SANITY, STATUS_MAX_ITER,  # noqa: F401
                    STATUS_EPA_NOT_CONVERGED, STATUS_EPA_FACE_OVERFLOW, STATUS_EPA_DEGENERATE, D3DError)
-from .collider_set import (ColliderSet, SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL)  # noqa: F401
+from .collider_set import (ColliderSet, SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL,  # noqa: F401
+                           DISK, ELLIPSE, CONE, MARGIN)
 
 __version__ = "0.1.0"

@@ -4,10 +4,14 @@ the device store are built from.
 One row per collider:
 
 * ``types``       int32 (n,)     SPHERE=0 CAPSULE=1 BOX=2 CYLINDER=3 ELLIPSOID=4 HULL=5
+                                 DISK=6 ELLIPSE=7 CONE=8, or-ed with MARGIN (0x100) for
+                                 a collider wrapped in distance3d's Margin
 * ``poses``       float64 (n,12) rotation R row-major (9 values) then translation t (3)
 * ``params``      float64 (n,4)  sphere (r) | capsule (r, h) | box (size xyz, full edge
                                  lengths as in distance3d colliders.py:147-184) |
-                                 cylinder (r, L) | ellipsoid (radii xyz) | hull (unused)
+                                 cylinder (r, L) | ellipsoid (radii xyz) | hull (unused) |
+                                 disk (r) | ellipse (radii, 2) | cone (r, height);
+                                 params[3] is the margin of a Margin wrapper
 * ``hull_offset`` int64 (n,)     first row of the collider in ``vertices`` (-1: none)
 * ``hull_count``  int32 (n,)     number of hull vertices
 * ``vertices``    float64 (V,4)  world-space hull vertices, xyz plus a zero pad so a
@@ -16,13 +20,20 @@ One row per collider:
 
 A sphere keeps its center in ``t`` (its rotation is unused, distance3d
 colliders.py:243-287); a ConvexHullVertices has the identity pose
-(colliders.py:143-144).  Boxes carry no vertices here: the device store derives
-their 8 vertices from pose and size (geometry.py:135-157).
+(colliders.py:143-144).  A disk keeps its normal in R column 2 (columns 0 and
+1 are derived from it on the device, utils.py:78-122); an ellipse keeps its
+two axes in R columns 0 and 1 and their cross product in column 2
+(colliders.py:546-551).  A Margin (colliders.py:606-647) wraps one collider
+of any other type; Margin of a Margin is not representable.  Boxes carry no
+vertices here: the device store derives their 8 vertices from pose and size
+(geometry.py:135-157).
 """
 import numpy as np
 
-SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL = 0, 1, 2, 3, 4, 5
-TYPE_NAMES = ("Sphere", "Capsule", "Box", "Cylinder", "Ellipsoid", "ConvexHullVertices")
+SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL, DISK, ELLIPSE, CONE = range(9)
+MARGIN = 0x100
+TYPE_NAMES = ("Sphere", "Capsule", "Box", "Cylinder", "Ellipsoid", "ConvexHullVertices", "Disk", "Ellipse",
+              "Cone")
 
 
 class ColliderSet:
@@ -48,20 +59,31 @@ class ColliderSet:
     def n_vertices(self):
         return len(self.vertices)
 
+    @property
+    def base_types(self):
+        """Type codes without the Margin flag."""
+        return self.types & ~MARGIN
+
+    @property
+    def wrapped(self):
+        """True where the collider is wrapped in Margin."""
+        return (self.types & MARGIN) != 0
+
     def validate(self):
         n = len(self.types)
         for name in ("poses", "params", "hull_offset", "hull_count"):
             if len(getattr(self, name)) != n:
                 raise ValueError(f"ColliderSet.{name} has {len(getattr(self, name))} rows, expected {n}")
-        if n and (self.types.min() < 0 or self.types.max() > HULL):
+        base = self.base_types
+        if n and (base.min() < 0 or base.max() > CONE):
             raise ValueError("ColliderSet.types holds an unknown collider type")
-        hulls = self.types == HULL
+        hulls = base == HULL
         if np.any(self.hull_count[hulls] < 1):
             raise ValueError("ConvexHullVertices needs at least one vertex")
         if np.any(self.hull_offset[hulls] < 0) or np.any(
                 self.hull_offset[hulls] + self.hull_count[hulls] > len(self.vertices)):
             raise ValueError("hull vertex range outside the vertex pool")
-        if len(self.vertices) + 8 * int(np.count_nonzero(self.types == BOX)) >= 2 ** 31:
+        if len(self.vertices) + 8 * int(np.count_nonzero(base == BOX)) >= 2 ** 31:
             raise ValueError("vertex pool larger than 2^31 rows")
 
     @staticmethod
@@ -85,7 +107,7 @@ class ColliderSet:
 
         Accepts this package's colliders and distance3d's own (the class name,
         searched along the MRO, selects the type; the attributes read are the
-        ones distance3d's constructors set, colliders.py:109-440).
+        ones distance3d's constructors set, colliders.py:109-647).
         """
         n = len(colliders)
         types = np.zeros(n, np.int32)
@@ -96,8 +118,17 @@ class ColliderSet:
         verts = []
         nv = 0
         for i, c in enumerate(colliders):
+            if _is_margin(c):
+                inner = c.collider
+                if _is_margin(inner):
+                    raise TypeError("Margin of a Margin is not supported on the GPU path")
+                params[i, 3] = float(c.margin)
+                flag = MARGIN
+                c = inner
+            else:
+                flag = 0
             t = collider_type(c)
-            types[i] = t
+            types[i] = t | flag
             if t == SPHERE:
                 pose = np.eye(4)
                 pose[:3, 3] = np.asarray(c.c, dtype=float)
@@ -114,6 +145,21 @@ class ColliderSet:
             elif t == ELLIPSOID:
                 pose = np.asarray(c.ellipsoid2origin, dtype=float)
                 params[i, :3] = np.asarray(c.radii, dtype=float)
+            elif t == DISK:
+                pose = np.eye(4)
+                pose[:3, 2] = np.asarray(c.normal, dtype=float)
+                pose[:3, 3] = np.asarray(c.c, dtype=float)
+                params[i, 0] = float(c.radius)
+            elif t == ELLIPSE:
+                axes = np.asarray(c.axes, dtype=float).reshape(2, 3)
+                pose = np.eye(4)
+                pose[:3, :2] = axes.T
+                pose[:3, 2] = np.cross(axes[0], axes[1])
+                pose[:3, 3] = np.asarray(c.c, dtype=float)
+                params[i, :2] = np.asarray(c.radii, dtype=float).reshape(-1)[:2]
+            elif t == CONE:
+                pose = np.asarray(c.cone2origin, dtype=float)
+                params[i, :2] = (float(c.radius), float(c.height))
             else:
                 pose = np.eye(4)
                 v = np.asarray(c.vertices, dtype=float).reshape(-1, 3)
@@ -125,6 +171,10 @@ class ColliderSet:
             poses[i, 9:] = pose[:3, 3]
         v = np.concatenate(verts) if verts else np.zeros((0, 3))
         return ColliderSet(types, poses, params, offs, counts, v)
+
+
+def _is_margin(c):
+    return any(k.__name__ == "Margin" for k in type(c).__mro__)
 
 
 def collider_type(c):

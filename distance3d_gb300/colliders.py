@@ -1,9 +1,11 @@
 """Colliders with distance3d's constructors and attributes.
 
-Mirrors distance3d colliders.py:17-440 for the six types on the GPU path:
-``ConvexHullVertices``, ``Box``, ``Sphere``, ``Capsule``, ``Ellipsoid`` and
-``Cylinder``.  Attributes carry the reference's names (``c``/``radius``,
-``capsule2origin``/``radius``/``height``, ``box2origin``/``size``, ...), so
+Mirrors distance3d colliders.py:17-647 for the types on the GPU path:
+``ConvexHullVertices``, ``Box``, ``Sphere``, ``Capsule``, ``Ellipsoid``,
+``Cylinder``, ``Disk``, ``Ellipse``, ``Cone`` and the ``Margin`` wrapper
+(``MeshGraph`` is not on the path).  Attributes carry the reference's names
+(``c``/``radius``, ``capsule2origin``/``radius``/``height``,
+``box2origin``/``size``, ...), so
 ``ColliderSet.from_colliders`` packs these and the reference's own objects
 alike.  ``support_function`` and ``aabb`` run on the GPU (one-collider store,
 cached until ``update_pose``); ``make_artist`` is not provided (no
@@ -205,6 +207,124 @@ class Cylinder(ConvexCollider):
         return self.cylinder2origin
 
 
+def _plane_basis(n):
+    """utils.py:78-122 plane_basis_from_normal."""
+    if abs(n[0]) >= abs(n[1]):
+        length = np.sqrt(n[0] * n[0] + n[2] * n[2])
+        x = np.array([-n[2] / length, 0.0, n[0] / length])
+        y = np.array([n[1] * x[2], n[2] * x[0] - n[0] * x[2], -n[1] * x[0]])
+    else:
+        length = np.sqrt(n[1] * n[1] + n[2] * n[2])
+        x = np.array([0.0, n[2] / length, -n[1] / length])
+        y = np.array([n[1] * x[2] - n[2] * x[1], -n[0] * x[2], n[0] * x[1]])
+    return x, y
+
+
+class Disk(ConvexCollider):
+    """Disk collider (colliders.py:443-497)."""
+
+    def __init__(self, center, radius, normal, artist=None):
+        super().__init__(artist)
+        self.c = center
+        self.radius = radius
+        self.normal = normal
+
+    def center(self):
+        return self.c
+
+    def first_vertex(self):
+        x, _ = _plane_basis(np.asarray(self.normal, dtype=float))
+        return self.c + self.radius * x
+
+    def update_pose(self, pose):
+        self.c = pose[:3, 3]
+        self.normal = pose[:3, 2]
+        self._invalidate()
+
+    def collider2origin(self):
+        x, y = _plane_basis(np.asarray(self.normal, dtype=float))
+        m = np.eye(4)
+        m[:3, :3] = np.column_stack((x, y, self.normal))
+        m[:3, 3] = self.c
+        return m
+
+
+class Ellipse(ConvexCollider):
+    """Ellipse collider (colliders.py:500-551); ``axes`` (2,3), ``radii`` (2,)."""
+
+    def __init__(self, center, axes, radii, artist=None):
+        super().__init__(artist)
+        self.c = center
+        self.axes = axes
+        self.radii = radii
+
+    def center(self):
+        return self.c
+
+    def first_vertex(self):
+        return self.c + self.axes[0] * self.radii[0]
+
+    def update_pose(self, pose):
+        self.c = pose[:3, 3]
+        self.axes = pose[:3, :2].T
+        self._invalidate()
+
+    def collider2origin(self):
+        m = np.eye(4)
+        m[:3, :2] = self.axes.T
+        m[:3, 2] = np.cross(self.axes[0], self.axes[1])
+        m[:3, 3] = self.c
+        return m
+
+
+class Cone(ConvexCollider):
+    """Cone collider (colliders.py:554-603): base disk at the origin of
+    ``cone2origin``, tip at ``height`` along its z axis."""
+
+    def __init__(self, cone2origin, radius, height, artist=None):
+        super().__init__(artist)
+        self.cone2origin = cone2origin
+        self.radius = radius
+        self.height = height
+
+    def center(self):
+        return self.cone2origin[:3, 3] + 0.5 * self.height * self.cone2origin[:3, 2]
+
+    def first_vertex(self):
+        return self.cone2origin[:3, 3] + self.height * self.cone2origin[:3, 2]
+
+    def update_pose(self, pose):
+        self.cone2origin = pose
+        self._invalidate()
+
+    def collider2origin(self):
+        return self.cone2origin
+
+
+class Margin(ConvexCollider):
+    """Margin around another collider (colliders.py:606-647): its support
+    point moved by ``margin`` along the unit search direction, its box grown
+    by ``margin``."""
+
+    def __init__(self, collider, margin):
+        super().__init__(getattr(collider, "artist_", None))
+        self.collider = collider
+        self.margin = margin
+
+    def first_vertex(self):
+        return self.collider.first_vertex()
+
+    def center(self):
+        return self.collider.center()
+
+    def update_pose(self, pose):
+        self.collider.update_pose(pose)
+        self._invalidate()
+
+    def collider2origin(self):
+        return self.collider.collider2origin()
+
+
 COLLIDERS = {
     "sphere": Sphere,
     "ellipsoid": Ellipsoid,
@@ -212,4 +332,7 @@ COLLIDERS = {
     "cylinder": Cylinder,
     "box": Box,
     "convex": ConvexHullVertices,
+    "disk": Disk,
+    "ellipse": Ellipse,
+    "cone": Cone,
 }

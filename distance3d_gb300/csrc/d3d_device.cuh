@@ -1,6 +1,7 @@
 // d3d_device.cuh -- device-side building blocks shared by the kernels of
 // libd3d_gb300: vector arithmetic with the reference's rounding sequence,
-// collider loads from the store, and the six support functions.
+// collider loads from the store, and the support functions of the nine
+// collider types and of the Margin wrapper.
 //
 // Rounding.  The reference computes its small dot products through NumPy,
 // whose BLAS rounds them as fused multiply-add chains in two fixed orders
@@ -75,11 +76,12 @@ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
 // ----------------------------------------------------------------------------
 
 // One collider as the kernels see it.  R row-major, t, params; hull vertex
-// range [off, off + nv) for boxes and hulls.
+// range [off, off + nv) for boxes and hulls; margin m when wrapped (a Margin
+// of margin 0 still adds 0 * d/|d|, as the reference does).
 template <typename T>
 struct Col {
-    int type, nv, off;
-    T R[9], t[3], p[3];
+    int type, nv, off, wrapped, idx;
+    T R[9], t[3], p[3], m;
 };
 
 __device__ __forceinline__ void load_meta(const d3d_store& s, int idx, int& type, int& nv, int& off) {
@@ -88,9 +90,18 @@ __device__ __forceinline__ void load_meta(const d3d_store& s, int idx, int& type
     nv = m.y;
     off = m.z;
 }
+template <typename T>
+__device__ __forceinline__ void load_meta(const d3d_store& s, int idx, Col<T>& c) {
+    int4 m = __ldg(reinterpret_cast<const int4*>(s.meta) + idx);
+    c.type = m.x;
+    c.nv = m.y;
+    c.off = m.z;
+    c.wrapped = m.w;
+    c.idx = idx;
+}
 
 __device__ __forceinline__ void load_col(const d3d_store& s, int idx, Col<double>& c) {
-    load_meta(s, idx, c.type, c.nv, c.off);
+    load_meta(s, idx, c);
     const double2* r = reinterpret_cast<const double2*>(s.rec64) + (size_t)idx * 8;
     double v[16];
 #pragma unroll
@@ -106,10 +117,11 @@ __device__ __forceinline__ void load_col(const d3d_store& s, int idx, Col<double
         c.t[k] = v[9 + k];
         c.p[k] = v[12 + k];
     }
+    c.m = v[15];
 }
 
 __device__ __forceinline__ void load_col(const d3d_store& s, int idx, Col<float>& c) {
-    load_meta(s, idx, c.type, c.nv, c.off);
+    load_meta(s, idx, c);
     const float4* r = reinterpret_cast<const float4*>(s.rec32) + (size_t)idx * 4;
     float v[16];
 #pragma unroll
@@ -127,6 +139,7 @@ __device__ __forceinline__ void load_col(const d3d_store& s, int idx, Col<float>
         c.t[k] = v[9 + k];
         c.p[k] = v[12 + k];
     }
+    c.m = v[15];
 }
 
 __device__ __forceinline__ d3 load_vertex(const double* verts, int row) {
@@ -172,11 +185,44 @@ __device__ __forceinline__ int hull_argmax(const T* verts, int off, int nv, V3<T
     return best;
 }
 
-// Support point of collider c along d.  Sphere geometry.py:314-346, capsule
-// :209-256, cylinder :160-206, ellipsoid :259-284 (norm_vector utils.py:12-30),
-// box and hull: first-maximum vertex (colliders.py:131-132).
+// utils.py:78-122 plane_basis_from_normal: x, y of the plane with normal n
+// (unfused Python scalar arithmetic); the record of a disk stores them as R
+// columns 0 and 1.
 template <typename T>
-__device__ __forceinline__ V3<T> support(const Col<T>& c, const T* verts, V3<T> d) {
+__device__ __forceinline__ void plane_basis(T n0, T n1, T n2, V3<T>& x, V3<T>& y) {
+    if (abs_t(n0) >= abs_t(n1)) {
+        const T len = sqrt_t(n0 * n0 + n2 * n2);
+        x = mk(-n2 / len, T(0), n0 / len);
+        y = mk(n1 * x.z, n2 * x.x - n0 * x.z, -n1 * x.x);
+    } else {
+        const T len = sqrt_t(n1 * n1 + n2 * n2);
+        x = mk(T(0), n2 / len, -n1 / len);
+        y = mk(n1 * x.z - n2 * x.y, -n0 * x.z, n0 * x.y);
+    }
+}
+
+// Cone (geometry.py:421-455): the disk point of the local direction l, and
+// whether the rim wins over the tip (np.dot(local_dir, disk_point) >=
+// local_dir[2] * height).  The FP32 refinement of the mixed form repeats this
+// decision on the FP32 record.
+template <typename T>
+__device__ __forceinline__ bool cone_rim(const Col<T>& c, V3<T> l, V3<T>& q) {
+    const T n = sqrt_t(fma_t(l.y, l.y, l.x * l.x));
+    if (n == T(0)) {
+        q = mk(T(0), T(0), T(0));
+    } else {
+        const T f = c.p[0] / n;
+        q = mk(l.x * f, l.y * f, T(0) * f);
+    }
+    return dot(l, q) >= l.z * c.p[1];
+}
+
+// Support point of the collider itself (without its margin) along d.  Sphere
+// geometry.py:314-346, capsule :209-256, cylinder :160-206, ellipsoid
+// :259-284 (norm_vector utils.py:12-30), disk :353-387, ellipse :390-418,
+// cone :421-455; box and hull: first-maximum vertex (colliders.py:131-132).
+template <typename T>
+__device__ __forceinline__ V3<T> base_support(const Col<T>& c, const T* verts, V3<T> d) {
     switch (c.type) {
     case D3D_SPHERE: {
         T n = sqrt_t(dot(d, d));
@@ -221,10 +267,59 @@ __device__ __forceinline__ V3<T> support(const Col<T>& c, const T* verts, V3<T> 
         a = mk(a.x * c.p[0], a.y * c.p[1], a.z * c.p[2]);
         return xform(c.R, c.t, a);
     }
+    case D3D_DISK: {
+        // point = np.dot(R.T, d) with R = column_stack(x, y, normal); the
+        // third component is dropped; center + np.dot(R, point)
+        const T p0 = dot012(c.R[0], c.R[3], c.R[6], d.x, d.y, d.z);
+        const T p1 = dot012(c.R[1], c.R[4], c.R[7], d.x, d.y, d.z);
+        const T n = sqrt_t(fma_t(p1, p1, p0 * p0));
+        const V3<T> ctr = mk(c.t[0], c.t[1], c.t[2]);
+        if (n == T(0)) return ctr;
+        const T f = c.p[0] / n;
+        const T q0 = p0 * f, q1 = p1 * f, q2 = T(0) * f;
+        return ctr + mk(dot102(c.R[0], c.R[1], c.R[2], q0, q1, q2), dot102(c.R[3], c.R[4], c.R[5], q0, q1, q2),
+                        dot102(c.R[6], c.R[7], c.R[8], q0, q1, q2));
+    }
+    case D3D_ELLIPSE: {
+        // axes.dot(d) over the two axis rows; norm_vector(radii * l) * radii;
+        // center + np.dot(l, axes)
+        T v0 = c.p[0] * dot102(c.R[0], c.R[3], c.R[6], d.x, d.y, d.z);
+        T v1 = c.p[1] * dot102(c.R[1], c.R[4], c.R[7], d.x, d.y, d.z);
+        const T n = sqrt_t(fma_t(v1, v1, v0 * v0));
+        if (n != T(0)) {
+            v0 = v0 / n;
+            v1 = v1 / n;
+        }
+        v0 = v0 * c.p[0];
+        v1 = v1 * c.p[1];
+        return mk(c.t[0] + fma_t(v1, c.R[1], v0 * c.R[0]), c.t[1] + fma_t(v1, c.R[4], v0 * c.R[3]),
+                  c.t[2] + fma_t(v1, c.R[7], v0 * c.R[6]));
+    }
+    case D3D_CONE: {
+        const V3<T> l = rt_mul(c.R, d);
+        V3<T> q;
+        if (!cone_rim(c, l, q)) q = mk(T(0), T(0), c.p[1]);
+        return xform(c.R, c.t, q);
+    }
     default:
         if (c.nv < 1) return mk(T(NAN), T(NAN), T(NAN));  // rejected by d3d_store_pack
         return load_vertex(verts, c.off + hull_argmax(verts, c.off, c.nv, d));
     }
+}
+
+// Margin (colliders.py:629-631): s + margin * norm_vector(d), the zero
+// direction staying zero (utils.py:26-30).
+template <typename T>
+__device__ __forceinline__ V3<T> add_margin(const Col<T>& c, V3<T> s, V3<T> d) {
+    if (!c.wrapped) return s;
+    const T n = sqrt_t(dot(d, d));
+    const V3<T> u = n == T(0) ? d : mk(d.x / n, d.y / n, d.z / n);
+    return mk(s.x + c.m * u.x, s.y + c.m * u.y, s.z + c.m * u.z);
+}
+
+template <typename T>
+__device__ __forceinline__ V3<T> support(const Col<T>& c, const T* verts, V3<T> d) {
+    return add_margin(c, base_support(c, verts, d), d);
 }
 
 }  // namespace d3d

@@ -149,7 +149,7 @@ __device__ __forceinline__ int mepa_step(MixedEpa& L, const Slot& s, const Col<f
     L.closest = closest;
     const float4 cn = s.fn[closest];
     const f3 sd = mk(cn.x, cn.y, cn.z);
-    const f3 w = support(c1, st.verts32, sd) - support(c2, st.verts32, -sd);
+    const f3 w = FastSupport::eval(c1, st, sd) - FastSupport::eval(c2, st, -sd);
     const float pd = dot(w, sd);
     const float wl = sqrtf(dot(w, w));
     L.scale = fmaxf(L.scale, wl);

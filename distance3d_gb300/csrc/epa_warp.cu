@@ -178,9 +178,9 @@ __device__ __forceinline__ f3 minkowski32(const d3d_store& st, int a, int b, f3 
         if (c.nv < 1)
             s = mk(NAN, NAN, NAN);
         else
-            s = load_vertex(st.verts32, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, dd, half_mask())));
+            s = margin_fast(st, c, load_vertex(st.verts32, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, dd, half_mask()))), dd);
     } else {
-        s = support(c, st.verts32, dd);
+        s = FastSupport::eval(c, st, dd);
     }
     const f3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
     return up ? o - s : s - o;
@@ -198,7 +198,7 @@ __device__ __forceinline__ d3 minkowski64_exact(const d3d_store& st, int a, int 
         if (c.nv < 1)
             s = mk(double(NAN), double(NAN), double(NAN));
         else
-            s = load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts64, c.off, c.nv, dd, half_mask())));
+            s = add_margin(c, load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts64, c.off, c.nv, dd, half_mask()))), dd);
     } else {
         s = support(c, st.verts64, dd);
     }
@@ -226,7 +226,9 @@ __device__ __forceinline__ d3 minkowski64(const d3d_store& st, int a, int b, d3 
             s = mk(double(NAN), double(NAN), double(NAN));
         } else {
             const f3 df = mk(__double2float_rn(dd.x), __double2float_rn(dd.y), __double2float_rn(dd.z));
-            s = load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, df, half_mask())));
+            s = margin_fast(
+                st, c, load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, df, half_mask()))),
+                dd);
         }
     } else {
         s = RefineSupport::eval(c, st, dd);

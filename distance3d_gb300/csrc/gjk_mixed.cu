@@ -49,8 +49,14 @@ struct Lists {
     unsigned long long* ctr;
 };
 
+// Phase A's register budget: at least 12 resident warps per SM (16 for
+// 256-thread blocks), which ptxas would otherwise trade for a few more
+// registers per thread.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_a(d3d_store s, const int32_t* __restrict__ i1,
+constexpr int phase_a_min_blocks() { return BLOCK == 256 ? 2 : 384 / BLOCK; }
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixed_a(d3d_store s, const int32_t* __restrict__ i1,
                                                         const int32_t* __restrict__ i2,
                                                         const int32_t* __restrict__ order, int64_t n,
                                                         const int64_t* __restrict__ n_dev, float tol_sq,

@@ -7,55 +7,143 @@
 
 namespace d3d {
 
-// FP64 support for the refinement phases.  Wherever the support function is
+// ---------------------------------------------------------------- supports
+// The mixed form evaluates the curved supports in the collider's own frame:
+// l = R^T d, one local point per type, then t + R v.  Wherever a support is
 // discontinuous -- the vertex of a polytope, the end of a capsule or a
-// cylinder (local z of the direction near 0) -- the choice is made in FP32,
-// exactly as the FP32 phase makes it (the FP32 record is the FP64 one
-// rounded, so its values are recomputed from the FP64 record here), and only
-// the point itself is evaluated in FP64.  A row re-evaluated along the
-// direction that produced it in FP32 therefore lands on the same feature; near
-// a discontinuity both features are supports to within the FP32 rounding of
-// the direction.
+// cylinder (local z near 0), the tip or the rim of a cone -- the choice is
+// made in FP32 on the FP32 record (the FP64 record rounded), and the FP64
+// refinement repeats that FP32 choice and evaluates only the point in FP64.
+// A row re-evaluated along the direction that produced it in FP32 therefore
+// lands on the same feature; near a discontinuity both features are supports
+// to within the FP32 rounding of the direction.  Norms are one reciprocal
+// square root (the reference divides by the norm; equal up to the last bits).
+
+__device__ __forceinline__ float rsqrt_t(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrt_t(double x) { return rsqrt(x); }
+
+// The discrete choice of the two-feature supports, in FP32: capsule and
+// cylinder upper end, cone rim (otherwise its tip).
+__device__ __forceinline__ bool upper_feature(int type, const float* R, float r, float h, f3 d) {
+    if (type == D3D_CONE) {
+        Col<float> cf;
+        cf.p[0] = r;
+        cf.p[1] = h;
+        f3 q;
+        return cone_rim(cf, rt_mul(R, d), q);
+    }
+    const float lz = dot102(R[2], R[5], R[8], d.x, d.y, d.z);
+    return type == D3D_CAPSULE ? lz > 0.f : !(lz < 0.f);
+}
+
+// Local support point v of a curved collider (not sphere, box or hull) for
+// the local direction l, with the discrete choice `up` made beforehand.
+template <typename T>
+__device__ __forceinline__ V3<T> local_point(const Col<T>& c, V3<T> l, bool up) {
+    const T r = c.p[0];
+    switch (c.type) {
+    case D3D_CAPSULE: {
+        const T n2 = dot(l, l);
+        V3<T> v = n2 == T(0) ? mk(r, T(0), T(0)) : l * (r * rsqrt_t(n2));
+        v.z += up ? T(0.5) * c.p[1] : T(-0.5) * c.p[1];
+        return v;
+    }
+    case D3D_ELLIPSOID: {
+        const V3<T> a = mk(l.x * c.p[0], l.y * c.p[1], l.z * c.p[2]);
+        const T n2 = dot(a, a);
+        const T f = n2 != T(0) ? rsqrt_t(n2) : T(1);
+        return mk(a.x * f * c.p[0], a.y * f * c.p[1], a.z * f * c.p[2]);
+    }
+    case D3D_ELLIPSE: {
+        const T a0 = l.x * c.p[0], a1 = l.y * c.p[1];
+        const T n2 = a0 * a0 + a1 * a1;
+        const T f = n2 != T(0) ? rsqrt_t(n2) : T(1);
+        return mk(a0 * f * c.p[0], a1 * f * c.p[1], T(0));
+    }
+    default: {  // cylinder, disk, cone: the rim point r (l.x, l.y) / |(l.x, l.y)|
+        const T n2 = l.x * l.x + l.y * l.y;
+        const T f = n2 != T(0) ? r * rsqrt_t(n2) : T(0);
+        if (c.type == D3D_CYLINDER) {
+            const T z = up ? T(0.5) * c.p[1] : T(-0.5) * c.p[1];
+            return n2 == T(0) ? mk(r, T(0), z) : mk(l.x * f, l.y * f, z);
+        }
+        if (c.type == D3D_CONE && !up) return mk(T(0), T(0), c.p[1]);
+        return mk(l.x * f, l.y * f, T(0));
+    }
+    }
+}
+
+// Margin: s + m d / |d| (the zero direction adds nothing).  The margin is
+// read from the record only here, so that no register holds it through the
+// support evaluation.
+__device__ __forceinline__ float record_margin(const d3d_store& st, const Col<float>& c) {
+    return __ldg(st.rec32 + (size_t)c.idx * 16 + 15);
+}
+__device__ __forceinline__ double record_margin(const d3d_store& st, const Col<double>& c) {
+    return __ldg(st.rec64 + (size_t)c.idx * 16 + 15);
+}
+template <typename T>
+__device__ __forceinline__ V3<T> margin_fast(const d3d_store& st, const Col<T>& c, V3<T> s, V3<T> d) {
+    if (!c.wrapped) return s;
+    const T n2 = dot(d, d);
+    return n2 == T(0) ? s : s + d * (record_margin(st, c) * rsqrt_t(n2));
+}
+
+// FP32 support of the mixed form's search phases.
+struct FastSupport {
+    static __device__ __forceinline__ f3 base(const Col<float>& c, const d3d_store& s, f3 d) {
+        if (c.type == D3D_BOX || c.type == D3D_HULL) {
+            if (c.nv < 1) return mk(NAN, NAN, NAN);
+            return load_vertex(s.verts32, c.off + hull_argmax(s.verts32, c.off, c.nv, d));
+        }
+        if (c.type == D3D_SPHERE) {
+            const float n2 = dot(d, d);
+            const f3 ctr = mk(c.t[0], c.t[1], c.t[2]);
+            return n2 == 0.f ? ctr + mk(0.f, 0.f, c.p[0]) : ctr + d * (c.p[0] * rsqrtf(n2));
+        }
+        const bool up = upper_feature(c.type, c.R, c.p[0], c.p[1], d);
+        return xform(c.R, c.t, local_point(c, rt_mul(c.R, d), up));
+    }
+    static __device__ __forceinline__ f3 eval(const Col<float>& c, const d3d_store& s, f3 d) {
+        return margin_fast(s, c, base(c, s, d), d);
+    }
+};
+
+// FP64 support of the refinement phases, with FastSupport's FP32 choices.
 struct RefineSupport {
     static __device__ __forceinline__ d3 eval(const Col<double>& c, const d3d_store& s, d3 d) {
+        return margin_fast(s, c, base(c, s, d), d);
+    }
+
+    static __device__ __forceinline__ d3 base(const Col<double>& c, const d3d_store& s, d3 d) {
         const f3 df = mk(__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z));
         if (c.type == D3D_BOX || c.type == D3D_HULL) {
             if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
             return load_vertex(s.verts64, c.off + hull_argmax(s.verts32, c.off, c.nv, df));
         }
-        // the curved supports normalise with one reciprocal square root (the
-        // reference divides by the norm; equal up to the last bits)
         if (c.type == D3D_SPHERE) {
             const double n2 = dot(d, d);
             const d3 ctr = mk(c.t[0], c.t[1], c.t[2]);
-            if (n2 == 0.0) return ctr + mk(0.0, 0.0, c.p[0]);
-            return ctr + d * (c.p[0] * rsqrt(n2));
+            return n2 == 0.0 ? ctr + mk(0.0, 0.0, c.p[0]) : ctr + d * (c.p[0] * rsqrt(n2));
         }
-        const d3 l = rt_mul(c.R, d);
-        d3 v;
-        if (c.type == D3D_ELLIPSOID) {
-            const d3 a = mk(l.x * c.p[0], l.y * c.p[1], l.z * c.p[2]);
-            const double n2 = dot(a, a);
-            const double f = n2 != 0.0 ? rsqrt(n2) : 1.0;
-            v = mk(a.x * f * c.p[0], a.y * f * c.p[1], a.z * f * c.p[2]);
-        } else {
-            // capsule / cylinder: the end is chosen by the FP32 sign of local z,
-            // as the FP32 support chooses it
-            const float lz = dot102(__double2float_rn(c.R[2]), __double2float_rn(c.R[5]),
-                                    __double2float_rn(c.R[8]), df.x, df.y, df.z);
-            const bool up = c.type == D3D_CAPSULE ? lz > 0.f : !(lz < 0.f);
-            const double z = up ? 0.5 * c.p[1] : -0.5 * c.p[1];
-            if (c.type == D3D_CAPSULE) {
-                const double n2 = dot(l, l);
-                v = n2 == 0.0 ? mk(c.p[0], 0.0, 0.0) : l * (c.p[0] * rsqrt(n2));
-                v.z += z;
-            } else {
-                const double n2 = l.x * l.x + l.y * l.y;
-                const double f = n2 == 0.0 ? 0.0 : c.p[0] * rsqrt(n2);
-                v = n2 == 0.0 ? mk(c.p[0], 0.0, z) : mk(l.x * f, l.y * f, z);
+        bool up = false;
+        if (c.type == D3D_CAPSULE || c.type == D3D_CYLINDER || c.type == D3D_CONE) {
+            // the FP32 record's rotation: column 2 (capsule, cylinder) or all (cone)
+            float Rf[9] = {};
+            Rf[2] = __double2float_rn(c.R[2]);
+            Rf[5] = __double2float_rn(c.R[5]);
+            Rf[8] = __double2float_rn(c.R[8]);
+            if (c.type == D3D_CONE) {
+                Rf[0] = __double2float_rn(c.R[0]);
+                Rf[1] = __double2float_rn(c.R[1]);
+                Rf[3] = __double2float_rn(c.R[3]);
+                Rf[4] = __double2float_rn(c.R[4]);
+                Rf[6] = __double2float_rn(c.R[6]);
+                Rf[7] = __double2float_rn(c.R[7]);
             }
+            up = upper_feature(c.type, Rf, __double2float_rn(c.p[0]), __double2float_rn(c.p[1]), df);
         }
-        return xform(c.R, c.t, v);
+        return xform(c.R, c.t, local_point(c, rt_mul(c.R, d), up));
     }
 };
 
@@ -116,7 +204,7 @@ __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a,
     if (L.it >= max_iter) return PA_FAILED;
     ++L.it;
     f3 p, q;
-    pair_supports<float, ExactSupport>(s, a, b, L.dir, p, q);
+    pair_supports<float, FastSupport>(s, a, b, L.dir, p, q);
     f3 w = p - q;
     float dd = dot(L.dir, w);
     if (dd < 0.f && dd * dd > L.vl * max_d2) return PA_CLIPPED;

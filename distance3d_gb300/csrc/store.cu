@@ -28,7 +28,23 @@ __device__ void write_box_vertices(const d3d_store& s, int off, const double* R,
     }
 }
 
-__device__ void write_record(const d3d_store& s, int i, const double* R, const double* t, const double* p) {
+// A disk's rotation is column_stack(x, y, normal) with x, y derived from its
+// normal, R column 2 (colliders.py:483-487 keeps only the normal of a pose;
+// geometry.py:375-376 derives the basis in every support call).
+__device__ void canonical_rotation(int type, double* R) {
+    if (type != D3D_DISK) return;
+    d3 x, y;
+    plane_basis(R[2], R[5], R[8], x, y);
+    R[0] = x.x;
+    R[3] = x.y;
+    R[6] = x.z;
+    R[1] = y.x;
+    R[4] = y.y;
+    R[7] = y.z;
+}
+
+__device__ void write_record(const d3d_store& s, int i, const double* R, const double* t, const double* p,
+                             double margin) {
     double* r = s.rec64 + (size_t)i * 16;
     float* f = s.rec32 + (size_t)i * 16;
 #pragma unroll
@@ -43,8 +59,8 @@ __device__ void write_record(const d3d_store& s, int i, const double* R, const d
         r[12 + k] = p[k];
         f[12 + k] = __double2float_rn(p[k]);
     }
-    r[15] = 0.0;
-    f[15] = 0.f;
+    r[15] = margin;
+    f[15] = __double2float_rn(margin);
 }
 
 __global__ void k_pack(d3d_store s, const int32_t* __restrict__ types, const double* __restrict__ poses,
@@ -52,14 +68,16 @@ __global__ void k_pack(d3d_store s, const int32_t* __restrict__ types, const dou
                        const int32_t* __restrict__ hull_count, int64_t n, int* __restrict__ bad) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int type = types[i];
+    const int wrapped = (types[i] & D3D_MARGIN) ? 1 : 0;
+    const int type = types[i] & ~D3D_MARGIN;
     double R[9], t[3], p[3];
     for (int k = 0; k < 9; ++k) R[k] = poses[i * 12 + k];
     for (int k = 0; k < 3; ++k) {
         t[k] = poses[i * 12 + 9 + k];
         p[k] = params[i * 4 + k];
     }
-    write_record(s, (int)i, R, t, p);
+    canonical_rotation(type, R);
+    write_record(s, (int)i, R, t, p, wrapped ? params[i * 4 + 3] : 0.0);
     int count = 0, off = 0;
     if (type == D3D_BOX) {
         count = 8;
@@ -80,10 +98,10 @@ __global__ void k_pack(d3d_store s, const int32_t* __restrict__ types, const dou
         } else {
             off = (int)o;
         }
-    } else if (type < 0 || type > D3D_HULL) {
+    } else if (type < 0 || type > D3D_CONE) {
         atomicExch(bad, 1);
     }
-    reinterpret_cast<int4*>(s.meta)[i] = make_int4(type, count, off, 0);
+    reinterpret_cast<int4*>(s.meta)[i] = make_int4(type, count, off, wrapped);
 }
 
 __global__ void k_hull_to_f32(d3d_store s, int64_t rows) {
@@ -110,7 +128,8 @@ __global__ void k_set_poses(d3d_store s, const int32_t* __restrict__ idx, const 
     int type, nv, off;
     load_meta(s, i, type, nv, off);
     if (type == D3D_HULL) return;
-    write_record(s, i, R, t, p);
+    canonical_rotation(type, R);
+    write_record(s, i, R, t, p, s.rec64[(size_t)i * 16 + 15]);
     if (type == D3D_BOX && nv == 8) write_box_vertices(s, off, R, t, p);
 }
 
@@ -126,7 +145,11 @@ __global__ void k_support(d3d_store s, const int32_t* __restrict__ idx, const do
     out[3 * k + 2] = r.z;
 }
 
-// containment.py:6-148, one collider per thread; writes [axis][min,max]
+// np.minimum / np.maximum: a NaN operand gives NaN
+__device__ __forceinline__ double np_min(double a, double b) { return (a != a || a < b) ? a : b; }
+__device__ __forceinline__ double np_max(double a, double b) { return (a != a || a > b) ? a : b; }
+
+// containment.py:6-229, one collider per thread; writes [axis][min,max]
 __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n, double* __restrict__ out) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -178,6 +201,31 @@ __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n,
         }
         break;
     }
+    case D3D_DISK:  // :151-174
+        for (int i = 0; i < 3; ++i) {
+            const double a = R[i * 3 + 2];
+            const double e = c.p[0] * sqrt(1.0 - a * a);
+            lo[i] = t[i] - e;
+            hi[i] = t[i] + e;
+        }
+        break;
+    case D3D_ELLIPSE:  // :206-229
+        for (int i = 0; i < 3; ++i) {
+            const double a = c.p[0] * R[i * 3], b = c.p[1] * R[i * 3 + 1];
+            const double e = sqrt(a * a + b * b);
+            lo[i] = t[i] - e;
+            hi[i] = t[i] + e;
+        }
+        break;
+    case D3D_CONE:  // :177-203
+        for (int i = 0; i < 3; ++i) {
+            const double pb = t[i] + c.p[1] * R[i * 3 + 2];
+            const double a = pb - t[i];
+            const double e = sqrt(1.0 - a * a / (c.p[1] * c.p[1]));
+            lo[i] = np_min(t[i] - e * c.p[0], pb);
+            hi[i] = np_max(t[i] + e * c.p[0], pb);
+        }
+        break;
     default: {  // box :47-67, hull :6-22
         if (c.nv < 1) {  // rejected by d3d_store_pack
             for (int i = 0; i < 3; ++i) lo[i] = hi[i] = NAN;
@@ -198,6 +246,12 @@ __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n,
         }
         break;
     }
+    }
+    if (c.wrapped) {  // colliders.py:639-643
+        for (int i = 0; i < 3; ++i) {
+            lo[i] = lo[i] - c.m;
+            hi[i] = hi[i] + c.m;
+        }
     }
     for (int i = 0; i < 3; ++i) {
         out[6 * k + 2 * i] = lo[i];

@@ -9,10 +9,11 @@
 //            setting unchanged
 //   stage 2  warp-EPA pairs per block {2, 4, 8} with the stage-1 winner
 //
-// Each candidate runs once untimed and twice timed (CUDA events on the
-// caller's stream); the faster of the two counts.  The result is process
+// Each candidate runs once untimed, then three timed samples of 1-16 runs
+// (CUDA events on the caller's stream); the fastest sample counts.  The result is process
 // state (d3d_set_tuning), read by every later launch.
 #include <climits>
+#include <cmath>
 #include <vector>
 
 #include "capi_util.h"
@@ -35,17 +36,19 @@ int run(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
                        (double*)b.p[8], (int8_t*)b.p[9], (int32_t*)b.p[10], b.p[11], b.scratch_bytes, st);
 }
 
-// milliseconds of the faster of two timed runs, or a negative code
+// milliseconds per run (the fastest of three timed samples, each sample
+// repeating the run until it spans about 2 ms, so that small batches are not
+// timed at the events' resolution), or a negative code
 float time_tuning(const d3d_tuning& t, const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
                   const d3d_gjk_options* gjk, const d3d_epa_options* epa, Buffers& b, cudaStream_t st,
                   cudaEvent_t e0, cudaEvent_t e1, int* rc) {
     *rc = d3d_set_tuning(&t);
     if (*rc) return -1.f;
-    *rc = run(store, i1, i2, n, gjk, epa, b, st);
+    int reps = 1;
     float best = -1.f;
-    for (int k = 0; k < 2 && !*rc; ++k) {
+    for (int k = 0; k < 4 && !*rc; ++k) {  // sample 0: warm-up and estimate
         cudaEventRecord(e0, st);
-        *rc = run(store, i1, i2, n, gjk, epa, b, st);
+        for (int r = 0; r < reps && !*rc; ++r) *rc = run(store, i1, i2, n, gjk, epa, b, st);
         cudaEventRecord(e1, st);
         if (cudaEventSynchronize(e1) != cudaSuccess) {
             *rc = D3D_ERR_CUDA;
@@ -53,6 +56,12 @@ float time_tuning(const d3d_tuning& t, const d3d_store* store, const int32_t* i1
         }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
+        if (k == 0) {
+            reps = ms > 0.f ? (int)ceilf(2.f / ms) : 16;
+            reps = reps < 1 ? 1 : (reps > 16 ? 16 : reps);
+            continue;
+        }
+        ms /= (float)reps;
         if (best < 0.f || ms < best) best = ms;
     }
     return best;

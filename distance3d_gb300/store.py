@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .collider_set import ColliderSet, BOX
+from .collider_set import ColliderSet, BOX, HULL, MARGIN
 
 
 def _ptr(t):
@@ -40,7 +40,7 @@ class PinnedColliderSet:
     store from it is a set of asynchronous host-to-device copies."""
 
     def __init__(self, cs):
-        boxes = np.flatnonzero(cs.types == BOX)
+        boxes = np.flatnonzero(cs.base_types == BOX)
         offsets = cs.hull_offset.copy()
         counts = cs.hull_count.copy()
         offsets[boxes] = cs.n_vertices + 8 * np.arange(len(boxes), dtype=np.int64)
@@ -85,7 +85,7 @@ class ColliderStore:
             self.device = torch.device("cuda", torch.cuda.current_device())
         cs = colliders
         n = len(cs)
-        boxes = np.flatnonzero(cs.types == BOX)
+        boxes = np.flatnonzero(cs.base_types == BOX)
         nv_hull = cs.n_vertices
         n_vertices = nv_hull + 8 * len(boxes)
         offsets = cs.hull_offset.copy()
@@ -160,7 +160,7 @@ class ColliderStore:
     def set_poses(self, idx, poses):
         """Set 4x4 (or 12-value R|t) poses of colliders ``idx`` (not hulls)."""
         idx_np = np.asarray(idx.cpu() if isinstance(idx, torch.Tensor) else idx, dtype=np.int64).reshape(-1)
-        if np.any(self.types_host[idx_np] == 5):
+        if np.any((self.types_host[idx_np] & ~MARGIN) == HULL):
             raise NotImplementedError("update_pose is not implemented for ConvexHullVertices")
         p = torch.as_tensor(poses, dtype=torch.float64)
         if p.ndim == 3:

@@ -17,10 +17,17 @@ from disk.  Rotations are quaternions drawn from a normalised 4-D Gaussian.
   ``INTERSECT30_HALF_WIDTH`` is calibrated to ~30% intersecting pairs.
 * ``scene_mixed_six``: broad-phase scene, the same type/size distributions
   placed uniformly in [-20,20]^3.
+* ``pairs_all_types``: the nine collider types, disk radius U[0.05,0.3],
+  ellipse radii U[0.05,0.3] per axis, cone radius U[0.05,0.3] and height
+  U[0.1,0.5] (the capsule's ranges), and a fraction of the colliders wrapped
+  in Margin with margin U[0.01,0.05].
 """
 import numpy as np
 
-from .collider_set import ColliderSet, SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL
+from .collider_set import (ColliderSet, SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL, DISK, ELLIPSE, CONE,
+                           MARGIN)
+
+ALL_TYPES = (SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL, DISK, ELLIPSE, CONE)
 
 # center half-width for which ~30% of mixed six-type pairs intersect
 # (calibrated with the oracle on 200k pairs, seed 0; see tests/test_workloads.py)
@@ -45,8 +52,10 @@ def random_rotations(rng, n):
     return R
 
 
-def random_colliders(rng, n, type_choices, center_half_width=1.0, hull_n_range=(8, 256)):
-    """n colliders with types drawn uniformly from ``type_choices``."""
+def random_colliders(rng, n, type_choices, center_half_width=1.0, hull_n_range=(8, 256), margin_fraction=0.0):
+    """n colliders with types drawn uniformly from ``type_choices``; with
+    ``margin_fraction`` > 0 that fraction is wrapped in Margin (the draws for
+    it come last, so the colliders themselves do not depend on it)."""
     types = rng.choice(np.asarray(type_choices, dtype=np.int32), size=n).astype(np.int32)
     R = random_rotations(rng, n)
     t = rng.uniform(-center_half_width, center_half_width, size=(n, 3))
@@ -65,6 +74,13 @@ def random_colliders(rng, n, type_choices, center_half_width=1.0, hull_n_range=(
     params[m, 1] = h[m]
     m = types == ELLIPSOID
     params[m, :3] = u[m]
+    m = types == DISK
+    params[m, 0] = u[m, 0]
+    m = types == ELLIPSE
+    params[m, :2] = u[m, :2]
+    m = types == CONE
+    params[m, 0] = u[m, 0]
+    params[m, 1] = h[m]
     hulls = np.flatnonzero(types == HULL)
     counts = np.zeros(n, np.int32)
     offsets = np.full(n, -1, np.int64)
@@ -86,6 +102,10 @@ def random_colliders(rng, n, type_choices, center_half_width=1.0, hull_n_range=(
     t[hulls] = 0.0
     R[types == SPHERE] = np.eye(3)
     poses = np.concatenate([R.reshape(n, 9), t], axis=1)
+    if margin_fraction > 0:
+        wrap = rng.uniform(size=n) < margin_fraction
+        params[wrap, 3] = rng.uniform(0.01, 0.05, size=int(wrap.sum()))
+        types = types | np.where(wrap, MARGIN, 0).astype(np.int32)
     return ColliderSet(types, poses, params, offsets, counts, verts)
 
 
@@ -102,6 +122,15 @@ def pairs_mixed_six(n_pairs, seed=0, center_half_width=1.0):
     rng = np.random.Generator(np.random.PCG64(seed))
     cs = random_colliders(rng, 2 * n_pairs, [SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL],
                           center_half_width)
+    idx = np.arange(n_pairs, dtype=np.int32)
+    return cs, 2 * idx, 2 * idx + 1
+
+
+def pairs_all_types(n_pairs, seed=0, center_half_width=INTERSECT30_HALF_WIDTH, margin_fraction=0.25):
+    """(ColliderSet with 2*n_pairs colliders, i1, i2): the nine types, a
+    fraction wrapped in Margin."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cs = random_colliders(rng, 2 * n_pairs, ALL_TYPES, center_half_width, margin_fraction=margin_fraction)
     idx = np.arange(n_pairs, dtype=np.int32)
     return cs, 2 * idx, 2 * idx + 1
 

@@ -35,13 +35,18 @@ extern "C" {
 #define D3D_ERR_CAPACITY 2  /* output or scratch capacity too small */
 #define D3D_ERR_CUDA 3      /* a CUDA runtime call failed */
 
-/* collider types (distance3d/colliders.py:109-440) */
+/* collider types (distance3d/colliders.py:109-647) */
 #define D3D_SPHERE 0
 #define D3D_CAPSULE 1
 #define D3D_BOX 2
 #define D3D_CYLINDER 3
 #define D3D_ELLIPSOID 4
 #define D3D_HULL 5          /* ConvexHullVertices */
+#define D3D_DISK 6          /* normal = R column 2 (colliders.py:443-497) */
+#define D3D_ELLIPSE 7       /* axes = R columns 0 and 1 (colliders.py:500-551) */
+#define D3D_CONE 8          /* colliders.py:554-603 */
+#define D3D_MARGIN 0x100    /* flag or-ed into a type: the collider wrapped in Margin
+                               (colliders.py:606-647), margin = params[3] */
 
 /* per-pair status codes */
 #define D3D_STATUS_OK 0
@@ -60,9 +65,13 @@ extern "C" {
  * Device-resident collider store.  Built by d3d_store_pack from the packed
  * host format (see distance3d_gb300/collider_set.py); all arrays are device
  * memory owned by the caller.
- *   rec64  [n][16] double : R row-major (9), t (3), params (3), 0
+ *   rec64  [n][16] double : R row-major (9), t (3), params (3), margin
  *   rec32  [n][16] float  : the same in FP32
- *   meta   [n][4]  int32  : type, vertex count, vertex offset, 0
+ *   meta   [n][4]  int32  : type (without the margin flag), vertex count,
+ *                           vertex offset, 1 if wrapped in Margin else 0
+ * A disk's R holds column_stack(x, y, normal) with x, y derived from the
+ * normal (utils.py:78-122 plane_basis_from_normal) when it is packed or
+ * posed, as the reference derives them in every support call.
  *   verts64 [V][4] double : hull vertices then 8 vertices per box (xyz, 0)
  *   verts32 [V][4] float  : the same in FP32
  */
@@ -97,7 +106,8 @@ int d3d_abi_version(void);
 const char* d3d_last_error(void);
 
 /* Pack a store.  Input arrays are the packed host format already copied to
- * the device: types[n], poses[n][12], params[n][4], hull_offset[n] (int64;
+ * the device: types[n] (D3D_* or-ed with D3D_MARGIN for a Margin wrapper),
+ * poses[n][12], params[n][4] (params[3]: the margin), hull_offset[n] (int64;
  * for a box: the row where its 8 derived vertices go, >= n_hull_vertices),
  * hull_count[n]; the caller has copied the n_hull_vertices hull rows into
  * store->verts64[0 : n_hull_vertices].  Box vertices follow

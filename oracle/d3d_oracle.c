@@ -20,8 +20,12 @@
  *
  * Collider record layout (shared with the product's host store):
  *   pose   : 12 doubles, R row-major (9) then t (3)
+ *   types  : type code, or-ed with T_MARGIN for a Margin wrapper
  *   params : 4 doubles  (sphere r | capsule r,h | box size xyz (full edge
- *            lengths) | cylinder r,L | ellipsoid radii xyz | hull unused)
+ *            lengths) | cylinder r,L | ellipsoid radii xyz | hull unused |
+ *            disk r | ellipse radii (2) | cone r,h; params[3] the margin)
+ *            A disk's normal is R column 2; an ellipse's axes are R columns
+ *            0 and 1.
  *   hull vertices: (V,4) doubles, xyz + pad, world space.
  */
 #include <math.h>
@@ -39,6 +43,10 @@
 #define T_CYLINDER 3
 #define T_ELLIPSOID 4
 #define T_HULL 5
+#define T_DISK 6
+#define T_ELLIPSE 7
+#define T_CONE 8
+#define T_MARGIN 0x100  /* flag: wrapped in Margin, margin = params[3] */
 
 #define ST_OK 0
 #define ST_CLIPPED 1
@@ -78,6 +86,8 @@ static inline v3 cross(v3 a, v3 b) {
 
 typedef struct {
     int type;
+    int wrapped;   /* Margin wrapper */
+    double margin;
     double R[9];
     double t[3];
     double p[3];
@@ -100,13 +110,34 @@ static void box_vertices(const double* R, const double* t, const double* size, d
     }
 }
 
+/* utils.py:78-122 plane_basis_from_normal (unfused scalar arithmetic) */
+static void plane_basis(const double* n, double* x, double* y) {
+    if (fabs(n[0]) >= fabs(n[1])) {
+        double len = sqrt(n[0] * n[0] + n[2] * n[2]);
+        x[0] = -n[2] / len; x[1] = 0.0; x[2] = n[0] / len;
+        y[0] = n[1] * x[2]; y[1] = n[2] * x[0] - n[0] * x[2]; y[2] = -n[1] * x[0];
+    } else {
+        double len = sqrt(n[1] * n[1] + n[2] * n[2]);
+        x[0] = 0.0; x[1] = n[2] / len; x[2] = -n[1] / len;
+        y[0] = n[1] * x[2] - n[2] * x[1]; y[1] = -n[0] * x[2]; y[2] = n[0] * x[1];
+    }
+}
+
 static void load_collider(collider* c, int idx, const int32_t* types, const double* poses,
                           const double* params, const int64_t* hull_offset,
                           const int32_t* hull_count, const double* vertices) {
-    c->type = types[idx];
+    c->type = types[idx] & ~T_MARGIN;
+    c->wrapped = (types[idx] & T_MARGIN) != 0;
+    c->margin = params[(int64_t)idx * 4 + 3];
     memcpy(c->R, poses + (int64_t)idx * 12, 9 * sizeof(double));
     memcpy(c->t, poses + (int64_t)idx * 12 + 9, 3 * sizeof(double));
     memcpy(c->p, params + (int64_t)idx * 4, 3 * sizeof(double));
+    if (c->type == T_DISK) {
+        /* R = column_stack(x, y, normal), geometry.py:375-376 */
+        double n[3] = {c->R[2], c->R[5], c->R[8]}, x[3], y[3];
+        plane_basis(n, x, y);
+        for (int i = 0; i < 3; ++i) { c->R[i * 3] = x[i]; c->R[i * 3 + 1] = y[i]; }
+    }
     c->verts = NULL;
     c->nverts = 0;
     if (c->type == T_BOX) {
@@ -135,8 +166,8 @@ static inline v3 xform(const double* R, const double* t, v3 v) {
 
 /* Support functions: colliders.py:131-132 (hull/box argmax, first max),
  * geometry.py:314-346 sphere, :209-256 capsule, :160-206 cylinder,
- * :259-284 ellipsoid. */
-static v3 support(const collider* c, v3 d) {
+ * :259-284 ellipsoid, :353-387 disk, :390-418 ellipse, :421-455 cone. */
+static v3 base_support(const collider* c, v3 d) {
     switch (c->type) {
     case T_SPHERE: {
         double n = sqrt(dot(d, d));
@@ -172,6 +203,45 @@ static v3 support(const collider* c, v3 d) {
         a = mk(a.x * c->p[0], a.y * c->p[1], a.z * c->p[2]);
         return xform(c->R, c->t, a);
     }
+    case T_DISK: {
+        const double* R = c->R;
+        /* point = np.dot(R.T, d), R from np.column_stack: ddot over columns */
+        double p0 = dot012(R[0], R[3], R[6], d.x, d.y, d.z);
+        double p1 = dot012(R[1], R[4], R[7], d.x, d.y, d.z);
+        double p2 = 0.0;  /* point[2] = 0.0 */
+        double n = sqrt(dot012(p0, p1, p2, p0, p1, p2));
+        if (n == 0.0) return mk(c->t[0], c->t[1], c->t[2]);
+        double f = c->p[0] / n;
+        p0 *= f; p1 *= f; p2 *= f;
+        /* center + np.dot(R, point), R C-contiguous: gemv */
+        return mk(c->t[0] + dot102(R[0], R[1], R[2], p0, p1, p2),
+                  c->t[1] + dot102(R[3], R[4], R[5], p0, p1, p2),
+                  c->t[2] + dot102(R[6], R[7], R[8], p0, p1, p2));
+    }
+    case T_ELLIPSE: {
+        const double* R = c->R;
+        /* local_dir = axes.dot(d): gemv over the axis rows (R columns 0, 1) */
+        double l0 = dot102(R[0], R[3], R[6], d.x, d.y, d.z);
+        double l1 = dot102(R[1], R[4], R[7], d.x, d.y, d.z);
+        double v0 = c->p[0] * l0, v1 = c->p[1] * l1;
+        double n = sqrt(fma(v1, v1, v0 * v0));  /* np.linalg.norm of 2 values */
+        if (n != 0.0) { v0 = v0 / n; v1 = v1 / n; }
+        v0 = v0 * c->p[0]; v1 = v1 * c->p[1];
+        /* center + np.dot(local_vertex, axes) */
+        return mk(c->t[0] + fma(v1, R[1], v0 * R[0]),
+                  c->t[1] + fma(v1, R[4], v0 * R[3]),
+                  c->t[2] + fma(v1, R[7], v0 * R[6]));
+    }
+    case T_CONE: {
+        double r = c->p[0], h = c->p[1];
+        v3 l = rt_mul(c->R, d);
+        v3 q = mk(l.x, l.y, 0.0);
+        double n = sqrt(dot(q, q));
+        if (n == 0.0) q = mk(0.0, 0.0, 0.0);
+        else q = scl(q, r / n);
+        if (!(dot(l, q) >= l.z * h)) q = mk(0.0, 0.0, h);
+        return xform(c->R, c->t, q);
+    }
     default: { /* box and hull */
         int best = 0;
         double bd = 0.0;
@@ -186,6 +256,15 @@ static v3 support(const collider* c, v3 d) {
         return mk(v[0], v[1], v[2]);
     }
     }
+}
+
+/* colliders.py:629-631 Margin: s + margin * norm_vector(d) (utils.py:12-30) */
+static v3 support(const collider* c, v3 d) {
+    v3 s = base_support(c, d);
+    if (!c->wrapped) return s;
+    double n = sqrt(dot(d, d));
+    v3 u = n == 0.0 ? d : mk(d.x / n, d.y / n, d.z / n);
+    return mk(s.x + c->margin * u.x, s.y + c->margin * u.y, s.z + c->margin * u.z);
 }
 
 /* ---------------- Jolt GJK sub-algorithms: gjk/_gjk_jolt.py --------------- */
@@ -612,8 +691,20 @@ static int epa(const v3* simplex, const collider* c1, const collider* c2, int ma
 
 /* ---------------------- AABBs: containment.py ---------------------------- */
 
-/* writes (3,2) [axis][min,max] */
+/* np.minimum / np.maximum: a NaN operand gives NaN */
+static inline double np_min(double a, double b) { return (a != a || a < b) ? a : b; }
+static inline double np_max(double a, double b) { return (a != a || a > b) ? a : b; }
+
+static void base_aabb(const collider* c, double* o);
+
+/* writes (3,2) [axis][min,max]; Margin colliders.py:639-643 */
 static void collider_aabb(const collider* c, double* o) {
+    base_aabb(c, o);
+    if (c->wrapped)
+        for (int i = 0; i < 3; ++i) { o[2 * i] = o[2 * i] - c->margin; o[2 * i + 1] = o[2 * i + 1] + c->margin; }
+}
+
+static void base_aabb(const collider* c, double* o) {
     const double* R = c->R;
     const double* t = c->t;
     switch (c->type) {
@@ -653,6 +744,29 @@ static void collider_aabb(const collider* c, double* o) {
         }
         return;
     }
+    case T_DISK:  /* :151-174 */
+        for (int i = 0; i < 3; ++i) {
+            double n = R[i * 3 + 2];
+            double e = c->p[0] * sqrt(1.0 - n * n);
+            o[2 * i] = t[i] - e; o[2 * i + 1] = t[i] + e;
+        }
+        return;
+    case T_ELLIPSE:  /* :206-229 */
+        for (int i = 0; i < 3; ++i) {
+            double a = c->p[0] * R[i * 3], b = c->p[1] * R[i * 3 + 1];
+            double e = sqrt(a * a + b * b);
+            o[2 * i] = t[i] - e; o[2 * i + 1] = t[i] + e;
+        }
+        return;
+    case T_CONE:  /* :177-203 */
+        for (int i = 0; i < 3; ++i) {
+            double pb = t[i] + c->p[1] * R[i * 3 + 2];
+            double a = pb - t[i];
+            double e = sqrt(1.0 - a * a / (c->p[1] * c->p[1]));
+            o[2 * i] = np_min(t[i] - e * c->p[0], pb);
+            o[2 * i + 1] = np_max(t[i] + e * c->p[0], pb);
+        }
+        return;
     default: {  /* box :47-67 and hull :6-22 (min/max of vertices) */
         for (int i = 0; i < 3; ++i) {
             double lo = c->verts[i], hi = c->verts[i];

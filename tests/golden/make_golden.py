@@ -3,8 +3,9 @@
 Run from the repository root, in a container where the reference source tree
 is available (it is NOT needed at test time):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/distance3d
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/distance3d [mixed6 scb all9 tree]
 
+(no names: every fixture).
 The reference is imported with its JIT disabled -- the mode its own CI uses --
 through the inert stand-ins in ``_standins/`` (numba: ``njit`` returns the
 function unchanged; pytransform3d: only names imported at module load).
@@ -22,6 +23,12 @@ Inputs come from ``distance3d_gb300.workloads`` (seeded).  Outputs:
   gjk_mixed6 whose four simplex rows were all written by GJK, at the default
   limits (64 faces; AssertionError -> face overflow) and at 256 faces / 128
   loose edges.
+* ``gjk_all9.npz``    -- 1,000 pairs of the nine types (``pairs_all_types``: adds
+  Disk, Ellipse and Cone, a quarter of the colliders wrapped in Margin), as
+  gjk_mixed6, plus every collider's ``support_function`` along six
+  directions (three random, +/- its local z axis, zero).
+* ``epa_all9.npz``    -- reference ``epa.epa`` on the intersecting pairs of
+  gjk_all9, as epa_mixed6.
 * ``aabb_tree.npz``   -- a 400-collider scene: reference AabbTree self overlap
   (both orders, i == j dropped, reduced to i < j), brute force
   ``all_aabbs_overlap``, BoundingVolumeHierarchy.aabb_overlapping_with_self on
@@ -51,7 +58,7 @@ def import_reference(ref_root):
 def make_ref_colliders(colliders, cs):
     out = []
     for i in range(len(cs)):
-        t = int(cs.types[i])
+        t = int(cs.types[i]) & 0xff
         pose = np.eye(4)
         pose[:3, :3] = cs.poses[i, :9].reshape(3, 3)
         pose[:3, 3] = cs.poses[i, 9:]
@@ -66,10 +73,35 @@ def make_ref_colliders(colliders, cs):
             out.append(colliders.Cylinder(pose, float(p[0]), float(p[1])))
         elif t == 4:
             out.append(colliders.Ellipsoid(pose, p[:3].copy()))
-        else:
+        elif t == 5:
             o, c = int(cs.hull_offset[i]), int(cs.hull_count[i])
             out.append(colliders.ConvexHullVertices(np.ascontiguousarray(cs.vertices[o:o + c, :3])))
+        elif t == 6:
+            out.append(colliders.Disk(pose[:3, 3].copy(), float(p[0]), pose[:3, 2].copy()))
+        elif t == 7:
+            out.append(colliders.Ellipse(pose[:3, 3].copy(), np.ascontiguousarray(pose[:3, :2].T), p[:2].copy()))
+        else:
+            out.append(colliders.Cone(pose, float(p[0]), float(p[1])))
+        if int(cs.types[i]) & 0x100:
+            out[-1] = colliders.Margin(out[-1], float(p[3]))
     return out
+
+
+def support_fixture(cols, cs, seed=11):
+    """Every collider's support_function along three random directions,
+    +/- its local z axis and the zero vector."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    n = len(cols)
+    dirs = np.zeros((n, 6, 3))
+    dirs[:, :3] = rng.standard_normal((n, 3, 3))
+    z = cs.poses[:, [2, 5, 8]]
+    dirs[:, 3] = z
+    dirs[:, 4] = -z
+    out = np.empty_like(dirs)
+    for i, c in enumerate(cols):
+        for k in range(6):
+            out[i, k] = c.support_function(dirs[i, k].copy())
+    return dict(support_dirs=dirs, supports=out)
 
 
 def ref_distance(gjk_mod, c1, c2, tolerance=1e-10, max_distance_squared=100000.0):
@@ -213,27 +245,50 @@ def tree_fixture(mods, cs, n_bvh=150, n_queries=20, seed=7):
                 queries=queries, query_idx=np.array(q_idx, np.int32), query_ptr=np.array(q_ptr, np.int64))
 
 
-def main(ref_root):
-    mods = import_reference(ref_root)
-    from distance3d_gb300 import workloads
+def make_mixed6(mods, workloads):
     print("mixed six-type pairs (calibrated ~30% intersecting)")
     cs, i1, i2 = workloads.pairs_mixed_six(1000, seed=1234, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
     gf, cols = gjk_fixture(mods, cs, i1, i2)
     print(f"  intersecting fraction {np.mean(gf['dist'] == 0.0):.3f}")
     np.savez_compressed(os.path.join(HERE, "gjk_mixed6.npz"), **gf)
-    ef = epa_fixture(mods, cols, gf)
-    np.savez_compressed(os.path.join(HERE, "epa_mixed6.npz"), **ef)
+    np.savez_compressed(os.path.join(HERE, "epa_mixed6.npz"), **epa_fixture(mods, cols, gf))
+
+
+def make_scb(mods, workloads):
     print("sphere/capsule/box pairs")
     cs, i1, i2 = workloads.pairs_sphere_capsule_box(1000, seed=99)
-    gf2, _ = gjk_fixture(mods, cs, i1, i2)
-    print(f"  intersecting fraction {np.mean(gf2['dist'] == 0.0):.3f}")
-    np.savez_compressed(os.path.join(HERE, "gjk_scb.npz"), **gf2)
+    gf, _ = gjk_fixture(mods, cs, i1, i2)
+    print(f"  intersecting fraction {np.mean(gf['dist'] == 0.0):.3f}")
+    np.savez_compressed(os.path.join(HERE, "gjk_scb.npz"), **gf)
+
+
+def make_all9(mods, workloads):
+    print("nine-type pairs with margins")
+    cs, i1, i2 = workloads.pairs_all_types(1000, seed=2024)
+    gf, cols = gjk_fixture(mods, cs, i1, i2)
+    gf.update(support_fixture(cols, cs))
+    print(f"  intersecting fraction {np.mean(gf['dist'] == 0.0):.3f}")
+    np.savez_compressed(os.path.join(HERE, "gjk_all9.npz"), **gf)
+    np.savez_compressed(os.path.join(HERE, "epa_all9.npz"), **epa_fixture(mods, cols, gf))
+
+
+def make_tree(mods, workloads):
     print("aabb tree scene")
     scene = workloads.scene_mixed_six(400, seed=4321, half_width=3.0)
     np.savez_compressed(os.path.join(HERE, "aabb_tree.npz"), **tree_fixture(mods, scene))
 
 
+FIXTURES = {"mixed6": make_mixed6, "scb": make_scb, "all9": make_all9, "tree": make_tree}
+
+
+def main(ref_root, names):
+    mods = import_reference(ref_root)
+    from distance3d_gb300 import workloads
+    for name in names or FIXTURES:
+        FIXTURES[name](mods, workloads)
+
+
 if __name__ == "__main__":
-    if len(sys.argv) != 2:
+    if len(sys.argv) < 2 or any(a not in FIXTURES for a in sys.argv[2:]):
         sys.exit(__doc__)
-    main(sys.argv[1])
+    main(sys.argv[1], sys.argv[2:])

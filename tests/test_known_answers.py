@@ -199,3 +199,51 @@ def test_epa_separation(backend):
     r2 = distance_batch(backend, moved)
     for d in r2["dist"]:
         assert approx(d) == 1.0
+
+
+def aabbs_of(backend, cols, poses=None):
+    """(n,3,2) boxes of collider objects; ``poses`` (index -> 4x4) are set
+    through the store's pose update (update_pose on the GPU path)."""
+    cs = ColliderSet.from_colliders(cols)
+    if backend == "oracle":
+        from oracle import oracle
+        if poses:
+            cs = ColliderSet(cs.types, cs.poses.copy(), cs.params, cs.hull_offset, cs.hull_count, cs.vertices)
+            for i, p in poses.items():
+                cs.poses[i, :9] = p[:3, :3].reshape(-1)
+                cs.poses[i, 9:] = p[:3, 3]
+        return oracle.aabbs(cs)
+    from distance3d_gb300.store import ColliderStore
+    st = ColliderStore(cs)
+    if poses:
+        st.set_poses(list(poses), np.stack(list(poses.values())))
+    return st.aabbs().cpu().numpy()
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_cone_disk_margin_aabbs(backend):
+    """test_colliders.py:47-97: cone, disk and Margin(box) boxes, before and
+    after update_pose."""
+    cone = colliders.Cone(np.eye(4), 0.5, 1.0)
+    disk = colliders.Disk(np.zeros(3), 0.5, np.array([0.0, 0.0, 1.0]))
+    boxm = colliders.Margin(colliders.Box(np.eye(4), np.array([1.0, 1.0, 1.0])), 0.1)
+    a = aabbs_of(backend, [cone, disk, boxm])
+    assert_array_almost_equal(a[0], [[-0.5, 0.5], [-0.5, 0.5], [0.0, 1.0]])
+    assert_array_almost_equal(a[1], [[-0.5, 0.5], [-0.5, 0.5], [0.0, 0.0]])
+    assert_array_almost_equal(a[2], [[-0.6, 0.6], [-0.6, 0.6], [-0.6, 0.6]])
+    p0, p1 = np.eye(4), np.eye(4)
+    p0[:3, 3] = 0.1, 0.2, 0.3
+    p1[:3, 3] = -0.1, -0.2, -0.3
+    a = aabbs_of(backend, [cone, disk, boxm], {0: p0, 1: p1, 2: p0})
+    assert_array_almost_equal(a[0], [[-0.4, 0.6], [-0.3, 0.7], [0.3, 1.3]])
+    assert_array_almost_equal(a[1], [[-0.6, 0.4], [-0.7, 0.3], [-0.3, -0.3]])
+    assert_array_almost_equal(a[2], [[-0.5, 0.7], [-0.4, 0.8], [-0.3, 0.9]])
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_gjk_distance_with_margin(backend):
+    """test_gjk.py:476-483: a margin of 0.1 shortens the distance by 0.1."""
+    box = colliders.Box(np.eye(4), np.array([2.0, 2.0, 2.0]))
+    sphere = colliders.Sphere(np.array([2.0, 0.0, 0.0]), 0.5)
+    r = distance_batch(backend, [(box, sphere), (colliders.Margin(box, 0.1), sphere)])
+    assert approx(r["dist"][0]) == r["dist"][1] + 0.1

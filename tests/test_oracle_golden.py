@@ -9,7 +9,7 @@ import pytest
 from oracle import oracle
 
 
-@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb"])
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb", "gjk_all9"])
 def test_gjk_distance_bit_exact(golden, name):
     g, cs = golden(name)
     r = oracle.gjk_distance(cs, g["i1"], g["i2"])
@@ -23,7 +23,7 @@ def test_gjk_distance_bit_exact(golden, name):
     assert np.all(r["status"] == 0)
 
 
-@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb"])
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb", "gjk_all9"])
 def test_gjk_intersection_and_aabbs(golden, name):
     g, cs = golden(name)
     h = oracle.gjk_intersection(cs, g["i1"], g["i2"])
@@ -32,11 +32,23 @@ def test_gjk_intersection_and_aabbs(golden, name):
     assert np.array_equal(oracle.aabbs(cs), g["aabbs"])
 
 
+def test_supports_bit_exact(golden):
+    """Every type's support function, Margin wrappers included, along random
+    directions, +/- the local z axis and the zero vector."""
+    g, cs = golden("gjk_all9")
+    n = len(cs)
+    idx = np.repeat(np.arange(n), 6)
+    got = oracle.support_batch(cs, idx, g["support_dirs"].reshape(-1, 3)).reshape(n, 6, 3)
+    assert np.array_equal(got, g["supports"])
+    assert np.unique(cs.base_types).size == 9 and cs.wrapped.any()
+
+
+@pytest.mark.parametrize("fixture", ["mixed6", "all9"])
 @pytest.mark.parametrize("tag,kw", [("default", {}),
                                     ("large", dict(max_faces=256, max_loose_edges=128))])
-def test_epa_bit_exact(golden, tag, kw):
-    g, cs = golden("gjk_mixed6")
-    e, _ = golden("epa_mixed6")
+def test_epa_bit_exact(golden, fixture, tag, kw):
+    g, cs = golden("gjk_" + fixture)
+    e, _ = golden("epa_" + fixture)
     p = e["pair"]
     r = oracle.epa(cs, g["i1"][p], g["i2"][p], g["simplex"][p], **kw)
     st = e[f"status_{tag}"]

@@ -75,7 +75,7 @@ def parse():
                     help="seconds of Poisson arrivals per load level in the serving report (0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch parameters (profiling runs)")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the broad+narrow and robot sections (profiling runs)")
+                    help="skip the broad+narrow, robot and MPR sections (profiling runs)")
     return ap.parse_args()
 
 
@@ -410,6 +410,47 @@ def robot_report(dev, n_configs=16384, seed=0, reps=3):
     return out
 
 
+def mpr_report(store, cs, i1_np, i2_np, dev, reps=3, check_pairs=20000, cpu_pairs=262144):
+    """MPR (mpr_penetration, FP64, the reference bit for bit) on the batched
+    workload: device time for all pairs (best of `reps` after a warm-up), the
+    intersection-only form, the oracle (C restatement, all host threads) on a
+    sample, and a bit-exact check of a sample against the oracle."""
+    import time
+    import torch
+    from distance3d_gb300.mpr import mpr_batch
+    from oracle import oracle
+    i1 = torch.as_tensor(i1_np, device=dev)
+    i2 = torch.as_tensor(i2_np, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {"pairs": len(i1_np), "tolerance": 1e-4, "max_iterations": 100}
+    for name, pen in (("penetration", True), ("intersection", False)):
+        r = mpr_batch(store, i1, i2, penetration=pen)
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r = mpr_batch(store, i1, i2, penetration=pen)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = {"ms": best, "pairs_per_s": len(i1_np) / best * 1e3,
+                     "intersecting_fraction": float(r["hit"].float().mean().item())}
+    k = np.arange(check_pairs)
+    got = {key: v[:check_pairs].cpu().numpy() for key, v in mpr_batch(store, i1[:check_pairs], i2[:check_pairs]).items()}
+    ref = oracle.mpr(cs, i1_np[k], i2_np[k])
+    out["bit_exact_vs_oracle_sample"] = bool(
+        np.array_equal(got["hit"], ref["hit"]) and np.array_equal(got["status"], ref["status"])
+        and all(np.array_equal(got[key], ref[key], equal_nan=True) for key in ("depth", "dir", "pos")))
+    out["check_pairs"] = check_pairs
+    t0 = time.perf_counter()
+    oracle.mpr(cs, i1_np[:cpu_pairs], i2_np[:cpu_pairs])
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"pairs_per_s": cpu_pairs / cpu_s, "cores": oracle.max_threads(), "kind": "port",
+                           "sample": f"{cpu_pairs} pairs, mpr_penetration, C restatement with OpenMP"}
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -604,6 +645,7 @@ def run_ours(args):
         serve = serve_report(store, i1_np, i2_np, args.serve_seconds) if args.serve_seconds > 0 else None
         broad = None if args.no_extras else broad_narrow_report(dev)
         robot = None if args.no_extras else robot_report(dev)
+        mpr = None if args.no_extras else mpr_report(store, cs, i1_np, i2_np, dev)
         cpu_value, cores, cpu_pairs, cpu_s = time_cpu(cs, i1_np, i2_np, args.cpu_seconds)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -633,6 +675,7 @@ def run_ours(args):
             "serve": serve,
             "broad_narrow": broad,
             "robot_self_collision": robot,
+            "mpr": mpr,
             "tuning": tuned,
             "step": "one CUDA-graph replay of d3d_collide (GJK, EPA pair selection, EPA) over all pairs",
             "gpu_launches": MIXED_STEP_LAUNCHES * args.steps,

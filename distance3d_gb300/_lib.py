@@ -35,6 +35,11 @@ class EpaOptions(ctypes.Structure):
                 ("precision", c_int32), ("epsilon", c_double)]
 
 
+class MprOptions(ctypes.Structure):
+    _fields_ = [("tolerance", c_double), ("max_iterations", c_int32), ("refine_limit", c_int32),
+                ("penetration", c_int32), ("reserved", c_int32)]
+
+
 class ServerOptions(ctypes.Structure):
     _fields_ = [("capacity", ctypes.c_int64), ("slots", ctypes.c_int32), ("use_graphs", ctypes.c_int32),
                 ("hbm_budget", ctypes.c_int64)]
@@ -85,6 +90,8 @@ SIGNATURES = [
     ("d3d_collide_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(GjkOptions), ctypes.POINTER(EpaOptions)]),
     ("d3d_collide", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, ctypes.POINTER(GjkOptions),
                             ctypes.POINTER(EpaOptions)] + [c_void_p] * 11 + [c_size_t, c_void_p]),
+    ("d3d_mpr", c_int, [_SP, c_void_p, c_void_p, c_int64, ctypes.POINTER(MprOptions), c_void_p, c_void_p,
+                        c_void_p, c_void_p, c_void_p, c_void_p]),
     ("d3d_chain_fk", c_int, [ctypes.POINTER(Chain), c_void_p, c_int64, c_void_p, c_void_p]),
     ("d3d_get_tuning", c_int, [ctypes.POINTER(Tuning)]),
     ("d3d_set_tuning", c_int, [ctypes.POINTER(Tuning)]),

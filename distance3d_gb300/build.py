@@ -43,6 +43,7 @@ UNITS = [
     ("tune.cu", []),
     ("robot.cu", ["-fmad=false"]),
     ("bvh.cu", []),
+    ("mpr.cu", ["-fmad=false"]),
 ]
 
 

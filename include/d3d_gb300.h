@@ -197,6 +197,24 @@ int d3d_collide(const d3d_store* store, const int32_t* i1, const int32_t* i2, in
                 double* mtv, int8_t* epa_status, int32_t* n_faces, void* scratch, size_t scratch_bytes,
                 void* stream);
 
+/* Minkowski portal refinement (MPR).  Replaces mpr.mpr_intersection and
+ * mpr.mpr_penetration (mpr.py:21-110), FP64, bit for bit: hit[k] for pairs
+ * (i1[k], i2[k]); with options->penetration also depth[k], dir[k][3] (unit
+ * or zero vector: adding depth * dir to the second collider separates them)
+ * and pos[k][3] (contact position), NaN where the reference returns None.
+ * status[k]: D3D_STATUS_OK, or D3D_STATUS_MAX_ITER after refine_limit portal
+ * expansions (the reference's refinement loop has no bound; hit = 0 then).
+ * Output pointers depth/dir/pos may be NULL. */
+typedef struct d3d_mpr_options {
+    double tolerance;        /* 1e-4 (mpr.py:21) */
+    int32_t max_iterations;  /* 100: portal discovery and penetration search */
+    int32_t refine_limit;    /* 10000: bound on the refinement loop */
+    int32_t penetration;     /* 1: mpr_penetration, 0: mpr_intersection */
+    int32_t reserved;        /* 0 */
+} d3d_mpr_options;
+int d3d_mpr(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n, const d3d_mpr_options* options,
+            int8_t* hit, double* depth, double* dir, double* pos, int8_t* status, void* stream);
+
 /* A serial kinematic chain with collision bodies (device pointers).  Link 0
  * is the base; revolute joint j at the fixed transform joint_origin[j] of
  * link j turns link j+1 about the unit axis joint_axis[j]; body b is fixed

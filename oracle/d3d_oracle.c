@@ -689,6 +689,245 @@ static int epa(const v3* simplex, const collider* c1, const collider* c2, int ma
     return ST_EPA_NOT_CONVERGED;
 }
 
+/* ------------------------- MPR: mpr.py ----------------------------------- */
+
+/* ConvexCollider.center (colliders.py): the pose translation, a hull's
+ * vertex mean (np.mean(axis=0): rows summed in order, then divided), a
+ * cone's mid-axis point :582-584; Margin passes through :633-634. */
+static v3 collider_center(const collider* c) {
+    if (c->type == T_HULL) {
+        v3 s = mk(c->verts[0], c->verts[1], c->verts[2]);
+        for (int k = 1; k < c->nverts; ++k)
+            s = add(s, mk(c->verts[k * 4], c->verts[k * 4 + 1], c->verts[k * 4 + 2]));
+        double n = (double)c->nverts;
+        return mk(s.x / n, s.y / n, s.z / n);
+    }
+    v3 t = mk(c->t[0], c->t[1], c->t[2]);
+    if (c->type == T_CONE) {
+        double f = 0.5 * c->p[1];
+        return add(t, mk(f * c->R[2], f * c->R[5], f * c->R[8]));
+    }
+    return t;
+}
+
+enum { PORTAL_CONTINUE = -2, PORTAL_OUTSIDE = -1, PORTAL_BUILT = 0, PORTAL_ON_V1 = 1, PORTAL_ON_SEGMENT = 2 };
+
+/* portal rows: v (Minkowski difference), a (collider 1), b (collider 2) */
+typedef struct { v3 v[4], a[4], b[4]; } portal;
+
+static void portal_support(const collider* c1, const collider* c2, v3 d, portal* P, int i) {
+    P->a[i] = support(c1, d);
+    P->b[i] = support(c2, neg(d));
+    P->v[i] = sub(P->a[i], P->b[i]);  /* minkowski.py:23-55 */
+}
+
+static void portal_copy(portal* P, int dst, int src) {
+    P->v[dst] = P->v[src]; P->a[dst] = P->a[src]; P->b[dst] = P->b[src];
+}
+
+static inline int all_zero(v3 v) { return v.x == 0.0 && v.y == 0.0 && v.z == 0.0; }
+
+/* :123-158 _discover_portal with :161-240 */
+static int mpr_discover(const collider* c1, const collider* c2, int max_iter, portal* P) {
+    /* :161-174 origin ray from the centers */
+    P->a[0] = collider_center(c1);
+    P->b[0] = collider_center(c2);
+    P->v[0] = sub(P->a[0], P->b[0]);
+    if (all_zero(P->v[0])) P->v[0].x += EPS * 10.0;
+    /* :177-185 */
+    v3 d = norm_vec(neg(P->v[0]));
+    portal_support(c1, c2, d, P, 1);
+    if (!all_zero(P->v[1]) && dot(P->v[1], d) < EPS) return PORTAL_OUTSIDE;
+    /* :188-201 */
+    d = cross(P->v[0], P->v[1]);
+    if (dot(d, d) < EPS) return all_zero(P->v[1]) ? PORTAL_ON_V1 : PORTAL_ON_SEGMENT;
+    d = norm_vec(d);
+    portal_support(c1, c2, d, P, 2);
+    if (dot(P->v[2], d) < EPS) return PORTAL_OUTSIDE;
+    /* :204-210 */
+    d = norm_vec(cross(sub(P->v[1], P->v[0]), sub(P->v[2], P->v[0])));
+    if (dot(d, P->v[0]) > 0.0) {
+        /* :232-240 _swap_vertices keeps row idx1 as a NumPy view, so after
+         * row idx1 = row idx2 the "swap" writes row idx2 back onto itself:
+         * both rows end up holding the old row 2 */
+        portal_copy(P, 1, 2);
+        d = scl(d, -1.0);
+    }
+    int n_points = 3, it = 0;
+    while (n_points < 4) {
+        portal_support(c1, c2, d, P, 3);
+        if (dot(P->v[3], d) < EPS) return PORTAL_OUTSIDE;
+        /* :213-229 _iterate_discover_portal */
+        int cont = 0;
+        if (dot(cross(P->v[1], P->v[3]), P->v[0]) < EPS) {
+            portal_copy(P, 2, 3);
+            cont = 1;
+        }
+        if (!cont && dot(cross(P->v[3], P->v[2]), P->v[0]) < EPS) {
+            portal_copy(P, 1, 3);
+            cont = 1;
+        }
+        if (cont) d = norm_vec(cross(sub(P->v[1], P->v[0]), sub(P->v[2], P->v[0])));
+        else n_points = 4;
+        if (++it >= max_iter) break;
+    }
+    return PORTAL_BUILT;
+}
+
+/* :276-281 */
+static inline v3 portal_direction(const portal* P) {
+    return norm_vec(cross(sub(P->v[2], P->v[1]), sub(P->v[3], P->v[1])));
+}
+
+/* :290-299: min over the three portal vertices of (v4 - v_i) . d, with
+ * v[1:].dot(d) through gemv */
+static int portal_reach_tolerance(const portal* P, v3 v4, v3 d, double tol) {
+    double s4 = dot(v4, d);
+    double m = 0.0;
+    for (int i = 1; i < 4; ++i) {
+        double e = s4 - dot102(P->v[i].x, P->v[i].y, P->v[i].z, d.x, d.y, d.z);
+        if (i == 1 || e < m) m = e;
+    }
+    return m < tol + EPS;
+}
+
+/* :302-317 */
+static void expand_portal(portal* P, v3 v4, v3 a4, v3 b4) {
+    v3 c = cross(v4, P->v[0]);
+    int idx;
+    if (dot(P->v[1], c) > 0.0) idx = dot(P->v[2], c) > 0.0 ? 1 : 3;
+    else idx = dot(P->v[3], c) > 0.0 ? 2 : 1;
+    P->v[idx] = v4; P->a[idx] = a4; P->b[idx] = b4;
+}
+
+/* :243-273 _refine_portal.  The reference loops until it decides; here at
+ * most `limit` expansions, then *status = ST_MAX_ITER. */
+static int mpr_refine(const collider* c1, const collider* c2, portal* P, double tol, int limit, int* status) {
+    for (int it = 0;; ++it) {
+        v3 d = portal_direction(P);
+        if (dot(P->v[1], d) > -10.0 * EPS) return 1;
+        v3 a4 = support(c1, d), b4 = support(c2, neg(d)), v4 = sub(a4, b4);
+        if (!(dot(v4, d) > -10.0 * EPS) || portal_reach_tolerance(P, v4, d, tol)) return 0;
+        if (it >= limit) { *status = ST_MAX_ITER; return 0; }
+        expand_portal(P, v4, a4, b4);
+    }
+}
+
+/* distance/_triangle.py:12-89 point_to_triangle for the origin:
+ * returns the distance, *cp the closest point */
+static double origin_to_triangle(v3 A, v3 B, v3 C, v3* cp) {
+    const v3 o = mk(0.0, 0.0, 0.0);
+    v3 ab = sub(B, A), ac = sub(C, A);
+    v3 ap = sub(o, A);
+    double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.0 && d2 <= 0.0) { *cp = A; return sqrt(dot(sub(o, A), sub(o, A))); }
+    v3 bp = sub(o, B);
+    double d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0 && d4 <= d3) { *cp = B; return sqrt(dot(sub(o, B), sub(o, B))); }
+    double vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.0 && 0.0 <= d1 && d3 <= 0.0) {
+        double v = d1 / (d1 - d3);
+        *cp = add(A, scl(ab, v));
+    } else {
+        v3 cpt = sub(o, C);
+        double d5 = dot(ab, cpt), d6 = dot(ac, cpt);
+        if (d6 >= 0.0 && d5 <= d6) { *cp = C; return sqrt(dot(sub(o, C), sub(o, C))); }
+        double vb = d5 * d2 - d1 * d6;
+        if (vb <= 0.0 && 0.0 <= d2 && d6 <= 0.0) {
+            double w = d2 / (d2 - d6);
+            *cp = add(A, scl(ac, w));
+        } else {
+            double va = d3 * d6 - d5 * d4;
+            if (va <= 0.0 && 0.0 <= d4 - d3 && d5 - d6 >= 0.0) {
+                double w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+                *cp = add(B, scl(sub(C, B), w));
+            } else {
+                double denom = 1.0 / ((va + vb) + vc);
+                double v = vb * denom, w = vc * denom;
+                *cp = add(add(A, scl(ab, v)), scl(ac, w));
+            }
+        }
+    }
+    v3 r = sub(o, *cp);
+    return sqrt(dot(r, r));
+}
+
+/* :372-393 _contact_position: barycentric weights of the origin in the
+ * portal (np.sum in order, b.dot(V) through gemv as
+ * fma(b0,V0,b1*V1) + fma(b2,V2,b3*V3)) */
+static v3 contact_position(const portal* P, v3 d) {
+    const v3* v = P->v;
+    double w[4];
+    w[0] = dot(cross(v[1], v[2]), v[3]);
+    w[1] = dot(cross(v[3], v[2]), v[0]);
+    w[2] = dot(cross(v[0], v[1]), v[3]);
+    w[3] = dot(cross(v[2], v[1]), v[0]);
+    double sum = ((w[0] + w[1]) + w[2]) + w[3];
+    if (sum < EPS) {
+        w[0] = 0.0;
+        w[1] = dot(cross(v[2], v[3]), d);
+        w[2] = dot(cross(v[3], v[1]), d);
+        w[3] = dot(cross(v[1], v[2]), d);
+        sum = ((w[0] + w[1]) + w[2]) + w[3];
+    }
+    for (int i = 0; i < 4; ++i) w[i] = w[i] / sum;
+    double p1[3], p2[3];
+    for (int j = 0; j < 3; ++j) {
+        const double* A0 = &P->a[0].x; const double* A1 = &P->a[1].x;
+        const double* A2 = &P->a[2].x; const double* A3 = &P->a[3].x;
+        const double* B0 = &P->b[0].x; const double* B1 = &P->b[1].x;
+        const double* B2 = &P->b[2].x; const double* B3 = &P->b[3].x;
+        p1[j] = fma(w[0], A0[j], w[1] * A1[j]) + fma(w[2], A2[j], w[3] * A3[j]);
+        p2[j] = fma(w[0], B0[j], w[1] * B1[j]) + fma(w[2], B2[j], w[3] * B3[j]);
+    }
+    return mk(0.5 * (p1[0] + p2[0]), 0.5 * (p1[1] + p2[1]), 0.5 * (p1[2] + p2[2]));
+}
+
+typedef struct { int hit, status; double depth; v3 dir, pos; } mpr_result;
+
+/* :21-110 mpr_intersection (penetration = 0) and mpr_penetration; depth,
+ * dir and pos are NaN where the reference returns None. */
+static void mpr(const collider* c1, const collider* c2, double tol, int max_iter, int limit, int penetration,
+                mpr_result* r) {
+    portal P;
+    memset(&P, 0, sizeof(P));
+    r->status = ST_OK;
+    r->depth = NAN;
+    r->dir = r->pos = mk(NAN, NAN, NAN);
+    int res = mpr_discover(c1, c2, max_iter, &P);
+    if (res == PORTAL_OUTSIDE) { r->hit = 0; return; }
+    if (res == PORTAL_ON_V1 || res == PORTAL_ON_SEGMENT) {
+        r->hit = 1;
+        if (!penetration) return;
+        r->pos = scl(add(P.a[1], P.b[1]), 0.5);  /* :337-352 */
+        if (res == PORTAL_ON_V1) {
+            r->depth = 0.0;
+            r->dir = mk(0.0, 0.0, 0.0);
+        } else {
+            r->depth = sqrt(dot(P.v[1], P.v[1]));
+            r->dir = norm_vec(P.v[1]);
+        }
+        return;
+    }
+    r->hit = mpr_refine(c1, c2, &P, tol, limit, &r->status);
+    if (!r->hit || !penetration) return;
+    /* :320-334 _find_penetration_info, :355-362 _penetration_info */
+    for (int it = 0;; ++it) {
+        v3 d = portal_direction(&P);
+        v3 a4 = support(c1, d), b4 = support(c2, neg(d)), v4 = sub(a4, b4);
+        if (portal_reach_tolerance(&P, v4, d, tol) || it > max_iter) {
+            v3 cp;
+            double depth = origin_to_triangle(P.v[1], P.v[2], P.v[3], &cp);
+            if (fabs(depth) < EPS) cp = mk(0.0, 0.0, 0.0);
+            r->depth = depth;
+            r->pos = contact_position(&P, portal_direction(&P));
+            r->dir = norm_vec(cp);
+            return;
+        }
+        expand_portal(&P, v4, a4, b4);
+    }
+}
+
 /* ---------------------- AABBs: containment.py ---------------------------- */
 
 /* np.minimum / np.maximum: a NaN operand gives NaN */
@@ -982,5 +1221,25 @@ void orc_support_batch(SET_ARGS, const int32_t* idx, const double* dirs, int64_t
         load_collider(&c, idx[k], SET_PASS);
         v3 r = support(&c, mk(dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2]));
         out[3 * k] = r.x; out[3 * k + 1] = r.y; out[3 * k + 2] = r.z;
+    }
+}
+
+/* MPR for pairs (i1[k], i2[k]): hit[k], depth[k], dir[k][3], pos[k][3],
+ * status[k] (mpr.py:21-110) */
+void orc_mpr(SET_ARGS, const int32_t* i1, const int32_t* i2, int64_t n, double tol, int max_iter, int limit,
+             int penetration, int8_t* hit, double* depth, double* dir, double* pos, int8_t* status, int nthreads) {
+    set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t k = 0; k < n; ++k) {
+        collider a, b;
+        load_collider(&a, i1[k], SET_PASS);
+        load_collider(&b, i2[k], SET_PASS);
+        mpr_result r;
+        mpr(&a, &b, tol, max_iter, limit, penetration, &r);
+        hit[k] = (int8_t)r.hit;
+        status[k] = (int8_t)r.status;
+        depth[k] = r.depth;
+        dir[3 * k] = r.dir.x; dir[3 * k + 1] = r.dir.y; dir[3 * k + 2] = r.dir.z;
+        pos[3 * k] = r.pos.x; pos[3 * k + 1] = r.pos.y; pos[3 * k + 2] = r.pos.z;
     }
 }

@@ -42,6 +42,9 @@ def lib():
         _lib.orc_self_pairs_sweep.argtypes = [DP, ctypes.c_int64, I32P, ctypes.c_int64]
         _lib.orc_self_pairs_sweep.restype = ctypes.c_int64
         _lib.orc_support_batch.argtypes = _set_args + [I32P, DP, ctypes.c_int64, DP, ctypes.c_int]
+        _lib.orc_mpr.argtypes = _set_args + [
+            I32P, I32P, ctypes.c_int64, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+            I8P, DP, DP, DP, I8P, ctypes.c_int]
         _lib.orc_max_threads.restype = ctypes.c_int
         _lib.orc_box_vertices.argtypes = [DP, DP, DP]
     return _lib
@@ -105,6 +108,20 @@ def epa(cs, i1, i2, simplices, max_iter=64, max_loose_edges=32, max_faces=64, ep
     out = dict(mtv=mtv, status=status, n_faces=nf)
     if want_faces:
         out["faces"] = faces
+    return out
+
+
+def mpr(cs, i1, i2, tolerance=0.0001, max_iterations=100, refine_limit=10000, penetration=True, nthreads=0):
+    """MPR (mpr.py:21-110): hit, depth, dir, pos (NaN where the reference
+    returns None), status."""
+    i1, i2 = _idx(i1), _idx(i2)
+    n = len(i1)
+    out = dict(hit=np.empty(n, np.int8), depth=np.empty(n), dir=np.empty((n, 3)), pos=np.empty((n, 3)),
+               status=np.empty(n, np.int8))
+    lib().orc_mpr(*_set(cs), _p(i1, I32P), _p(i2, I32P), n, tolerance, max_iterations, refine_limit,
+                  1 if penetration else 0, _p(out["hit"], I8P), _p(out["depth"], DP), _p(out["dir"], DP),
+                  _p(out["pos"], DP), _p(out["status"], I8P), nthreads)
+    out["hit"] = out["hit"].astype(bool)
     return out
 
 

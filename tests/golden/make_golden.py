@@ -29,6 +29,9 @@ Inputs come from ``distance3d_gb300.workloads`` (seeded).  Outputs:
   directions (three random, +/- its local z axis, zero).
 * ``epa_all9.npz``    -- reference ``epa.epa`` on the intersecting pairs of
   gjk_all9, as epa_mixed6.
+* ``mpr_all9.npz``    -- reference ``mpr.mpr_penetration`` (flag, depth,
+  direction, contact position; NaN for None) and ``mpr.mpr_intersection`` on
+  every gjk_all9 pair, at the default tolerance and iteration limit.
 * ``aabb_tree.npz``   -- a 400-collider scene: reference AabbTree self overlap
   (both orders, i == j dropped, reduced to i < j), brute force
   ``all_aabbs_overlap``, BoundingVolumeHierarchy.aabb_overlapping_with_self on
@@ -53,6 +56,11 @@ def import_reference(ref_root):
     import distance3d  # noqa: F401
     from distance3d import gjk, epa, colliders, aabb_tree, broad_phase
     return gjk, epa, colliders, aabb_tree, broad_phase
+
+
+def import_mpr():
+    from distance3d import mpr
+    return mpr
 
 
 def make_ref_colliders(colliders, cs):
@@ -200,6 +208,26 @@ def epa_fixture(mods, cols, gf):
     return out
 
 
+def mpr_fixture(cols, gf):
+    mpr = import_mpr()
+    n = len(gf["i1"])
+    hit = np.zeros(n, bool)
+    hit_i = np.zeros(n, bool)
+    depth = np.full(n, np.nan)
+    pdir = np.full((n, 3), np.nan)
+    pos = np.full((n, 3), np.nan)
+    t0 = time.time()
+    for k in range(n):
+        c1, c2 = cols[gf["i1"][k]], cols[gf["i2"][k]]
+        h, d, p, c = mpr.mpr_penetration(c1, c2)
+        hit[k] = h
+        if d is not None:
+            depth[k], pdir[k], pos[k] = d, p, c
+        hit_i[k] = mpr.mpr_intersection(c1, c2)
+    print(f"  mpr: {n} pairs in {time.time() - t0:.1f}s, {hit.sum()} intersecting")
+    return dict(i1=gf["i1"], i2=gf["i2"], hit=hit, depth=depth, dir=pdir, pos=pos, hit_intersection=hit_i)
+
+
 class _FakeTM:
     def __init__(self):
         self.T = {}
@@ -270,6 +298,7 @@ def make_all9(mods, workloads):
     print(f"  intersecting fraction {np.mean(gf['dist'] == 0.0):.3f}")
     np.savez_compressed(os.path.join(HERE, "gjk_all9.npz"), **gf)
     np.savez_compressed(os.path.join(HERE, "epa_all9.npz"), **epa_fixture(mods, cols, gf))
+    np.savez_compressed(os.path.join(HERE, "mpr_all9.npz"), **mpr_fixture(cols, gf))
 
 
 def make_tree(mods, workloads):

@@ -247,3 +247,57 @@ def test_gjk_distance_with_margin(backend):
     sphere = colliders.Sphere(np.array([2.0, 0.0, 0.0]), 0.5)
     r = distance_batch(backend, [(box, sphere), (colliders.Margin(box, 0.1), sphere)])
     assert approx(r["dist"][0]) == r["dist"][1] + 0.1
+
+
+def mpr_batch(backend, pairs, **kw):
+    cols = [c for p in pairs for c in p]
+    cs = ColliderSet.from_colliders(cols)
+    i1 = np.arange(0, 2 * len(pairs), 2, dtype=np.int32)
+    i2 = i1 + 1
+    if backend == "oracle":
+        from oracle import oracle
+        return oracle.mpr(cs, i1, i2, **kw)
+    from distance3d_gb300.mpr import mpr_batch as run
+    from distance3d_gb300.store import ColliderStore
+    r = run(ColliderStore(cs), i1, i2, **kw)
+    return {k: v.cpu().numpy() for k, v in r.items()}
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_mpr_intersection_vs_gjk(backend):
+    """test_mpr.py:7-20 (RandomState(24)): MPR and GJK agree on intersection."""
+    rs = np.random.RandomState(24)
+    pairs = [(hull(rs.rand(6, 3) * np.array([[2, 2, 2]])), hull(rs.rand(6, 3) * np.array([[1, 1, 1]])))
+             for _ in range(50)]
+    g = distance_batch(backend, pairs)
+    m = mpr_batch(backend, pairs, penetration=False)
+    assert np.array_equal(g["dist"] < 1e-16, m["hit"].astype(bool))
+
+
+@pytest.mark.parametrize("backend", BACKENDS)
+def test_mpr_penetration_points_segments_spheres(backend):
+    """test_mpr.py:23-93: points, segments and spheres."""
+    p0, p1 = hull([[0.0, 0.0, 0.0]]), hull([[1.0, 0.0, 0.0]])
+    s1 = hull([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
+    o = colliders.Sphere(np.zeros(3), 1.0)
+    pairs = [(p0, p0), (s1, s1), (s1, p0), (s1, p1), (o, colliders.Sphere(np.zeros(3), 1.0)),
+             (o, colliders.Sphere(np.array([0.0, 0.0, 1.0]), 0.5)),
+             (o, colliders.Sphere(np.array([1.0, 0.0, 0.0]), 0.5))]
+    r = mpr_batch(backend, pairs)
+    assert np.all(r["hit"])
+    depth = [0.0, 1.0, 0.0, 0.0]
+    dirs = [np.zeros(3), [-1, 0, 0], np.zeros(3), np.zeros(3)]
+    pos = [np.zeros(3), [0.5, 0, 0], np.zeros(3), [1, 0, 0]]
+    for k in range(4):
+        assert approx(r["depth"][k]) == depth[k]
+        assert_array_almost_equal(r["dir"][k], dirs[k])
+        assert_array_almost_equal(r["pos"][k], pos[k])
+    assert r["depth"][4] == 2.0
+    assert approx(np.linalg.norm(r["dir"][4])) == 1.0
+    assert_array_almost_equal(r["pos"][4], [0, 0, 0])
+    assert r["depth"][5] == 0.5
+    assert_array_almost_equal(r["dir"][5], [0, 0, 1])
+    assert_array_almost_equal(r["pos"][5], [0, 0, 0.75])
+    assert r["depth"][6] == 0.5
+    assert_array_almost_equal(r["dir"][6], [1, 0, 0])
+    assert_array_almost_equal(r["pos"][6], [0.75, 0, 0])

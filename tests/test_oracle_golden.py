@@ -75,3 +75,18 @@ def test_queries_match_tree(golden):
         want = t["query_idx"][t["query_ptr"][q]:t["query_ptr"][q + 1]]
         got = oracle.cross_pairs(t["queries"][q:q + 1], t["aabbs"])[:, 1]
         assert np.array_equal(np.sort(got), want)
+
+
+def test_mpr_bit_exact(golden):
+    """mpr_penetration and mpr_intersection on the nine-type pairs."""
+    g, cs = golden("gjk_all9")
+    m, _ = golden("mpr_all9")
+    r = oracle.mpr(cs, m["i1"], m["i2"])
+    assert np.all(r["status"] == 0)
+    assert np.array_equal(r["hit"], m["hit"])
+    assert m["hit"].sum() > 200
+    assert np.array_equal(r["depth"], m["depth"], equal_nan=True)
+    assert np.array_equal(r["dir"], m["dir"], equal_nan=True)
+    assert np.array_equal(r["pos"], m["pos"], equal_nan=True)
+    ri = oracle.mpr(cs, m["i1"], m["i2"], penetration=False)
+    assert np.array_equal(ri["hit"], m["hit_intersection"])

@@ -1,16 +1,22 @@
 // mpr.cu -- Minkowski portal refinement (MPR), the plain FP64 drop-in for
-// distance3d's mpr_intersection and mpr_penetration (mpr.py:21-110), one
-// thread per pair.  Compiled with -fmad=false: every step is the reference's
+// distance3d's mpr_intersection and mpr_penetration (mpr.py:21-110).
+// Compiled with -fmad=false: every step is the reference's
 // rounding sequence (NumPy orders as in d3d_device.cuh), so flags, depths,
 // directions and contact positions are the reference's bit for bit.
 //
-// The portal (four Minkowski-difference vertices and the two colliders'
-// support points behind each) lives in shared memory, one column per lane
-// (stride BLOCK), because the reference replaces its rows by data-dependent
-// index.  The refinement loop of the reference has no bound; here it stops
-// after `refine_limit` expansions with status D3D_STATUS_MAX_ITER.
+// Each lane of the persistent kernel runs one pair as a state machine with
+// one support evaluation per round (portal discovery, refinement,
+// penetration search), and takes the next pair of the type-sorted order when
+// its pair ends.  The portal (four Minkowski-difference vertices and the two
+// colliders' support points behind each) lives in shared memory, one column
+// per lane (stride kBlock), because the reference replaces its rows by
+// data-dependent index.  The refinement loop of the reference has no bound;
+// here it stops after `refine_limit` expansions with status
+// D3D_STATUS_MAX_ITER.
 #include "capi_util.h"
 #include "jolt.cuh"
+#include "persist.cuh"
+#include "scratch.h"
 
 namespace {
 
@@ -80,61 +86,6 @@ __device__ __forceinline__ void supports(const d3d_store& st, int i, int j, d3 d
     pair_supports<double, ExactSupport>(st, i, j, d, pa, pb);
 }
 
-enum { kContinue = -2, kOutside = -1, kBuilt = 0, kOnV1 = 1, kOnSegment = 2 };
-
-// mpr.py:123-158 _discover_portal with :161-240
-__device__ int discover(const d3d_store& st, int i, int j, int max_iter, const Portal& P) {
-    // :161-174 origin ray from the centers
-    const d3 c1 = collider_center(st, i), c2 = collider_center(st, j);
-    d3 v0 = c1 - c2;
-    if (all_zero(v0)) v0.x += kEps * 10.0;
-    P.set3(0, v0, c1, c2);
-    // :177-185
-    d3 d = norm_vector(-v0);
-    d3 pa, pb;
-    supports(st, i, j, d, pa, pb);
-    P.set(1, pa, pb);
-    const d3 v1 = P.v(1);
-    if (!all_zero(v1) && dot(v1, d) < kEps) return kOutside;
-    // :188-201
-    d = cross(v0, v1);
-    if (dot(d, d) < kEps) return all_zero(v1) ? kOnV1 : kOnSegment;
-    d = norm_vector(d);
-    supports(st, i, j, d, pa, pb);
-    P.set(2, pa, pb);
-    if (dot(P.v(2), d) < kEps) return kOutside;
-    // :204-210; the reference's row swap (:232-240) keeps row 1 as a NumPy
-    // view, so it ends with both rows holding the old row 2
-    d = norm_vector(cross(P.v(1) - v0, P.v(2) - v0));
-    if (dot(d, v0) > 0.0) {
-        P.copy(1, 2);
-        d = d * -1.0;
-    }
-    int n_points = 3, it = 0;
-    while (n_points < 4) {
-        supports(st, i, j, d, pa, pb);
-        P.set(3, pa, pb);
-        const d3 v3 = P.v(3);
-        if (dot(v3, d) < kEps) return kOutside;
-        // :213-229 _iterate_discover_portal
-        bool cont = false;
-        if (dot(cross(P.v(1), v3), v0) < kEps) {
-            P.copy(2, 3);
-            cont = true;
-        }
-        if (!cont && dot(cross(v3, P.v(2)), v0) < kEps) {
-            P.copy(1, 3);
-            cont = true;
-        }
-        if (cont)
-            d = norm_vector(cross(P.v(1) - v0, P.v(2) - v0));
-        else
-            n_points = 4;
-        if (++it >= max_iter) break;
-    }
-    return kBuilt;
-}
-
 // :276-281
 __device__ __forceinline__ d3 portal_direction(const Portal& P) {
     const d3 v1 = P.v(1);
@@ -163,23 +114,6 @@ __device__ __forceinline__ void expand(const Portal& P, d3 pa, d3 pb) {
     else
         r = dot(P.v(3), c) > 0.0 ? 2 : 1;
     P.set3(r, v4, pa, pb);
-}
-
-// :243-273 _refine_portal, bounded
-__device__ bool refine(const d3d_store& st, int i, int j, const Portal& P, double tol, int limit, int& status) {
-    for (int it = 0;; ++it) {
-        const d3 d = portal_direction(P);
-        if (dot(P.v(1), d) > -10.0 * kEps) return true;
-        d3 pa, pb;
-        supports(st, i, j, d, pa, pb);
-        const d3 v4 = pa - pb;
-        if (!(dot(v4, d) > -10.0 * kEps) || reach_tolerance(P, v4, d, tol)) return false;
-        if (it >= limit) {
-            status = D3D_STATUS_MAX_ITER;
-            return false;
-        }
-        expand(P, pa, pb);
-    }
 }
 
 // distance/_triangle.py:12-89 point_to_triangle for the origin
@@ -268,60 +202,173 @@ __device__ __forceinline__ void put3(double* p, int64_t k, d3 x) {
     p[3 * k + 2] = x.z;
 }
 
-// :21-110 mpr_intersection / mpr_penetration for pairs k = thread, stride grid
+// The phases of one pair, each ending in one support evaluation.
+enum Phase { kV1 = 0, kV2, kDiscover, kRefine, kPenetrate };
+
+// One lane's pair between rounds.
+struct Lane {
+    d3 d;         // direction of the next support evaluation
+    int phase;
+    int it;
+};
+
+// Enter the refinement (:243-273) with the portal built: returns 1 if the
+// portal already encloses the origin, else prepares the first refinement
+// support.
+__device__ __forceinline__ int enter_refine(const Portal& P, Lane& L) {
+    L.d = portal_direction(P);
+    if (dot(P.v(1), L.d) > -10.0 * kEps) return 1;
+    L.phase = kRefine;
+    L.it = 0;
+    return 0;
+}
+
+// Outcome of a round: still running, or finished with (hit, status) and the
+// penetration fields set.
+enum { kRunning = -1, kMiss = 0, kHit = 1 };
+
+// Process the support points (pa, pb) along L.d for the lane's phase
+// (mpr.py:123-158 with :161-240, :243-273, :320-334); returns kRunning or the
+// outcome.  On a penetrating hit with `pen`, depth / dir / pos are set.
+__device__ int mpr_round(const Portal& P, Lane& L, d3 pa, d3 pb, const d3d_mpr_options& opt, int& status,
+                         double& depth, d3& dir, d3& pos) {
+    const d3 v0 = P.v(0);
+    switch (L.phase) {
+    case kV1: {  // :177-201
+        P.set(1, pa, pb);
+        const d3 v1 = P.v(1);
+        if (!all_zero(v1) && dot(v1, L.d) < kEps) return kMiss;
+        d3 d = cross(v0, v1);
+        if (dot(d, d) < kEps) {  // :337-352
+            if (opt.penetration) {
+                pos = (P.a(1) + P.b(1)) * 0.5;
+                if (all_zero(v1)) {
+                    depth = 0.0;
+                    dir = mk(0.0, 0.0, 0.0);
+                } else {
+                    depth = sqrt(dot(v1, v1));
+                    dir = norm_vector(v1);
+                }
+            }
+            return kHit;
+        }
+        L.d = norm_vector(d);
+        L.phase = kV2;
+        return kRunning;
+    }
+    case kV2: {  // :198-210; the reference's row swap (:232-240) keeps row 1
+                 // as a NumPy view, so both rows end up holding the old row 2
+        P.set(2, pa, pb);
+        if (dot(P.v(2), L.d) < kEps) return kMiss;
+        L.d = norm_vector(cross(P.v(1) - v0, P.v(2) - v0));
+        if (dot(L.d, v0) > 0.0) {
+            P.copy(1, 2);
+            L.d = L.d * -1.0;
+        }
+        L.phase = kDiscover;
+        L.it = 0;
+        return kRunning;
+    }
+    case kDiscover: {  // :145-158, :213-229
+        P.set(3, pa, pb);
+        const d3 v3 = P.v(3);
+        if (dot(v3, L.d) < kEps) return kMiss;
+        bool cont = false;
+        if (dot(cross(P.v(1), v3), v0) < kEps) {
+            P.copy(2, 3);
+            cont = true;
+        }
+        if (!cont && dot(cross(v3, P.v(2)), v0) < kEps) {
+            P.copy(1, 3);
+            cont = true;
+        }
+        if (cont) L.d = norm_vector(cross(P.v(1) - v0, P.v(2) - v0));
+        if (cont && ++L.it < opt.max_iterations) return kRunning;
+        if (!enter_refine(P, L)) return kRunning;
+        break;  // the built portal encloses the origin
+    }
+    case kRefine: {  // :243-273, bounded
+        const d3 v4 = pa - pb;
+        if (!(dot(v4, L.d) > -10.0 * kEps) || reach_tolerance(P, v4, L.d, opt.tolerance)) return kMiss;
+        if (L.it >= opt.refine_limit) {
+            status = D3D_STATUS_MAX_ITER;
+            return kMiss;
+        }
+        expand(P, pa, pb);
+        ++L.it;
+        L.d = portal_direction(P);
+        if (!(dot(P.v(1), L.d) > -10.0 * kEps)) return kRunning;
+        break;  // the origin is inside
+    }
+    default: {  // kPenetrate, :320-334 and :355-362
+        if (reach_tolerance(P, pa - pb, L.d, opt.tolerance) || L.it > opt.max_iterations) {
+            d3 cp;
+            depth = origin_to_triangle(P.v(1), P.v(2), P.v(3), cp);
+            if (fabs(depth) < kEps) cp = mk(0.0, 0.0, 0.0);
+            pos = contact_position(P, L.d);
+            dir = norm_vector(cp);
+            return kHit;
+        }
+        expand(P, pa, pb);
+        ++L.it;
+        L.d = portal_direction(P);
+        return kRunning;
+    }
+    }
+    // the portal encloses the origin
+    if (!opt.penetration) return kHit;
+    L.phase = kPenetrate;
+    L.it = 0;
+    L.d = portal_direction(P);
+    return kRunning;
+}
+
+// Persistent MPR: each lane runs one pair's MPR one support evaluation per
+// round and fetches the next pair (in the type-sorted `order`) when its pair
+// ends, so the support code runs once per round for the whole warp.
 __global__ void __launch_bounds__(kBlock) k_mpr(d3d_store st, const int32_t* __restrict__ i1,
-                                                const int32_t* __restrict__ i2, int64_t n, d3d_mpr_options opt,
-                                                MprOut o) {
+                                                const int32_t* __restrict__ i2, const int32_t* __restrict__ order,
+                                                int64_t n, unsigned long long* __restrict__ cursor,
+                                                d3d_mpr_options opt, MprOut o) {
     __shared__ double rows[36 * kBlock];
     const Portal P{rows + threadIdx.x};
     const d3 nan3 = mk(double(NAN), double(NAN), double(NAN));
-    for (int64_t k = (int64_t)blockIdx.x * kBlock + threadIdx.x; k < n; k += (int64_t)gridDim.x * kBlock) {
-        const int i = i1[k], j = i2[k];
+    Lane L;
+    int64_t pid = 0;
+    int i = 0, j = 0;
+    bool need = true;
+    while (true) {
+        const long long slot = fetch_slot(cursor, need);
+        if (need) {
+            if (slot >= n) break;
+            pid = order ? order[slot] : slot;
+            i = i1[pid];
+            j = i2[pid];
+            // :161-185: origin ray from the centers, first direction
+            const d3 c1 = collider_center(st, i), c2 = collider_center(st, j);
+            d3 v0 = c1 - c2;
+            if (all_zero(v0)) v0.x += kEps * 10.0;
+            P.set3(0, v0, c1, c2);
+            L.d = norm_vector(-v0);
+            L.phase = kV1;
+            L.it = 0;
+            need = false;
+        }
+        d3 pa, pb;
+        supports(st, i, j, L.d, pa, pb);
         int status = D3D_STATUS_OK;
-        bool hit;
         double depth = NAN;
         d3 dir = nan3, pos = nan3;
-        const int res = discover(st, i, j, opt.max_iterations, P);
-        if (res == kOutside) {
-            hit = false;
-        } else if (res == kOnV1 || res == kOnSegment) {
-            hit = true;
-            pos = (P.a(1) + P.b(1)) * 0.5;  // :337-352
-            if (res == kOnV1) {
-                depth = 0.0;
-                dir = mk(0.0, 0.0, 0.0);
-            } else {
-                const d3 v1 = P.v(1);
-                depth = sqrt(dot(v1, v1));
-                dir = norm_vector(v1);
+        const int r = mpr_round(P, L, pa, pb, opt, status, depth, dir, pos);
+        if (r != kRunning) {
+            o.hit[pid] = (int8_t)r;
+            o.status[pid] = (int8_t)status;
+            if (opt.penetration) {
+                if (o.depth) o.depth[pid] = depth;
+                put3(o.dir, pid, dir);
+                put3(o.pos, pid, pos);
             }
-        } else {
-            hit = refine(st, i, j, P, opt.tolerance, opt.refine_limit, status);
-            if (hit && opt.penetration) {
-                // :320-334 _find_penetration_info, :355-362 _penetration_info
-                for (int it = 0;; ++it) {
-                    const d3 d = portal_direction(P);
-                    d3 pa, pb;
-                    supports(st, i, j, d, pa, pb);
-                    if (reach_tolerance(P, pa - pb, d, opt.tolerance) || it > opt.max_iterations) {
-                        d3 cp;
-                        depth = origin_to_triangle(P.v(1), P.v(2), P.v(3), cp);
-                        if (fabs(depth) < kEps) cp = mk(0.0, 0.0, 0.0);
-                        pos = contact_position(P, portal_direction(P));
-                        dir = norm_vector(cp);
-                        break;
-                    }
-                    expand(P, pa, pb);
-                }
-            }
-        }
-        o.hit[k] = hit ? 1 : 0;
-        o.status[k] = (int8_t)status;
-        if (opt.penetration) {
-            if (!hit) depth = NAN, dir = pos = nan3;
-            if (o.depth) o.depth[k] = depth;
-            put3(o.dir, k, dir);
-            put3(o.pos, k, pos);
+            need = true;
         }
     }
 }
@@ -339,13 +386,31 @@ extern "C" int d3d_mpr(const d3d_store* store, const int32_t* i1, const int32_t*
     D3D_REQUIRE(opt->tolerance >= 0.0, "d3d_mpr: negative tolerance");
     if (n == 0) return D3D_SUCCESS;
     D3D_REQUIRE(i1 && i2 && hit && status, "d3d_mpr: null pointer");
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t need = (n + kBlock - 1) / kBlock;
-    const int64_t cap = (int64_t)(sms > 0 ? sms : 1) * 8;
-    const unsigned grid = (unsigned)(need < cap ? need : cap);
-    MprOut o{hit, depth, dir, pos, status};
-    k_mpr<<<grid, kBlock, 0, d3d::as_stream(stream)>>>(*store, i1, i2, n, *opt, o);
-    return d3d::check_launch("d3d_mpr");
+    D3D_REQUIRE(n <= INT32_MAX, "d3d_mpr: more than 2^31 pairs");
+    cudaStream_t st = d3d::as_stream(stream);
+    const bool sched = n >= d3d::tuning().sort_min;
+    const size_t order_bytes = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
+    const size_t bytes = 256 + (sched ? order_bytes + d3d::pair_order_temp_bytes(n) : 0);
+    void* scratch = nullptr;
+    rc = d3d::scratch_alloc(&scratch, bytes, st);
+    if (rc) return rc;
+    unsigned long long* cursor = static_cast<unsigned long long*>(scratch);
+    int32_t* order = sched ? reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + 256) : nullptr;
+    cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) {
+        d3d::scratch_free(scratch, st);
+        d3d::set_error("d3d_mpr: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    if (sched)
+        rc = d3d::pair_order(*store, i1, i2, n, order, static_cast<char*>(scratch) + 256 + order_bytes,
+                             d3d::pair_order_temp_bytes(n), st);
+    if (!rc) {
+        MprOut o{hit, depth, dir, pos, status};
+        const int blocks = d3d::persistent_blocks((const void*)k_mpr, kBlock, n);
+        k_mpr<<<blocks, kBlock, 0, st>>>(*store, i1, i2, order, n, cursor, *opt, o);
+        rc = d3d::check_launch("d3d_mpr");
+    }
+    d3d::scratch_free(scratch, st);
+    return rc;
 }

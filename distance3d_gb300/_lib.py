@@ -22,7 +22,8 @@ PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 class D3DStore(ctypes.Structure):
     _fields_ = [("n_colliders", c_int64), ("n_vertices", c_int64), ("rec64", c_void_p),
-                ("rec32", c_void_p), ("meta", c_void_p), ("verts64", c_void_p), ("verts32", c_void_p)]
+                ("rec32", c_void_p), ("meta", c_void_p), ("verts64", c_void_p), ("verts32", c_void_p),
+                ("links", c_void_p), ("n_links", c_int64)]
 
 
 class GjkOptions(ctypes.Structure):

@@ -2,8 +2,8 @@
 
 Mirrors distance3d colliders.py:17-647 for the types on the GPU path:
 ``ConvexHullVertices``, ``Box``, ``Sphere``, ``Capsule``, ``Ellipsoid``,
-``Cylinder``, ``Disk``, ``Ellipse``, ``Cone`` and the ``Margin`` wrapper
-(``MeshGraph`` is not on the path).  Attributes carry the reference's names
+``Cylinder``, ``Disk``, ``Ellipse``, ``Cone``, ``MeshGraph`` and the
+``Margin`` wrapper.  Attributes carry the reference's names
 (``c``/``radius``, ``capsule2origin``/``radius``/``height``,
 ``box2origin``/``size``, ...), so
 ``ColliderSet.from_colliders`` packs these and the reference's own objects
@@ -301,6 +301,34 @@ class Cone(ConvexCollider):
         return self.cone2origin
 
 
+class MeshGraph(ConvexCollider):
+    """Convex mesh with hill-climbing support (colliders.py:187-240):
+    ``vertices`` (n,3) in the mesh frame, ``triangles`` (m,3) vertex
+    indices.  Every support call climbs from the mesh's start vertex
+    (the smallest index in ``triangles``); the reference starts from its
+    previous answer, which gives the same vertex unless the climb can stop
+    within 10 EPSILON of the maximum."""
+
+    def __init__(self, mesh2origin, vertices, triangles, artist=None):
+        super().__init__(artist)
+        self.mesh2origin = mesh2origin
+        self.vertices = vertices
+        self.triangles = triangles
+
+    def first_vertex(self):
+        return self.mesh2origin[:3, 3] + np.dot(self.mesh2origin[:3, :3], self.vertices[0])
+
+    def center(self):
+        return self.mesh2origin[:3, 3] + np.dot(self.mesh2origin[:3, :3], np.mean(self.vertices, axis=0))
+
+    def update_pose(self, mesh2origin):
+        self.mesh2origin = mesh2origin
+        self._invalidate()
+
+    def collider2origin(self):
+        return self.mesh2origin
+
+
 class Margin(ConvexCollider):
     """Margin around another collider (colliders.py:606-647): its support
     point moved by ``margin`` along the unit search direction, its box grown
@@ -335,4 +363,5 @@ COLLIDERS = {
     "disk": Disk,
     "ellipse": Ellipse,
     "cone": Cone,
+    "mesh": MeshGraph,
 }

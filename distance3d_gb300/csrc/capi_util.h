@@ -27,12 +27,13 @@ inline int check_launch(const char* what) {
 
 inline int check_store(const d3d_store* s, const char* what) {
     if (!s || !s->rec64 || !s->rec32 || !s->meta || s->n_colliders < 0 || s->n_vertices < 0 ||
-        (s->n_vertices > 0 && (!s->verts64 || !s->verts32))) {
+        (s->n_vertices > 0 && (!s->verts64 || !s->verts32)) || s->n_links < 0 || (s->n_links > 0 && !s->links)) {
         set_error("%s: invalid d3d_store", what);
         return D3D_ERR_INVALID;
     }
-    if (s->n_colliders >= (int64_t(1) << 31) || s->n_vertices >= (int64_t(1) << 31)) {
-        set_error("%s: store larger than 2^31 colliders or vertices", what);
+    if (s->n_colliders >= (int64_t(1) << 31) || s->n_vertices >= (int64_t(1) << 31) ||
+        s->n_links >= (int64_t(1) << 31)) {
+        set_error("%s: store larger than 2^31 colliders, vertices or links", what);
         return D3D_ERR_INVALID;
     }
     return D3D_SUCCESS;

@@ -1,6 +1,6 @@
 // d3d_device.cuh -- device-side building blocks shared by the kernels of
 // libd3d_gb300: vector arithmetic with the reference's rounding sequence,
-// collider loads from the store, and the support functions of the nine
+// collider loads from the store, and the support functions of the ten
 // collider types and of the Margin wrapper.
 //
 // Rounding.  The reference computes its small dot products through NumPy,
@@ -217,12 +217,66 @@ __device__ __forceinline__ bool cone_rim(const Col<T>& c, V3<T> l, V3<T>& q) {
     return dot(l, q) >= l.z * c.p[1];
 }
 
+__device__ __forceinline__ const double* store_verts(const d3d_store& s, double) { return s.verts64; }
+__device__ __forceinline__ const float* store_verts(const d3d_store& s, float) { return s.verts32; }
+
+// mesh.py:12-127 hill_climb_mesh_extreme for the mesh-frame direction l:
+// from the start vertex, the six shortcut vertices, then passes over the
+// neighbours of the vertex a pass starts at (the reference iterates that
+// vertex's list even after it has moved), moving whenever the projection of
+// the step exceeds 10 EPSILON (PROJECTION_LENGTH_EPSILON).  The climb
+// strictly increases the projection, so it ends within nv passes; the bound
+// is a guard.  Out-of-range links are skipped.
+// The links offset and the start vertex are read from the FP64 record (exact
+// integers there; the FP32 record cannot hold large offsets).
+template <typename T>
+__device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, V3<T> l) {
+    const T* verts = store_verts(st, T(0));
+    const int nv = c.nv;
+    const double* rec = st.rec64 + (size_t)c.idx * 16;
+    const int32_t* blk = st.links + (int64_t)__ldg(rec + 12);
+    const T eps = T(10.0 * DBL_EPSILON);
+    int best = (int)__ldg(rec + 13);
+    if (best < 0 || best >= nv) best = 0;
+    V3<T> vb = load_vertex(verts, c.off + best);
+    for (int k = 0; k < 6; ++k) {
+        const int cand = __ldg(blk + k);
+        if (cand < 0 || cand >= nv) continue;
+        const V3<T> v = load_vertex(verts, c.off + cand);
+        const V3<T> diff = v - vb;
+        if (dot(l, diff) > eps) {
+            best = cand;
+            vb = v;
+        }
+    }
+    for (int pass = 0; pass <= nv; ++pass) {
+        bool converged = true;
+        const int lo = __ldg(blk + 6 + best), hi = __ldg(blk + 7 + best);
+        for (int e = lo; e < hi; ++e) {
+            const int cand = __ldg(blk + e);
+            if (cand < 0 || cand >= nv) continue;
+            const V3<T> v = load_vertex(verts, c.off + cand);
+            const V3<T> diff = v - vb;
+            if (dot(l, diff) > eps) {
+                best = cand;
+                vb = v;
+                converged = false;
+            }
+        }
+        if (converged) break;
+    }
+    return best;
+}
+
 // Support point of the collider itself (without its margin) along d.  Sphere
 // geometry.py:314-346, capsule :209-256, cylinder :160-206, ellipsoid
 // :259-284 (norm_vector utils.py:12-30), disk :353-387, ellipse :390-418,
-// cone :421-455; box and hull: first-maximum vertex (colliders.py:131-132).
+// cone :421-455; box and hull: first-maximum vertex (colliders.py:131-132);
+// mesh: hill climb from the mesh's start vertex (mesh.py:77-85; each call
+// starts there, where the reference starts from its previous answer).
 template <typename T>
-__device__ __forceinline__ V3<T> base_support(const Col<T>& c, const T* verts, V3<T> d) {
+__device__ __forceinline__ V3<T> base_support(const Col<T>& c, const d3d_store& st, V3<T> d) {
+    const T* verts = store_verts(st, T(0));
     switch (c.type) {
     case D3D_SPHERE: {
         T n = sqrt_t(dot(d, d));
@@ -301,6 +355,11 @@ __device__ __forceinline__ V3<T> base_support(const Col<T>& c, const T* verts, V
         if (!cone_rim(c, l, q)) q = mk(T(0), T(0), c.p[1]);
         return xform(c.R, c.t, q);
     }
+    case D3D_MESH: {
+        if (c.nv < 1) return mk(T(NAN), T(NAN), T(NAN));  // rejected by d3d_store_pack
+        const int k = mesh_climb(c, st, rt_mul(c.R, d));
+        return xform(c.R, c.t, load_vertex(verts, c.off + k));
+    }
     default:
         if (c.nv < 1) return mk(T(NAN), T(NAN), T(NAN));  // rejected by d3d_store_pack
         return load_vertex(verts, c.off + hull_argmax(verts, c.off, c.nv, d));
@@ -318,8 +377,8 @@ __device__ __forceinline__ V3<T> add_margin(const Col<T>& c, V3<T> s, V3<T> d) {
 }
 
 template <typename T>
-__device__ __forceinline__ V3<T> support(const Col<T>& c, const T* verts, V3<T> d) {
-    return add_margin(c, base_support(c, verts, d), d);
+__device__ __forceinline__ V3<T> support(const Col<T>& c, const d3d_store& st, V3<T> d) {
+    return add_margin(c, base_support(c, st, d), d);
 }
 
 }  // namespace d3d

@@ -83,8 +83,8 @@ __device__ __forceinline__ void epa_begin(EpaLoop& L, const double* simplex, dou
 // One iteration of epa.py:59-74.  Returns -1 while running, else the status
 // (mtv written).
 __device__ __forceinline__ int epa_step(EpaLoop& L, const Col<double>& c1, const Col<double>& c2,
-                                        const double* verts, const d3d_epa_options& o, double* F, double* E,
-                                        d3& mtv) {
+                                        const d3d_store& store, const d3d_epa_options& o, double* F,
+                                        double* E, d3& mtv) {
     const double eps = o.epsilon;
     if (L.it >= o.max_iterations) {
         // epa.py:77: closest_face is a view, read after the last iteration's edits
@@ -112,7 +112,7 @@ __device__ __forceinline__ int epa_step(EpaLoop& L, const Col<double>& c1, const
     }
     L.closest = closest;
     d3 sd = ld(F + 12 * closest + 9);
-    d3 np_ = support(c1, verts, sd) - support(c2, verts, -sd);
+    d3 np_ = support(c1, store, sd) - support(c2, store, -sd);
     double pd = dot(np_, sd);
     if (pd - md < eps) {  // epa.py:67-70
         mtv = sd * pd;
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __re
         load_col(s, a, c1);
         load_col(s, b, c2);
         d3 m;
-        const int stt = epa_step(L, c1, c2, s.verts64, o, F, E, m);
+        const int stt = epa_step(L, c1, c2, s, o, F, E, m);
         if (stt >= 0) {
             mtv[3 * pid] = m.x;
             mtv[3 * pid + 1] = m.y;

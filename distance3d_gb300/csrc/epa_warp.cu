@@ -200,7 +200,7 @@ __device__ __forceinline__ d3 minkowski64_exact(const d3d_store& st, int a, int 
         else
             s = add_margin(c, load_vertex(st.verts64, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts64, c.off, c.nv, dd, half_mask()))), dd);
     } else {
-        s = support(c, st.verts64, dd);
+        s = support(c, st, dd);
     }
     const d3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
     return up ? o - s : s - o;

@@ -101,6 +101,10 @@ struct FastSupport {
             const f3 ctr = mk(c.t[0], c.t[1], c.t[2]);
             return n2 == 0.f ? ctr + mk(0.f, 0.f, c.p[0]) : ctr + d * (c.p[0] * rsqrtf(n2));
         }
+        if (c.type == D3D_MESH) {
+            if (c.nv < 1) return mk(NAN, NAN, NAN);
+            return xform(c.R, c.t, load_vertex(s.verts32, c.off + mesh_climb(c, s, rt_mul(c.R, d))));
+        }
         const bool up = upper_feature(c.type, c.R, c.p[0], c.p[1], d);
         return xform(c.R, c.t, local_point(c, rt_mul(c.R, d), up));
     }
@@ -125,6 +129,16 @@ struct RefineSupport {
             const double n2 = dot(d, d);
             const d3 ctr = mk(c.t[0], c.t[1], c.t[2]);
             return n2 == 0.0 ? ctr + mk(0.0, 0.0, c.p[0]) : ctr + d * (c.p[0] * rsqrt(n2));
+        }
+        if (c.type == D3D_MESH) {
+            // the vertex the FP32 climb reaches on the FP32 mirror
+            if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
+            Col<float> cf;
+            cf.nv = c.nv;
+            cf.off = c.off;
+            cf.idx = c.idx;
+            for (int k = 0; k < 9; ++k) cf.R[k] = __double2float_rn(c.R[k]);
+            return xform(c.R, c.t, load_vertex(s.verts64, c.off + mesh_climb(cf, s, rt_mul(cf.R, df))));
         }
         bool up = false;
         if (c.type == D3D_CAPSULE || c.type == D3D_CYLINDER || c.type == D3D_CONE) {

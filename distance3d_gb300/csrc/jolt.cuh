@@ -425,14 +425,12 @@ __device__ __forceinline__ void closest_points(const Simplex<T, Rows>& S, const 
 
 enum GjkEnd { GJK_NO_INTERSECTION = 0, GJK_INTERSECTION = 1, GJK_CLIPPED = 3 };
 
-__device__ __forceinline__ const double* store_verts(const d3d_store& s, double) { return s.verts64; }
-__device__ __forceinline__ const float* store_verts(const d3d_store& s, float) { return s.verts32; }
 
 // Support evaluated in the loop's own precision (the reference's function).
 struct ExactSupport {
     template <typename T>
     static __device__ __forceinline__ V3<T> eval(const Col<T>& c, const d3d_store& s, V3<T> d) {
-        return support(c, store_verts(s, T(0)), d);
+        return support(c, s, d);
     }
 };
 

@@ -27,16 +27,19 @@ constexpr double kEps = DBL_EPSILON;
 
 // colliders.py center(): the pose translation, a hull's vertex mean
 // (np.mean(axis=0): rows summed in order, then divided by the count), a
-// cone's mid-axis point (:582-584); Margin passes through (:633-634).
+// mesh's vertex mean posed, a cone's mid-axis point (:582-584); Margin passes
+// through (:633-634).
 __device__ d3 collider_center(const d3d_store& st, int idx) {
     Col<double> c;
     load_col(st, idx, c);
-    if (c.type == D3D_HULL) {
+    if (c.type == D3D_HULL || c.type == D3D_MESH) {
         if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
         d3 s = load_vertex(st.verts64, c.off);
         for (int k = 1; k < c.nv; ++k) s = s + load_vertex(st.verts64, c.off + k);
         const double n = (double)c.nv;
-        return mk(s.x / n, s.y / n, s.z / n);
+        const d3 m = mk(s.x / n, s.y / n, s.z / n);
+        // a mesh's vertices are in its frame: t + R mean (colliders.py:224-226)
+        return c.type == D3D_MESH ? xform(c.R, c.t, m) : m;
     }
     const d3 t = mk(c.t[0], c.t[1], c.t[2]);
     if (c.type == D3D_CONE) {

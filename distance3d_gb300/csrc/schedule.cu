@@ -18,8 +18,8 @@ inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 std::mutex g_tune_mu;
 d3d_tuning g_tuning = {128, 0, 4, 4096};
 
-// key = ((type1 * 9 + type2) << 4) | size class of the larger hull (at most
-// 80 * 16 + 15 < 2^11); slots at and beyond the device-side count (if given)
+// key = ((type1 * 10 + type2) << 4) | size class of the larger hull or mesh
+// (at most 99 * 16 + 15 < 2^11); slots at and beyond the device-side count (if given)
 // get the largest key
 __global__ void k_pair_keys(d3d_store s, const int32_t* __restrict__ i1, const int32_t* __restrict__ i2, int64_t n,
                             const int64_t* __restrict__ n_dev, uint32_t* __restrict__ keys,
@@ -33,10 +33,10 @@ __global__ void k_pair_keys(d3d_store s, const int32_t* __restrict__ i1, const i
     }
     int4 a = __ldg(reinterpret_cast<const int4*>(s.meta) + i1[k]);
     int4 b = __ldg(reinterpret_cast<const int4*>(s.meta) + i2[k]);
-    int nv = max(a.x == D3D_HULL ? a.y : 0, b.x == D3D_HULL ? b.y : 0);
+    int nv = max(a.x == D3D_HULL || a.x == D3D_MESH ? a.y : 0, b.x == D3D_HULL || b.x == D3D_MESH ? b.y : 0);
     int cls = nv > 0 ? min(32 - __clz(nv), 15) : 0;
-    unsigned ta = (unsigned)min(max(a.x, 0), D3D_CONE), tb = (unsigned)min(max(b.x, 0), D3D_CONE);
-    keys[k] = ((ta * 9u + tb) << 4) | (unsigned)cls;
+    unsigned ta = (unsigned)min(max(a.x, 0), D3D_MESH), tb = (unsigned)min(max(b.x, 0), D3D_MESH);
+    keys[k] = ((ta * 10u + tb) << 4) | (unsigned)cls;
 }
 
 }  // namespace

@@ -89,16 +89,27 @@ __global__ void k_pack(d3d_store s, const int32_t* __restrict__ types, const dou
             off = (int)o;
             write_box_vertices(s, off, R, t, p);
         }
-    } else if (type == D3D_HULL) {
+    } else if (type == D3D_HULL || type == D3D_MESH) {
         int64_t o = hull_offset[i];
         count = hull_count[i];
-        if (o < 0 || count < 1 || o + count > s.n_vertices) {
+        bool ok = o >= 0 && count >= 1 && o + count <= s.n_vertices;
+        if (ok && type == D3D_MESH) {
+            // links block: 6 shortcuts, count + 1 offsets, the lists (mesh.py:26-52)
+            const double b = p[0], start = p[1];
+            ok = b >= 0.0 && b == floor(b) && b + 7.0 + count <= (double)s.n_links && start >= 0.0 &&
+                 start < (double)count && start == floor(start);
+            if (ok) {
+                const int32_t* blk = s.links + (int64_t)b;
+                ok = blk[6] == 7 + count && blk[6 + count] >= blk[6] && (int64_t)b + blk[6 + count] <= s.n_links;
+            }
+        }
+        if (!ok) {
             atomicExch(bad, 1);
             count = 0;
         } else {
             off = (int)o;
         }
-    } else if (type < 0 || type > D3D_CONE) {
+    } else if (type < 0 || type > D3D_MESH) {
         atomicExch(bad, 1);
     }
     reinterpret_cast<int4*>(s.meta)[i] = make_int4(type, count, off, wrapped);
@@ -139,7 +150,7 @@ __global__ void k_support(d3d_store s, const int32_t* __restrict__ idx, const do
     if (k >= n) return;
     Col<double> c;
     load_col(s, idx[k], c);
-    d3 r = support(c, s.verts64, mk(dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2]));
+    d3 r = support(c, s, mk(dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2]));
     out[3 * k] = r.x;
     out[3 * k + 1] = r.y;
     out[3 * k + 2] = r.z;
@@ -226,6 +237,21 @@ __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n,
             hi[i] = np_max(t[i] + e * c.p[0], pb);
         }
         break;
+    case D3D_MESH: {  // colliders.py:234-237: t + V R^T (dgemm, order of dot012), min / max
+        if (c.nv < 1) {
+            for (int i = 0; i < 3; ++i) lo[i] = hi[i] = NAN;
+            break;
+        }
+        for (int r = 0; r < c.nv; ++r) {
+            const d3 v = load_vertex(s.verts64, c.off + r);
+            for (int i = 0; i < 3; ++i) {
+                const double w = t[i] + dot012(v.x, v.y, v.z, R[i * 3], R[i * 3 + 1], R[i * 3 + 2]);
+                if (r == 0 || w < lo[i]) lo[i] = w;
+                if (r == 0 || w > hi[i]) hi[i] = w;
+            }
+        }
+        break;
+    }
     default: {  // box :47-67, hull :6-22
         if (c.nv < 1) {  // rejected by d3d_store_pack
             for (int i = 0; i < 3; ++i) lo[i] = hi[i] = NAN;

@@ -58,10 +58,11 @@ class PinnedColliderSet:
         self.offsets = pin(offsets)
         self.counts = pin(counts)
         self.vertices = pin(cs.vertices)
+        self.links = pin(cs.links)
 
     def nbytes(self):
         return sum(t.numel() * t.element_size() for t in
-                   (self.types, self.poses, self.params, self.offsets, self.counts, self.vertices))
+                   (self.types, self.poses, self.params, self.offsets, self.counts, self.vertices, self.links))
 
 
 class ColliderStore:
@@ -104,13 +105,16 @@ class ColliderStore:
             self.verts32 = torch.empty((max(n_vertices, 1), 4), dtype=torch.float32, device=dev)
             if nv_hull:
                 self.verts64[:nv_hull].copy_(torch.from_numpy(cs.vertices))
+            self.links = torch.from_numpy(cs.links).to(dev) if len(cs.links) else None
             types = torch.from_numpy(cs.types).to(dev)
             poses = torch.from_numpy(cs.poses).to(dev)
             params = torch.from_numpy(cs.params).to(dev)
             offs = torch.from_numpy(offsets).to(dev)
             cnts = torch.from_numpy(counts).to(dev)
             self._view = _lib.D3DStore(n, n_vertices, self.rec64.data_ptr(), self.rec32.data_ptr(),
-                                       self.meta.data_ptr(), self.verts64.data_ptr(), self.verts32.data_ptr())
+                                       self.meta.data_ptr(), self.verts64.data_ptr(), self.verts32.data_ptr(),
+                                       self.links.data_ptr() if self.links is not None else None,
+                                       len(cs.links))
             _lib.check(lib.d3d_store_pack(ctypes.byref(self._view), _ptr(types), _ptr(poses), _ptr(params),
                                           _ptr(offs), _ptr(cnts), nv_hull, _stream(dev)))
 
@@ -132,13 +136,16 @@ class ColliderStore:
             self.verts32 = torch.empty((max(nv, 1), 4), dtype=torch.float32, device=dev)
             if p.n_hull_vertices:
                 self.verts64[:p.n_hull_vertices].copy_(p.vertices, non_blocking=True)
+            self.links = p.links.to(dev, non_blocking=True) if p.links.numel() else None
             types = p.types.to(dev, non_blocking=True)
             poses = p.poses.to(dev, non_blocking=True)
             params = p.params.to(dev, non_blocking=True)
             offs = p.offsets.to(dev, non_blocking=True)
             cnts = p.counts.to(dev, non_blocking=True)
             self._view = _lib.D3DStore(n, nv, self.rec64.data_ptr(), self.rec32.data_ptr(),
-                                       self.meta.data_ptr(), self.verts64.data_ptr(), self.verts32.data_ptr())
+                                       self.meta.data_ptr(), self.verts64.data_ptr(), self.verts32.data_ptr(),
+                                       self.links.data_ptr() if self.links is not None else None,
+                                       p.links.numel())
             _lib.check(lib.d3d_store_pack(ctypes.byref(self._view), _ptr(types), _ptr(poses), _ptr(params),
                                           _ptr(offs), _ptr(cnts), p.n_hull_vertices, _stream(dev)))
 
@@ -155,7 +162,8 @@ class ColliderStore:
 
     def nbytes(self):
         return sum(t.numel() * t.element_size() for t in
-                   (self.rec64, self.rec32, self.meta, self.verts64, self.verts32))
+                   (self.rec64, self.rec32, self.meta, self.verts64, self.verts32)) + \
+            (self.links.numel() * 4 if self.links is not None else 0)
 
     def set_poses(self, idx, poses):
         """Set 4x4 (or 12-value R|t) poses of colliders ``idx`` (not hulls)."""

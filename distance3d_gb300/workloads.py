@@ -20,14 +20,18 @@ from disk.  Rotations are quaternions drawn from a normalised 4-D Gaussian.
 * ``pairs_all_types``: the nine collider types, disk radius U[0.05,0.3],
   ellipse radii U[0.05,0.3] per axis, cone radius U[0.05,0.3] and height
   U[0.1,0.5] (the capsule's ranges), and a fraction of the colliders wrapped
-  in Margin with margin U[0.01,0.05].
+  in Margin with margin U[0.01,0.05].  With ``types=ALL_TYPES_MESH`` also
+  MeshGraphs: N points on the unit sphere in the mesh frame,
+  N = floor(exp(U[ln 8, ln 64])), scaled by U[0.05,0.3], triangulated by
+  their convex hull (scipy), posed by the collider's rotation and center.
 """
 import numpy as np
 
 from .collider_set import (ColliderSet, SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL, DISK, ELLIPSE, CONE,
-                           MARGIN)
+                           MESH, MARGIN, mesh_links)
 
 ALL_TYPES = (SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL, DISK, ELLIPSE, CONE)
+ALL_TYPES_MESH = ALL_TYPES + (MESH,)
 
 # center half-width for which ~30% of mixed six-type pairs intersect
 # (calibrated with the oracle on 200k pairs, seed 0; see tests/test_workloads.py)
@@ -101,12 +105,35 @@ def random_colliders(rng, n, type_choices, center_half_width=1.0, hull_n_range=(
     R[hulls] = np.eye(3)
     t[hulls] = 0.0
     R[types == SPHERE] = np.eye(3)
+    links = np.zeros(0, np.int32)
+    meshes = np.flatnonzero(types == MESH)
+    if len(meshes):
+        from scipy.spatial import ConvexHull
+        nm = np.floor(np.exp(rng.uniform(np.log(8), np.log(64), size=len(meshes)))).astype(np.int64)
+        blocks, mverts = [], []
+        nl = 0
+        for k, i in enumerate(meshes):
+            p = rng.standard_normal((nm[k], 3))
+            p /= np.linalg.norm(p, axis=1, keepdims=True)
+            p *= u[i, 0]
+            tri = ConvexHull(p).simplices
+            blk = mesh_links(p, tri)
+            offsets[i] = total + sum(len(m) for m in mverts)
+            counts[i] = len(p)
+            params[i, :2] = (nl, float(np.min(tri)))
+            blocks.append(blk)
+            nl += len(blk)
+            mverts.append(p)
+        links = np.concatenate(blocks)
+        mv = np.zeros((sum(len(m) for m in mverts), 4))
+        mv[:, :3] = np.concatenate(mverts)
+        verts = np.concatenate([verts, mv])
     poses = np.concatenate([R.reshape(n, 9), t], axis=1)
     if margin_fraction > 0:
         wrap = rng.uniform(size=n) < margin_fraction
         params[wrap, 3] = rng.uniform(0.01, 0.05, size=int(wrap.sum()))
         types = types | np.where(wrap, MARGIN, 0).astype(np.int32)
-    return ColliderSet(types, poses, params, offsets, counts, verts)
+    return ColliderSet(types, poses, params, offsets, counts, verts, links)
 
 
 def pairs_sphere_capsule_box(n_pairs, seed=0):
@@ -126,11 +153,12 @@ def pairs_mixed_six(n_pairs, seed=0, center_half_width=1.0):
     return cs, 2 * idx, 2 * idx + 1
 
 
-def pairs_all_types(n_pairs, seed=0, center_half_width=INTERSECT30_HALF_WIDTH, margin_fraction=0.25):
-    """(ColliderSet with 2*n_pairs colliders, i1, i2): the nine types, a
-    fraction wrapped in Margin."""
+def pairs_all_types(n_pairs, seed=0, center_half_width=INTERSECT30_HALF_WIDTH, margin_fraction=0.25,
+                    types=ALL_TYPES):
+    """(ColliderSet with 2*n_pairs colliders, i1, i2): the nine types (ten
+    with ``types=ALL_TYPES_MESH``), a fraction wrapped in Margin."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    cs = random_colliders(rng, 2 * n_pairs, ALL_TYPES, center_half_width, margin_fraction=margin_fraction)
+    cs = random_colliders(rng, 2 * n_pairs, types, center_half_width, margin_fraction=margin_fraction)
     idx = np.arange(n_pairs, dtype=np.int32)
     return cs, 2 * idx, 2 * idx + 1
 

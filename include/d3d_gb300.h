@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define D3D_ABI_VERSION 1
+#define D3D_ABI_VERSION 2
 
 /* return codes */
 #define D3D_SUCCESS 0
@@ -45,6 +45,8 @@ extern "C" {
 #define D3D_DISK 6          /* normal = R column 2 (colliders.py:443-497) */
 #define D3D_ELLIPSE 7       /* axes = R columns 0 and 1 (colliders.py:500-551) */
 #define D3D_CONE 8          /* colliders.py:554-603 */
+#define D3D_MESH 9          /* MeshGraph (colliders.py:187-240): vertices in the mesh frame,
+                               hill-climbing support over the links block (mesh.py:12-127) */
 #define D3D_MARGIN 0x100    /* flag or-ed into a type: the collider wrapped in Margin
                                (colliders.py:606-647), margin = params[3] */
 
@@ -69,9 +71,17 @@ extern "C" {
  *   rec32  [n][16] float  : the same in FP32
  *   meta   [n][4]  int32  : type (without the margin flag), vertex count,
  *                           vertex offset, 1 if wrapped in Margin else 0
+ *   links  [L]     int32  : MeshGraph adjacency blocks (may be NULL without meshes)
  * A disk's R holds column_stack(x, y, normal) with x, y derived from the
  * normal (utils.py:78-122 plane_basis_from_normal) when it is packed or
  * posed, as the reference derives them in every support call.
+ * A MeshGraph's vertices (mesh frame) sit in the vertex pool like a hull's;
+ * its params are (links offset, start vertex, 0).  Its links block, for nv
+ * vertices: the 6 shortcut vertices (argmax x, y, z, argmin x, y, z of the
+ * vertices, mesh.py:44-47), then nv + 1 offsets of the neighbour lists
+ * (relative to the block), then the neighbour lists in the order the
+ * reference iterates them (mesh.py:34-52).  Vertex indices are local to the
+ * mesh.
  *   verts64 [V][4] double : hull vertices then 8 vertices per box (xyz, 0)
  *   verts32 [V][4] float  : the same in FP32
  */
@@ -83,6 +93,8 @@ typedef struct d3d_store {
     int32_t* meta;
     double* verts64;
     float* verts32;
+    int32_t* links;
+    int64_t n_links;
 } d3d_store;
 
 typedef struct d3d_gjk_options {
@@ -108,11 +120,13 @@ const char* d3d_last_error(void);
 /* Pack a store.  Input arrays are the packed host format already copied to
  * the device: types[n] (D3D_* or-ed with D3D_MARGIN for a Margin wrapper),
  * poses[n][12], params[n][4] (params[3]: the margin), hull_offset[n] (int64;
+ * for a hull or a mesh: its first vertex row;
  * for a box: the row where its 8 derived vertices go, >= n_hull_vertices),
- * hull_count[n]; the caller has copied the n_hull_vertices hull rows into
- * store->verts64[0 : n_hull_vertices].  Box vertices follow
- * geometry.py:138-157 (convert_box_to_vertices); FP32 mirrors are rounded from
- * FP64.  Replaces collider construction, colliders.py:109-440. */
+ * hull_count[n]; the caller has copied the n_hull_vertices hull and mesh rows
+ * into store->verts64[0 : n_hull_vertices] and the mesh links blocks into
+ * store->links.  Box vertices follow geometry.py:138-157
+ * (convert_box_to_vertices); FP32 mirrors are rounded from FP64.  Replaces
+ * collider construction, colliders.py:109-647. */
 int d3d_store_pack(const d3d_store* store, const int32_t* types, const double* poses,
                    const double* params, const int64_t* hull_offset, const int32_t* hull_count,
                    int64_t n_hull_vertices, void* stream);

@@ -23,7 +23,8 @@
  *   types  : type code, or-ed with T_MARGIN for a Margin wrapper
  *   params : 4 doubles  (sphere r | capsule r,h | box size xyz (full edge
  *            lengths) | cylinder r,L | ellipsoid radii xyz | hull unused |
- *            disk r | ellipse radii (2) | cone r,h; params[3] the margin)
+ *            disk r | ellipse radii (2) | cone r,h | mesh links offset,
+ *            start vertex; params[3] the margin)
  *            A disk's normal is R column 2; an ellipse's axes are R columns
  *            0 and 1.
  *   hull vertices: (V,4) doubles, xyz + pad, world space.
@@ -46,6 +47,7 @@
 #define T_DISK 6
 #define T_ELLIPSE 7
 #define T_CONE 8
+#define T_MESH 9        /* MeshGraph: vertices in the mesh frame, links block */
 #define T_MARGIN 0x100  /* flag: wrapped in Margin, margin = params[3] */
 
 #define ST_OK 0
@@ -93,6 +95,8 @@ typedef struct {
     double p[3];
     const double* verts; /* (n,4) */
     int nverts;
+    const int32_t* links; /* mesh: links block (shortcuts, offsets, neighbour lists) */
+    int start;            /* mesh: start vertex of the hill climb */
     double box[8 * 4];   /* box vertices, geometry.py:138-157 */
 } collider;
 
@@ -125,7 +129,7 @@ static void plane_basis(const double* n, double* x, double* y) {
 
 static void load_collider(collider* c, int idx, const int32_t* types, const double* poses,
                           const double* params, const int64_t* hull_offset,
-                          const int32_t* hull_count, const double* vertices) {
+                          const int32_t* hull_count, const double* vertices, const int32_t* links) {
     c->type = types[idx] & ~T_MARGIN;
     c->wrapped = (types[idx] & T_MARGIN) != 0;
     c->margin = params[(int64_t)idx * 4 + 3];
@@ -144,9 +148,15 @@ static void load_collider(collider* c, int idx, const int32_t* types, const doub
         box_vertices(c->R, c->t, c->p, c->box);
         c->verts = c->box;
         c->nverts = 8;
-    } else if (c->type == T_HULL) {
+    } else if (c->type == T_HULL || c->type == T_MESH) {
         c->verts = vertices + hull_offset[idx] * 4;
         c->nverts = hull_count[idx];
+    }
+    c->links = NULL;
+    c->start = 0;
+    if (c->type == T_MESH) {
+        c->links = links + (int64_t)c->p[0];
+        c->start = (int)c->p[1];
     }
 }
 
@@ -241,6 +251,33 @@ static v3 base_support(const collider* c, v3 d) {
         else q = scl(q, r / n);
         if (!(dot(l, q) >= l.z * h)) q = mk(0.0, 0.0, h);
         return xform(c->R, c->t, q);
+    }
+    case T_MESH: {
+        /* mesh.py:77-85, 88-127: direction into the mesh frame, hill climb
+         * from the start vertex (each call starts there), posed vertex */
+        v3 l = rt_mul(c->R, d);
+        const int32_t* blk = c->links;
+        const double eps = 10.0 * EPS;  /* PROJECTION_LENGTH_EPSILON */
+        int best = c->start;
+        for (int k = 0; k < 6; ++k) {
+            int cand = blk[k];
+            const double* a = c->verts + (int64_t)cand * 4;
+            const double* b = c->verts + (int64_t)best * 4;
+            if (dot(l, mk(a[0] - b[0], a[1] - b[1], a[2] - b[2])) > eps) best = cand;
+        }
+        int converged = 0;
+        while (!converged) {
+            converged = 1;
+            int lo = blk[6 + best], hi = blk[7 + best];
+            for (int e = lo; e < hi; ++e) {
+                int cand = blk[e];
+                const double* a = c->verts + (int64_t)cand * 4;
+                const double* b = c->verts + (int64_t)best * 4;
+                if (dot(l, mk(a[0] - b[0], a[1] - b[1], a[2] - b[2])) > eps) { best = cand; converged = 0; }
+            }
+        }
+        const double* v = c->verts + (int64_t)best * 4;
+        return xform(c->R, c->t, mk(v[0], v[1], v[2]));
     }
     default: { /* box and hull */
         int best = 0;
@@ -695,12 +732,13 @@ static int epa(const v3* simplex, const collider* c1, const collider* c2, int ma
  * vertex mean (np.mean(axis=0): rows summed in order, then divided), a
  * cone's mid-axis point :582-584; Margin passes through :633-634. */
 static v3 collider_center(const collider* c) {
-    if (c->type == T_HULL) {
+    if (c->type == T_HULL || c->type == T_MESH) {
         v3 s = mk(c->verts[0], c->verts[1], c->verts[2]);
         for (int k = 1; k < c->nverts; ++k)
             s = add(s, mk(c->verts[k * 4], c->verts[k * 4 + 1], c->verts[k * 4 + 2]));
         double n = (double)c->nverts;
-        return mk(s.x / n, s.y / n, s.z / n);
+        v3 m = mk(s.x / n, s.y / n, s.z / n);
+        return c->type == T_MESH ? xform(c->R, c->t, m) : m;  /* colliders.py:224-226 */
     }
     v3 t = mk(c->t[0], c->t[1], c->t[2]);
     if (c->type == T_CONE) {
@@ -997,6 +1035,18 @@ static void base_aabb(const collider* c, double* o) {
             o[2 * i] = t[i] - e; o[2 * i + 1] = t[i] + e;
         }
         return;
+    case T_MESH:  /* colliders.py:234-237: t + V R^T (dgemm: dot012 order), min / max */
+        for (int i = 0; i < 3; ++i) {
+            double lo = 0.0, hi = 0.0;
+            for (int k = 0; k < c->nverts; ++k) {
+                const double* v = c->verts + (int64_t)k * 4;
+                double w = t[i] + dot012(v[0], v[1], v[2], R[i * 3], R[i * 3 + 1], R[i * 3 + 2]);
+                if (k == 0 || w < lo) lo = w;
+                if (k == 0 || w > hi) hi = w;
+            }
+            o[2 * i] = lo; o[2 * i + 1] = hi;
+        }
+        return;
     case T_CONE:  /* :177-203 */
         for (int i = 0; i < 3; ++i) {
             double pb = t[i] + c->p[1] * R[i * 3 + 2];
@@ -1024,8 +1074,8 @@ static void base_aabb(const collider* c, double* o) {
 /* ---------------------------- exported batch API -------------------------- */
 
 #define SET_ARGS const int32_t* types, const double* poses, const double* params, \
-    const int64_t* hull_offset, const int32_t* hull_count, const double* vertices
-#define SET_PASS types, poses, params, hull_offset, hull_count, vertices
+    const int64_t* hull_offset, const int32_t* hull_count, const double* vertices, const int32_t* links
+#define SET_PASS types, poses, params, hull_offset, hull_count, vertices, links
 
 static void set_threads(int nthreads) {
 #ifdef _OPENMP

@@ -24,7 +24,7 @@ def lib():
     if _lib is None:
         path = _build.build()
         _lib = ctypes.CDLL(path)
-        _set_args = [I32P, DP, DP, I64P, I32P, DP]
+        _set_args = [I32P, DP, DP, I64P, I32P, DP, I32P]
         _lib.orc_gjk_distance.argtypes = _set_args + [
             I32P, I32P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
             ctypes.c_int, DP, DP, DP, DP, I8P, I8P, I32P, ctypes.c_int]
@@ -55,8 +55,9 @@ def _p(a, t):
 
 
 def _set(cs):
+    links = cs.links if len(cs.links) else None
     return [_p(cs.types, I32P), _p(cs.poses, DP), _p(cs.params, DP),
-            _p(cs.hull_offset, I64P), _p(cs.hull_count, I32P), _p(cs.vertices, DP)]
+            _p(cs.hull_offset, I64P), _p(cs.hull_count, I32P), _p(cs.vertices, DP), _p(links, I32P)]
 
 
 def max_threads():

@@ -22,7 +22,7 @@ def load_golden(name):
     cs = None
     if "types" in g:
         cs = ColliderSet(g["types"], g["poses"], g["params"], g["hull_offset"],
-                         g["hull_count"], g["vertices"])
+                         g["hull_count"], g["vertices"], g.get("links"))
     return g, cs
 
 

@@ -32,6 +32,12 @@ Inputs come from ``distance3d_gb300.workloads`` (seeded).  Outputs:
 * ``mpr_all9.npz``    -- reference ``mpr.mpr_penetration`` (flag, depth,
   direction, contact position; NaN for None) and ``mpr.mpr_intersection`` on
   every gjk_all9 pair, at the default tolerance and iteration limit.
+* ``gjk_mesh10.npz``, ``epa_mesh10.npz``, ``mpr_mesh10.npz`` -- the same for
+  1,000 pairs of the ten types (MeshGraph included).  The reference's
+  MeshGraph support starts from its previous answer (the object caches it);
+  here every support call restarts from the mesh's start vertex, the
+  semantics of the GPU path, so that the fixture does not depend on the
+  order of the calls.
 * ``aabb_tree.npz``   -- a 400-collider scene: reference AabbTree self overlap
   (both orders, i == j dropped, reduced to i < j), brute force
   ``all_aabbs_overlap``, BoundingVolumeHierarchy.aabb_overlapping_with_self on
@@ -88,11 +94,37 @@ def make_ref_colliders(colliders, cs):
             out.append(colliders.Disk(pose[:3, 3].copy(), float(p[0]), pose[:3, 2].copy()))
         elif t == 7:
             out.append(colliders.Ellipse(pose[:3, 3].copy(), np.ascontiguousarray(pose[:3, :2].T), p[:2].copy()))
-        else:
+        elif t == 8:
             out.append(colliders.Cone(pose, float(p[0]), float(p[1])))
+        else:
+            out.append(fresh_mesh_graph(colliders, cs, i, pose))
         if int(cs.types[i]) & 0x100:
             out[-1] = colliders.Margin(out[-1], float(p[3]))
     return out
+
+
+def fresh_mesh_graph(colliders, cs, i, pose):
+    """The reference's MeshGraph for collider i, its triangles recomputed by
+    scipy's ConvexHull as the workload made them (checked against the packed
+    links), and its support restarted from the first vertex of the
+    triangles in every call: the reference caches the last answer in the
+    object (mesh.py:84), the GPU path starts every call afresh."""
+    from scipy.spatial import ConvexHull
+    from distance3d_gb300.collider_set import mesh_links
+    o, c = int(cs.hull_offset[i]), int(cs.hull_count[i])
+    v = np.ascontiguousarray(cs.vertices[o:o + c, :3])
+    tri = ConvexHull(v).simplices
+    blk = mesh_links(v, tri)
+    b = int(cs.params[i, 0])
+    assert np.array_equal(cs.links[b:b + len(blk)], blk) and cs.params[i, 1] == np.min(tri)
+    m = colliders.MeshGraph(pose, v, tri)
+    start = np.min(tri)
+
+    def support_function(d, m=m, start=start):
+        m._support_function.first_idx = start
+        return m._support_function(d)[1]
+    m.support_function = support_function
+    return m
 
 
 def support_fixture(cols, cs, seed=11):
@@ -174,7 +206,7 @@ def gjk_fixture(mods, cs, i1, i2):
     aabbs = np.stack([c.aabb() for c in cols])
     print(f"  gjk: {n} pairs in {dt:.1f}s ({n / dt:.0f} pairs/s incl. intersection)")
     return dict(types=cs.types, poses=cs.poses, params=cs.params, hull_offset=cs.hull_offset,
-                hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), i1=i1, i2=i2,
+                hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), links=cs.links, i1=i1, i2=i2,
                 dist=dist, cp1=cp1, cp2=cp2, simplex=simplex, n_simplex=n_simplex,
                 iterations=iters, intersect=hit, aabbs=aabbs), cols
 
@@ -301,13 +333,24 @@ def make_all9(mods, workloads):
     np.savez_compressed(os.path.join(HERE, "mpr_all9.npz"), **mpr_fixture(cols, gf))
 
 
+def make_mesh(mods, workloads):
+    print("ten-type pairs (MeshGraph included) with margins")
+    cs, i1, i2 = workloads.pairs_all_types(1000, seed=2025, types=workloads.ALL_TYPES_MESH)
+    gf, cols = gjk_fixture(mods, cs, i1, i2)
+    gf.update(support_fixture(cols, cs))
+    print(f"  intersecting fraction {np.mean(gf['dist'] == 0.0):.3f}")
+    np.savez_compressed(os.path.join(HERE, "gjk_mesh10.npz"), **gf)
+    np.savez_compressed(os.path.join(HERE, "epa_mesh10.npz"), **epa_fixture(mods, cols, gf))
+    np.savez_compressed(os.path.join(HERE, "mpr_mesh10.npz"), **mpr_fixture(cols, gf))
+
+
 def make_tree(mods, workloads):
     print("aabb tree scene")
     scene = workloads.scene_mixed_six(400, seed=4321, half_width=3.0)
     np.savez_compressed(os.path.join(HERE, "aabb_tree.npz"), **tree_fixture(mods, scene))
 
 
-FIXTURES = {"mixed6": make_mixed6, "scb": make_scb, "all9": make_all9, "tree": make_tree}
+FIXTURES = {"mixed6": make_mixed6, "scb": make_scb, "all9": make_all9, "mesh10": make_mesh, "tree": make_tree}
 
 
 def main(ref_root, names):

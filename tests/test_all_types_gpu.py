@@ -1,6 +1,6 @@
-"""Disk, Ellipse, Cone and the Margin wrapper on the GPU, next to the six
-original types: supports, AABBs, pose updates, GJK and EPA in both forms,
-against the reference's golden vectors and the oracle.
+"""Disk, Ellipse, Cone, MeshGraph and the Margin wrapper on the GPU, next to
+the six original types: supports, AABBs, pose updates, GJK and EPA in both
+forms, against the reference's golden vectors and the oracle.
 
 FP64 results are compared bit for bit.  The mixed form keeps the tolerances
 of the six-type tests (1e-5 relative distance error, identical intersection
@@ -21,8 +21,12 @@ from tests.test_gjk_gpu import assert_bit_exact, host, mixed_check
 pytestmark = pytest.mark.gpu
 
 
-def test_supports_and_aabbs_match_reference(golden):
-    g, cs = golden("gjk_all9")
+FIXTURES = ["all9", "mesh10"]
+
+
+@pytest.mark.parametrize("fx", FIXTURES)
+def test_supports_and_aabbs_match_reference(golden, fx):
+    g, cs = golden("gjk_" + fx)
     st = ColliderStore(cs)
     n = len(cs)
     idx = np.repeat(np.arange(n), 6).astype(np.int32)
@@ -31,8 +35,9 @@ def test_supports_and_aabbs_match_reference(golden):
     assert np.array_equal(st.aabbs().cpu().numpy(), g["aabbs"])
 
 
-def test_fp64_gjk_matches_reference_golden(golden):
-    g, cs = golden("gjk_all9")
+@pytest.mark.parametrize("fx", FIXTURES)
+def test_fp64_gjk_matches_reference_golden(golden, fx):
+    g, cs = golden("gjk_" + fx)
     st = ColliderStore(cs)
     r = host(gjk_distance_batch(st, g["i1"], g["i2"]))
     assert np.all(r["status"] == 0)
@@ -41,10 +46,11 @@ def test_fp64_gjk_matches_reference_golden(golden):
     assert np.array_equal(h["hit"].cpu().numpy(), g["intersect"])
 
 
+@pytest.mark.parametrize("fx", FIXTURES)
 @pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))])
-def test_fp64_epa_matches_reference_golden(golden, tag, kw):
-    g, cs = golden("gjk_all9")
-    e, _ = golden("epa_all9")
+def test_fp64_epa_matches_reference_golden(golden, fx, tag, kw):
+    g, cs = golden("gjk_" + fx)
+    e, _ = golden("epa_" + fx)
     p = e["pair"]
     r = host(epa_batch(ColliderStore(cs), g["i1"][p], g["i2"][p], g["simplex"][p], **kw))
     st = e[f"status_{tag}"]
@@ -54,9 +60,10 @@ def test_fp64_epa_matches_reference_golden(golden, tag, kw):
     assert np.array_equal(r["n_faces"][ok], e[f"n_faces_{tag}"][ok])
 
 
-@pytest.mark.parametrize("margin_fraction", [0.0, 0.5])
-def test_fp64_matches_oracle(margin_fraction):
-    cs, i1, i2 = workloads.pairs_all_types(20000, seed=41, margin_fraction=margin_fraction)
+@pytest.mark.parametrize("margin_fraction,types", [(0.0, workloads.ALL_TYPES), (0.5, workloads.ALL_TYPES),
+                                                   (0.25, workloads.ALL_TYPES_MESH)])
+def test_fp64_matches_oracle(margin_fraction, types):
+    cs, i1, i2 = workloads.pairs_all_types(20000, seed=41, margin_fraction=margin_fraction, types=types)
     st = ColliderStore(cs)
     r = host(gjk_distance_batch(st, i1, i2))
     ref = oracle.gjk_distance(cs, i1, i2)
@@ -73,19 +80,21 @@ def test_fp64_matches_oracle(margin_fraction):
     assert np.array_equal(e["n_faces"], eref["n_faces"])
 
 
-def test_mixed_gjk_within_tolerance(golden):
-    cs, i1, i2 = workloads.pairs_all_types(30000, seed=42)
+@pytest.mark.parametrize("fx,types", [("all9", workloads.ALL_TYPES), ("mesh10", workloads.ALL_TYPES_MESH)])
+def test_mixed_gjk_within_tolerance(golden, fx, types):
+    cs, i1, i2 = workloads.pairs_all_types(30000, seed=42, types=types)
     st = ColliderStore(cs)
     r = host(gjk_distance_batch(st, i1, i2, precision="mixed"))
     assert np.all(r["status"] == 0)
     mixed_check(r, oracle.gjk_distance(cs, i1, i2), cs, np.asarray(i1), np.asarray(i2))
-    g, cs = golden("gjk_all9")
+    g, cs = golden("gjk_" + fx)
     r = host(gjk_distance_batch(ColliderStore(cs), g["i1"], g["i2"], precision="mixed"))
     mixed_check(r, g, cs, g["i1"], g["i2"])
 
 
-def test_mixed_epa_within_tolerance():
-    cs, i1, i2 = workloads.pairs_all_types(30000, seed=43)
+@pytest.mark.parametrize("types", [workloads.ALL_TYPES, workloads.ALL_TYPES_MESH])
+def test_mixed_epa_within_tolerance(types):
+    cs, i1, i2 = workloads.pairs_all_types(30000, seed=43, types=types)
     st = ColliderStore(cs)
     g = host(gjk_distance_batch(st, i1, i2))
     hit = np.flatnonzero(g["dist"] == 0.0)
@@ -107,12 +116,13 @@ def test_set_poses_new_types():
     """update_pose of disks (normal = R column 2, basis re-derived), ellipses,
     cones and wrapped colliders: AABBs and supports as the oracle computes
     them from the new poses."""
-    cs, _, _ = workloads.pairs_all_types(2000, seed=44, margin_fraction=0.5)
+    cs, _, _ = workloads.pairs_all_types(2000, seed=44, margin_fraction=0.5, types=workloads.ALL_TYPES_MESH)
     st = ColliderStore(cs)
     movable = np.flatnonzero(cs.base_types != HULL).astype(np.int32)
     new = workloads.random_colliders(np.random.default_rng(5), len(movable), [1], 1.0).poses
     st.set_poses(movable, new)
-    moved = ColliderSet(cs.types, cs.poses.copy(), cs.params, cs.hull_offset, cs.hull_count, cs.vertices)
+    moved = ColliderSet(cs.types, cs.poses.copy(), cs.params, cs.hull_offset, cs.hull_count, cs.vertices,
+                        cs.links)
     moved.poses[movable] = new
     assert np.array_equal(st.aabbs().cpu().numpy(), oracle.aabbs(moved))
     idx = np.repeat(np.arange(len(cs)), 4).astype(np.int32)
@@ -123,12 +133,13 @@ def test_set_poses_new_types():
 
 
 def test_collider_objects(golden):
-    """This package's Disk / Ellipse / Cone / Margin objects, packed by
-    from_colliders, give the reference's supports and boxes."""
+    """This package's Disk / Ellipse / Cone / MeshGraph / Margin objects,
+    packed by from_colliders, give the reference's supports and boxes."""
+    from scipy.spatial import ConvexHull
     from distance3d_gb300 import colliders
-    g, cs = golden("gjk_all9")
+    g, cs = golden("gjk_mesh10")
     objs = []
-    for i in range(60):
+    for i in range(80):
         t = int(cs.types[i]) & ~MARGIN
         pose = np.eye(4)
         pose[:3, :3] = cs.poses[i, :9].reshape(3, 3)
@@ -140,6 +151,10 @@ def test_collider_objects(golden):
             c = colliders.Ellipse(pose[:3, 3].copy(), np.ascontiguousarray(pose[:3, :2].T), p[:2].copy())
         elif t == 8:
             c = colliders.Cone(pose, float(p[0]), float(p[1]))
+        elif t == 9:
+            o, n = int(cs.hull_offset[i]), int(cs.hull_count[i])
+            v = np.ascontiguousarray(cs.vertices[o:o + n, :3])
+            c = colliders.MeshGraph(pose, v, ConvexHull(v).simplices)
         else:
             continue
         if int(cs.types[i]) & MARGIN:

@@ -46,7 +46,7 @@ def test_binding_covers_header():
 
 
 def test_abi_version(lib):
-    assert lib.d3d_abi_version() == 1
+    assert lib.d3d_abi_version() == 2
 
 
 def test_epa_scratch_sizing(lib):
@@ -64,7 +64,7 @@ def test_invalid_arguments_rejected_on_host(lib):
                               None, None)
     assert rc == _lib.D3D_ERR_INVALID
     assert b"invalid d3d_store" in lib.d3d_last_error()
-    st = _lib.D3DStore(0, 0, 8, 8, 8, 0, 0)  # dummy non-null pointers, never dereferenced
+    st = _lib.D3DStore(0, 0, 8, 8, 8, 0, 0, 0, 0)  # dummy non-null pointers, never dereferenced
     bad = _lib.GjkOptions(1e-10, 1e5, 1e-8, 0, 0)
     rc = lib.d3d_gjk_distance(ctypes.byref(st), None, None, 1, ctypes.byref(bad), None, None, None, None,
                               None, None, None, None)

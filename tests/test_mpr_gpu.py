@@ -24,9 +24,10 @@ def assert_same(r, ref):
             assert np.array_equal(r[k], ref[k], equal_nan=True), k
 
 
-def test_mpr_matches_reference_golden(golden):
-    g, cs = golden("gjk_all9")
-    m, _ = golden("mpr_all9")
+@pytest.mark.parametrize("fx", ["all9", "mesh10"])
+def test_mpr_matches_reference_golden(golden, fx):
+    g, cs = golden("gjk_" + fx)
+    m, _ = golden("mpr_" + fx)
     st = ColliderStore(cs)
     r = host(mpr_batch(st, m["i1"], m["i2"]))
     assert np.all(r["status"] == 0)
@@ -40,6 +41,7 @@ def test_mpr_matches_reference_golden(golden):
 
 @pytest.mark.parametrize("maker,kw", [
     (workloads.pairs_all_types, dict(margin_fraction=0.5)),
+    (workloads.pairs_all_types, dict(types=workloads.ALL_TYPES_MESH)),
     (workloads.pairs_mixed_six, dict(center_half_width=workloads.INTERSECT30_HALF_WIDTH)),
     (workloads.pairs_sphere_capsule_box, {}),
 ])

@@ -9,7 +9,7 @@ import pytest
 from oracle import oracle
 
 
-@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb", "gjk_all9"])
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb", "gjk_all9", "gjk_mesh10"])
 def test_gjk_distance_bit_exact(golden, name):
     g, cs = golden(name)
     r = oracle.gjk_distance(cs, g["i1"], g["i2"])
@@ -23,7 +23,7 @@ def test_gjk_distance_bit_exact(golden, name):
     assert np.all(r["status"] == 0)
 
 
-@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb", "gjk_all9"])
+@pytest.mark.parametrize("name", ["gjk_mixed6", "gjk_scb", "gjk_all9", "gjk_mesh10"])
 def test_gjk_intersection_and_aabbs(golden, name):
     g, cs = golden(name)
     h = oracle.gjk_intersection(cs, g["i1"], g["i2"])
@@ -32,18 +32,19 @@ def test_gjk_intersection_and_aabbs(golden, name):
     assert np.array_equal(oracle.aabbs(cs), g["aabbs"])
 
 
-def test_supports_bit_exact(golden):
+@pytest.mark.parametrize("name", ["gjk_all9", "gjk_mesh10"])
+def test_supports_bit_exact(golden, name):
     """Every type's support function, Margin wrappers included, along random
     directions, +/- the local z axis and the zero vector."""
-    g, cs = golden("gjk_all9")
+    g, cs = golden(name)
     n = len(cs)
     idx = np.repeat(np.arange(n), 6)
     got = oracle.support_batch(cs, idx, g["support_dirs"].reshape(-1, 3)).reshape(n, 6, 3)
     assert np.array_equal(got, g["supports"])
-    assert np.unique(cs.base_types).size == 9 and cs.wrapped.any()
+    assert np.unique(cs.base_types).size >= 9 and cs.wrapped.any()
 
 
-@pytest.mark.parametrize("fixture", ["mixed6", "all9"])
+@pytest.mark.parametrize("fixture", ["mixed6", "all9", "mesh10"])
 @pytest.mark.parametrize("tag,kw", [("default", {}),
                                     ("large", dict(max_faces=256, max_loose_edges=128))])
 def test_epa_bit_exact(golden, fixture, tag, kw):
@@ -77,10 +78,11 @@ def test_queries_match_tree(golden):
         assert np.array_equal(np.sort(got), want)
 
 
-def test_mpr_bit_exact(golden):
-    """mpr_penetration and mpr_intersection on the nine-type pairs."""
-    g, cs = golden("gjk_all9")
-    m, _ = golden("mpr_all9")
+@pytest.mark.parametrize("fixture", ["all9", "mesh10"])
+def test_mpr_bit_exact(golden, fixture):
+    """mpr_penetration and mpr_intersection on the nine- and ten-type pairs."""
+    g, cs = golden("gjk_" + fixture)
+    m, _ = golden("mpr_" + fixture)
     r = oracle.mpr(cs, m["i1"], m["i2"])
     assert np.all(r["status"] == 0)
     assert np.array_equal(r["hit"], m["hit"])

@@ -227,24 +227,18 @@ __device__ __forceinline__ const float* store_verts(const d3d_store& s, float) {
 // the step exceeds 10 EPSILON (PROJECTION_LENGTH_EPSILON).  The climb
 // strictly increases the projection, so it ends within nv passes; the bound
 // is a guard.  Out-of-range links are skipped.
-// The links offset and the start vertex are read from the FP64 record (exact
-// integers there; the FP32 record cannot hold large offsets).
 template <typename T>
-__device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, V3<T> l) {
-    const T* verts = store_verts(st, T(0));
-    const int nv = c.nv;
-    const double* rec = st.rec64 + (size_t)c.idx * 16;
-    const int32_t* blk = st.links + (int64_t)__ldg(rec + 12);
+__device__ __forceinline__ int mesh_climb_body(const T* __restrict__ verts, const int32_t* __restrict__ blk, int off,
+                                               int nv, int best, T lx, T ly, T lz) {
+    const V3<T> l = mk(lx, ly, lz);
     const T eps = T(10.0 * DBL_EPSILON);
-    int best = (int)__ldg(rec + 13);
     if (best < 0 || best >= nv) best = 0;
-    V3<T> vb = load_vertex(verts, c.off + best);
+    V3<T> vb = load_vertex(verts, off + best);
     for (int k = 0; k < 6; ++k) {
         const int cand = __ldg(blk + k);
         if (cand < 0 || cand >= nv) continue;
-        const V3<T> v = load_vertex(verts, c.off + cand);
-        const V3<T> diff = v - vb;
-        if (dot(l, diff) > eps) {
+        const V3<T> v = load_vertex(verts, off + cand);
+        if (dot(l, v - vb) > eps) {
             best = cand;
             vb = v;
         }
@@ -255,9 +249,8 @@ __device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, 
         for (int e = lo; e < hi; ++e) {
             const int cand = __ldg(blk + e);
             if (cand < 0 || cand >= nv) continue;
-            const V3<T> v = load_vertex(verts, c.off + cand);
-            const V3<T> diff = v - vb;
-            if (dot(l, diff) > eps) {
+            const V3<T> v = load_vertex(verts, off + cand);
+            if (dot(l, v - vb) > eps) {
                 best = cand;
                 vb = v;
                 converged = false;
@@ -266,6 +259,26 @@ __device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, 
         if (converged) break;
     }
     return best;
+}
+
+// The same as a call (scalar arguments, nothing through the stack), for
+// kernels that keep the climb out of their hot loop.
+template <typename T>
+__device__ __noinline__ int mesh_climb_call(const T* __restrict__ verts, const int32_t* __restrict__ blk, int off,
+                                            int nv, int best, T lx, T ly, T lz) {
+    return mesh_climb_body(verts, blk, off, nv, best, lx, ly, lz);
+}
+
+// The climb for collider c, inlined (CALL = false) or called.  The links
+// offset and the start vertex are read from the FP64 record (exact integers
+// there; the FP32 record cannot hold large offsets).
+template <bool CALL = false, typename T>
+__device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, V3<T> l) {
+    const double* rec = st.rec64 + (size_t)c.idx * 16;
+    const int32_t* blk = st.links + (int64_t)__ldg(rec + 12);
+    const int start = (int)__ldg(rec + 13);
+    if (CALL) return mesh_climb_call(store_verts(st, T(0)), blk, c.off, c.nv, start, l.x, l.y, l.z);
+    return mesh_climb_body(store_verts(st, T(0)), blk, c.off, c.nv, start, l.x, l.y, l.z);
 }
 
 // Support point of the collider itself (without its margin) along d.  Sphere

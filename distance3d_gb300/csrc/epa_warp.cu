@@ -168,6 +168,7 @@ __device__ __forceinline__ unsigned half_mask() { return (lane_id() & 16) ? 0xff
 
 // w = s_a(d) - s_b(-d) in FP32: the lower half warp evaluates collider a, the
 // upper half collider b, together; every lane returns w.
+template <bool MESH>
 __device__ __forceinline__ f3 minkowski32(const d3d_store& st, int a, int b, f3 d) {
     const bool up = lane_id() & 16;
     Col<float> c;
@@ -180,7 +181,7 @@ __device__ __forceinline__ f3 minkowski32(const d3d_store& st, int a, int b, f3 
         else
             s = margin_fast(st, c, load_vertex(st.verts32, c.off + (c.nv == 1 ? 0 : half_argmax(st.verts32, c.off, c.nv, dd, half_mask()))), dd);
     } else {
-        s = FastSupport::eval(c, st, dd);
+        s = FastSupportT<MESH>::eval(c, st, dd);
     }
     const f3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
     return up ? o - s : s - o;
@@ -208,13 +209,16 @@ __device__ __forceinline__ d3 minkowski64_exact(const d3d_store& st, int a, int 
 
 // The polytope's precision: FP32 search on the FP32 mirror, or FP64 with the
 // reference's supports.
+template <bool MESH>
 __device__ __forceinline__ f3 minkowski_of(const d3d_store& st, int a, int b, f3 d);
+template <bool MESH>
 __device__ __forceinline__ d3 minkowski_of(const d3d_store& st, int a, int b, d3 d) {
     return minkowski64_exact(st, a, b, d);
 }
 
 // The same in FP64 with RefineSupport (polytope vertex chosen by the FP32
 // argmax of the rounded direction).
+template <bool MESH>
 __device__ __forceinline__ d3 minkowski64(const d3d_store& st, int a, int b, d3 d) {
     const bool up = lane_id() & 16;
     Col<double> c;
@@ -231,7 +235,7 @@ __device__ __forceinline__ d3 minkowski64(const d3d_store& st, int a, int b, d3 
                 dd);
         }
     } else {
-        s = RefineSupport::eval(c, st, dd);
+        s = RefineSupportT<MESH>::eval(c, st, dd);
     }
     const d3 o = mk(__shfl_xor_sync(kFull, s.x, 16), __shfl_xor_sync(kFull, s.y, 16), __shfl_xor_sync(kFull, s.z, 16));
     return up ? o - s : s - o;
@@ -248,7 +252,10 @@ __device__ __forceinline__ int warp_excl(int x) {
     return s - x;
 }
 
-__device__ __forceinline__ f3 minkowski_of(const d3d_store& st, int a, int b, f3 d) { return minkowski32(st, a, b, d); }
+template <bool MESH>
+__device__ __forceinline__ f3 minkowski_of(const d3d_store& st, int a, int b, f3 d) {
+    return minkowski32<MESH>(st, a, b, d);
+}
 
 // unit normal and offset of face (a, b, c); false if degenerate
 template <typename T>
@@ -301,7 +308,7 @@ struct Search {
 
 // The expanding-polytope search for one pair in the polytope's precision T
 // (uniform across the warp).
-template <typename T>
+template <typename T, bool MESH>
 __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int b, const double* simplex,
                               const d3d_epa_options& o) {
     const int ln = lane_id();
@@ -381,7 +388,7 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
         ++it;
         const Q4<T> cn = P.fn[cf];
         const V3<T> sd = mk(cn.x, cn.y, cn.z);
-        const V3<T> w = minkowski_of(st, a, b, sd);
+        const V3<T> w = minkowski_of<MESH>(st, a, b, sd);
         scale = maxf2(scale, sqrt_t(dot(w, w)));
         const T eps = maxf2((T)o.epsilon, T(8) * eps_of<T>() * scale);
         if (dot(w, sd) - cn.w < eps) {
@@ -538,15 +545,17 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
 // depth h(n), an upper bound on the penetration depth for every n, and the
 // FP32 normal of the converged face is within the search's tolerance of the
 // optimal direction.
+template <bool MESH>
 __device__ __forceinline__ d3 refine_face(const Poly<float>& P, const d3d_store& st, int a, int b, int f) {
     const Q4<float> fn = P.fn[f];
     d3 n = mk((double)fn.x, (double)fn.y, (double)fn.z);
     n = n * (1.0 / sqrt(dot(n, n)));
-    const d3 w = minkowski64(st, a, b, n);
+    const d3 w = minkowski64<MESH>(st, a, b, n);
     return n * dot(w, n);
 }
 
 // The FP64 polytope's face: its own unit normal and the reference's supports.
+template <bool MESH>
 __device__ __forceinline__ d3 refine_face(const Poly<double>& P, const d3d_store& st, int a, int b, int f) {
     const Q4<double> fn = P.fn[f];
     const d3 n = mk(fn.x, fn.y, fn.z);
@@ -554,7 +563,7 @@ __device__ __forceinline__ d3 refine_face(const Poly<double>& P, const d3d_store
     return n * dot(w, n);
 }
 
-template <typename T, int WARPS>
+template <typename T, int WARPS, bool MESH>
 __global__ void __launch_bounds__(32 * WARPS, 16 / WARPS) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
                                                           const int32_t* __restrict__ i2,
                                                           const int32_t* __restrict__ list, int64_t n,
@@ -578,14 +587,14 @@ __global__ void __launch_bounds__(32 * WARPS, 16 / WARPS) k_epa_warp(d3d_store s
         const int64_t k = list ? list[slot] : slot;
         const int a = i1[k], b = i2[k];
         const double* sx = simplex + 12 * k;
-        const Search R = search_pair(P, st, a, b, sx, o);
+        const Search R = search_pair<T, MESH>(P, st, a, b, sx, o);
         if (R.status == kEpaFallback) {
             if (ln == 0) fallback[atomicAdd(n_fallback, 1ull)] = (int32_t)k;
             __syncwarp();
             continue;
         }
         d3 m = mk(double(NAN), double(NAN), double(NAN));
-        if (R.status == D3D_STATUS_OK || R.status == D3D_STATUS_EPA_NOT_CONVERGED) m = refine_face(P, st, a, b, R.closest);
+        if (R.status == D3D_STATUS_OK || R.status == D3D_STATUS_EPA_NOT_CONVERGED) m = refine_face<MESH>(P, st, a, b, R.closest);
         const int nf = R.status == D3D_STATUS_EPA_DEGENERATE ? 0 : R.live;
         if (ln == 0) {
             mtv[3 * k] = m.x;
@@ -628,12 +637,12 @@ __global__ void __launch_bounds__(32 * WARPS, 16 / WARPS) k_epa_warp(d3d_store s
 
 namespace {
 
-template <typename T, int WARPS>
+template <typename T, int WARPS, bool MESH>
 int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                 const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                 const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
                 int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
-    const void* fn = (const void*)k_epa_warp<T, WARPS>;
+    const void* fn = (const void*)k_epa_warp<T, WARPS, MESH>;
     const int smem = layout_for<T>(o).bytes * WARPS;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e == cudaSuccess)
@@ -644,9 +653,23 @@ int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, co
         return D3D_ERR_CUDA;
     }
     const int blocks = persistent_blocks(fn, 32 * WARPS, n * 32, 0, smem);
-    k_epa_warp<T, WARPS><<<blocks, 32 * WARPS, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o,
-                                                               mtv, status, n_faces, faces, fallback, n_fallback);
+    k_epa_warp<T, WARPS, MESH><<<blocks, 32 * WARPS, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex,
+                                                                     o, mtv, status, n_faces, faces, fallback,
+                                                                     n_fallback);
     return check_launch("d3d_epa (mixed)");
+}
+
+// The kernels without the MeshGraph branch serve stores without meshes.
+template <typename T, int WARPS>
+int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
+    if (store.n_links > 0)
+        return launch_warp<T, WARPS, true>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces,
+                                           faces, fallback, n_fallback, stream);
+    return launch_warp<T, WARPS, false>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces,
+                                        faces, fallback, n_fallback, stream);
 }
 
 }  // namespace

@@ -55,7 +55,7 @@ struct Lists {
 template <int BLOCK>
 constexpr int phase_a_min_blocks() { return BLOCK == 256 ? 2 : 384 / BLOCK; }
 
-template <int BLOCK>
+template <int BLOCK, bool MESH>
 __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixed_a(d3d_store s, const int32_t* __restrict__ i1,
                                                         const int32_t* __restrict__ i2,
                                                         const int32_t* __restrict__ order, int64_t n,
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
             pa_begin(L);
             need = false;
         }
-        const int o = pa_step(L, s, a, b, tol_sq, max_d2, max_iter);
+        const int o = pa_step<MESH>(L, s, a, b, tol_sq, max_d2, max_iter);
         const bool done = o >= 0;
         if (done) hand[pid] = pa_handoff(L, o);
         if (__any_sync(__activemask(), done)) {
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
     }
 }
 
-template <int BLOCK>
+template <int BLOCK, bool MESH>
 __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_t* __restrict__ i1,
                                                         const int32_t* __restrict__ i2, d3d_gjk_options opt,
                                                         const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
             pb_begin(B, v);
             need = false;
         }
-        if (B.mode == PB_FALLBACK || pb_round(B, s, a, b, hand[pid].d, tol_sq, opt, E)) {
+        if (B.mode == PB_FALLBACK || pb_round<MESH>(B, s, a, b, hand[pid].d, tol_sq, opt, E)) {
             GjkResult<double> r;
             if (B.mode != PB_FALLBACK && pb_end(B.g, opt, E, r) == PB_DONE) {
                 r.iters += it_a;
@@ -139,19 +139,30 @@ size_t gjk_mixed_scratch_bytes(int64_t capacity) {
            up(sizeof(Handoff) * (size_t)capacity) + 2 * up(sizeof(int32_t) * (size_t)capacity);
 }
 
-template <int BLOCK>
+template <int BLOCK, bool MESH>
 int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
                  const int64_t* n_dev, const d3d_gjk_options& opt, Handoff* hand, const DistanceOut& o,
                  const Lists& lists, int per_sm, cudaStream_t stream) {
     const float tol_sq = (float)(opt.tolerance * opt.tolerance);
-    k_gjk_mixed_a<BLOCK><<<persistent_blocks((const void*)k_gjk_mixed_a<BLOCK>, BLOCK, n, per_sm), BLOCK, 0,
-                           stream>>>(store, i1, i2, order, n, n_dev, tol_sq, (float)opt.max_distance_squared,
-                                     opt.max_iterations, hand, lists);
+    const void* ka = (const void*)k_gjk_mixed_a<BLOCK, MESH>;
+    k_gjk_mixed_a<BLOCK, MESH><<<persistent_blocks(ka, BLOCK, n, per_sm), BLOCK, 0, stream>>>(
+        store, i1, i2, order, n, n_dev, tol_sq, (float)opt.max_distance_squared, opt.max_iterations, hand, lists);
     int rc = check_launch("d3d_gjk_distance (mixed, FP32 phase)");
     if (rc) return rc;
-    k_gjk_mixed_b<BLOCK><<<persistent_blocks((const void*)k_gjk_mixed_b<BLOCK>, BLOCK, n, per_sm), BLOCK, 0,
-                           stream>>>(store, i1, i2, opt, hand, o, lists);
+    const void* kb = (const void*)k_gjk_mixed_b<BLOCK, MESH>;
+    k_gjk_mixed_b<BLOCK, MESH><<<persistent_blocks(kb, BLOCK, n, per_sm), BLOCK, 0, stream>>>(store, i1, i2, opt,
+                                                                                             hand, o, lists);
     return check_launch("d3d_gjk_distance (mixed, FP64 phase)");
+}
+
+// The kernels without the MeshGraph branch serve stores without meshes.
+template <int BLOCK>
+int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
+                 const int64_t* n_dev, const d3d_gjk_options& opt, Handoff* hand, const DistanceOut& o,
+                 const Lists& lists, int per_sm, cudaStream_t stream) {
+    if (store.n_links > 0)
+        return launch_mixed<BLOCK, true>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, per_sm, stream);
+    return launch_mixed<BLOCK, false>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, per_sm, stream);
 }
 
 int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n, const int64_t* n_dev,

@@ -89,8 +89,10 @@ __device__ __forceinline__ V3<T> margin_fast(const d3d_store& st, const Col<T>& 
     return n2 == T(0) ? s : s + d * (record_margin(st, c) * rsqrt_t(n2));
 }
 
-// FP32 support of the mixed form's search phases.
-struct FastSupport {
+// FP32 support of the mixed form's search phases.  MESH = false leaves out
+// the MeshGraph branch, for kernels launched on stores without meshes.
+template <bool MESH>
+struct FastSupportT {
     static __device__ __forceinline__ f3 base(const Col<float>& c, const d3d_store& s, f3 d) {
         if (c.type == D3D_BOX || c.type == D3D_HULL) {
             if (c.nv < 1) return mk(NAN, NAN, NAN);
@@ -101,7 +103,7 @@ struct FastSupport {
             const f3 ctr = mk(c.t[0], c.t[1], c.t[2]);
             return n2 == 0.f ? ctr + mk(0.f, 0.f, c.p[0]) : ctr + d * (c.p[0] * rsqrtf(n2));
         }
-        if (c.type == D3D_MESH) {
+        if (MESH && c.type == D3D_MESH) {
             if (c.nv < 1) return mk(NAN, NAN, NAN);
             return xform(c.R, c.t, load_vertex(s.verts32, c.off + mesh_climb(c, s, rt_mul(c.R, d))));
         }
@@ -112,9 +114,11 @@ struct FastSupport {
         return margin_fast(s, c, base(c, s, d), d);
     }
 };
+using FastSupport = FastSupportT<true>;
 
 // FP64 support of the refinement phases, with FastSupport's FP32 choices.
-struct RefineSupport {
+template <bool MESH>
+struct RefineSupportT {
     static __device__ __forceinline__ d3 eval(const Col<double>& c, const d3d_store& s, d3 d) {
         return margin_fast(s, c, base(c, s, d), d);
     }
@@ -130,7 +134,7 @@ struct RefineSupport {
             const d3 ctr = mk(c.t[0], c.t[1], c.t[2]);
             return n2 == 0.0 ? ctr + mk(0.0, 0.0, c.p[0]) : ctr + d * (c.p[0] * rsqrt(n2));
         }
-        if (c.type == D3D_MESH) {
+        if (MESH && c.type == D3D_MESH) {
             // the vertex the FP32 climb reaches on the FP32 mirror
             if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
             Col<float> cf;
@@ -138,7 +142,7 @@ struct RefineSupport {
             cf.off = c.off;
             cf.idx = c.idx;
             for (int k = 0; k < 9; ++k) cf.R[k] = __double2float_rn(c.R[k]);
-            return xform(c.R, c.t, load_vertex(s.verts64, c.off + mesh_climb(cf, s, rt_mul(cf.R, df))));
+            return xform(c.R, c.t, load_vertex(s.verts64, c.off + mesh_climb<true>(cf, s, rt_mul(cf.R, df))));
         }
         bool up = false;
         if (c.type == D3D_CAPSULE || c.type == D3D_CYLINDER || c.type == D3D_CONE) {
@@ -160,6 +164,8 @@ struct RefineSupport {
         return xform(c.R, c.t, local_point(c, rt_mul(c.R, d), up));
     }
 };
+
+using RefineSupport = RefineSupportT<true>;
 
 // Duality gap at which the FP64 refinement stops: the distance bracket
 // within 1e-7 of the distance, or within 1e-9 of the scene's scale
@@ -212,13 +218,14 @@ __device__ __forceinline__ void pa_begin(PhaseALoop& L) {
 }
 
 // one iteration; -1 while running, else a PhaseAOutcome
+template <bool MESH = true>
 __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a, int b, float tol_sq, float max_d2,
                                        int max_iter) {
     const JoltEps<float> E = fp32_eps();
     if (L.it >= max_iter) return PA_FAILED;
     ++L.it;
     f3 p, q;
-    pair_supports<float, FastSupport>(s, a, b, L.dir, p, q);
+    pair_supports<float, FastSupportT<MESH>>(s, a, b, L.dir, p, q);
     f3 w = p - q;
     float dd = dot(L.dir, w);
     if (dd < 0.f && dd * dd > L.vl * max_d2) return PA_CLIPPED;
@@ -287,7 +294,7 @@ __device__ __forceinline__ void pb_begin(PhaseB<Rows>& B, float4 v) {
 // ended: g.state is GJK_INTERSECTION or GJK_NO_INTERSECTION (pb_end finishes
 // the pair), or B.mode is PB_FALLBACK (clipped, iteration bound, failed
 // replay).
-template <typename Rows>
+template <bool MESH = true, typename Rows>
 __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, int a, int b,
                                          const float4* __restrict__ dirs, double tol_sq, const d3d_gjk_options& opt,
                                          const JoltEps<double>& E) {
@@ -305,7 +312,7 @@ __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, in
         ++g.it;
     }
     d3 p, q;
-    pair_supports<double, RefineSupport>(s, a, b, d, p, q);
+    pair_supports<double, RefineSupportT<MESH>>(s, a, b, d, p, q);
     const d3 w = p - q;
     if (!replay) {
         const double dd = dot(g.dir, w);

@@ -38,7 +38,7 @@ class EpaOptions(ctypes.Structure):
 
 class MprOptions(ctypes.Structure):
     _fields_ = [("tolerance", c_double), ("max_iterations", c_int32), ("refine_limit", c_int32),
-                ("penetration", c_int32), ("reserved", c_int32)]
+                ("penetration", c_int32), ("precision", c_int32)]
 
 
 class ServerOptions(ctypes.Structure):

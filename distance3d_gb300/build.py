@@ -44,6 +44,7 @@ UNITS = [
     ("robot.cu", ["-fmad=false"]),
     ("bvh.cu", []),
     ("mpr.cu", ["-fmad=false"]),
+    ("mpr_mixed.cu", ["-fmad=true"]),
 ]
 
 

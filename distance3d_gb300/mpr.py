@@ -11,7 +11,9 @@ Drop-in functions:
   not intersect.
 
 Batched function (new): ``mpr_batch`` takes a ``ColliderStore`` and two index
-arrays and returns device tensors.  FP64, the reference's results bit for bit.
+arrays and returns device tensors.  ``precision="fp64"`` (the default and the
+drop-ins) gives the reference's results bit for bit; ``precision="mixed"``
+searches the portal in FP32 and evaluates the final portal in FP64.
 """
 import ctypes
 
@@ -22,10 +24,11 @@ from .collider_set import ColliderSet
 from .store import ColliderStore, as_index, _ptr
 
 DEFAULT_REFINE_LIMIT = 10000
+_PRECISIONS = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}
 
 
 def mpr_batch(store, i1, i2, *, mpr_tolerance=0.0001, max_iterations=100, penetration=True,
-              refine_limit=DEFAULT_REFINE_LIMIT):
+              refine_limit=DEFAULT_REFINE_LIMIT, precision="fp64"):
     """MPR for pairs (i1[k], i2[k]) of ``store``.
 
     Returns a dict of device tensors: ``hit`` (n,) bool and ``status`` (n,)
@@ -33,7 +36,11 @@ def mpr_batch(store, i1, i2, *, mpr_tolerance=0.0001, max_iterations=100, penetr
     ``pos`` (n,3) float64 (NaN where the pair does not intersect).
     ``status`` is ``STATUS_MAX_ITER`` where the portal refinement, which the
     reference runs without bound, took more than ``refine_limit`` steps.
+    ``precision="mixed"`` runs the portal search in FP32 (pairs whose FP32
+    refinement hits the bound rerun in FP64).
     """
+    if precision not in _PRECISIONS:
+        raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
     dev = store.device
     with torch.cuda.device(dev):
         a = as_index(i1, dev)
@@ -48,7 +55,8 @@ def mpr_batch(store, i1, i2, *, mpr_tolerance=0.0001, max_iterations=100, penetr
             out.update(depth=torch.empty(n, dtype=torch.float64, device=dev),
                        dir=torch.empty((n, 3), dtype=torch.float64, device=dev),
                        pos=torch.empty((n, 3), dtype=torch.float64, device=dev))
-        opt = _lib.MprOptions(float(mpr_tolerance), int(max_iterations), int(refine_limit), 1 if penetration else 0, 0)
+        opt = _lib.MprOptions(float(mpr_tolerance), int(max_iterations), int(refine_limit), 1 if penetration else 0,
+                              _PRECISIONS[precision])
         _lib.check(_lib.load().d3d_mpr(store.view, _ptr(a), _ptr(b), n, ctypes.byref(opt), _ptr(hit),
                                        _ptr(out.get("depth")), _ptr(out.get("dir")), _ptr(out.get("pos")),
                                        _ptr(status), store.stream()))

@@ -212,7 +212,11 @@ int d3d_collide(const d3d_store* store, const int32_t* i1, const int32_t* i2, in
                 void* stream);
 
 /* Minkowski portal refinement (MPR).  Replaces mpr.mpr_intersection and
- * mpr.mpr_penetration (mpr.py:21-110), FP64, bit for bit: hit[k] for pairs
+ * mpr.mpr_penetration (mpr.py:21-110).  D3D_PRECISION_FP64 gives the
+ * reference's results bit for bit; D3D_PRECISION_MIXED searches the portal
+ * in FP32 on the FP32 mirror and evaluates the final portal in FP64 along the
+ * FP32 search directions (depth, direction and contact position with the
+ * reference's formulas).  hit[k] for pairs
  * (i1[k], i2[k]); with options->penetration also depth[k], dir[k][3] (unit
  * or zero vector: adding depth * dir to the second collider separates them)
  * and pos[k][3] (contact position), NaN where the reference returns None.
@@ -224,7 +228,7 @@ typedef struct d3d_mpr_options {
     int32_t max_iterations;  /* 100: portal discovery and penetration search */
     int32_t refine_limit;    /* 10000: bound on the refinement loop */
     int32_t penetration;     /* 1: mpr_penetration, 0: mpr_intersection */
-    int32_t reserved;        /* 0 */
+    int32_t precision;       /* D3D_PRECISION_FP64 or D3D_PRECISION_MIXED */
 } d3d_mpr_options;
 int d3d_mpr(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n, const d3d_mpr_options* options,
             int8_t* hit, double* depth, double* dir, double* pos, int8_t* status, void* stream);

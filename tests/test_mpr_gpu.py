@@ -83,3 +83,60 @@ def test_drop_in_mpr():
     far = colliders.Sphere(np.array([5.0, 0.0, 0.0]), 0.5)
     assert mpr.mpr_penetration(s1, far) == (False, None, None, None)
     assert not mpr.mpr_intersection(s1, far)
+
+
+FLAG_MARGIN = 1e-6
+
+
+def rel_depth_err(a, b):
+    both = a["hit"] & b["hit"]
+    return np.abs(a["depth"][both] - b["depth"][both]) / np.maximum(1.0, b["depth"][both]), both
+
+
+@pytest.mark.parametrize("types", [workloads.ALL_TYPES, workloads.ALL_TYPES_MESH])
+def test_mixed_mpr_against_fp64(types):
+    """Mixed MPR against the plain FP64 MPR.
+
+    Flags: identical wherever the pair is more than 1e-6 from touching (FP64
+    GJK distance, FP64 EPA depth).  Depths: MPR's depth is the distance to
+    the final portal face, and which face the search ends on is sensitive to
+    its inputs -- moving every collider by 1e-9 changes the FP64 depth by
+    more than 1e-5 (relative to max(1, depth)) on about 2% of the pairs, by
+    up to 1e-2.  The mixed depths must stay within a few times that spread
+    (quantiles of the relative error against those of the moved FP64 run).
+    Directions are unit or zero vectors; the intersection-only flags equal
+    the penetration form's."""
+    from distance3d_gb300.collider_set import ColliderSet
+    from distance3d_gb300.epa import epa_batch
+    from distance3d_gb300.gjk import gjk_distance_batch
+    cs, i1, i2 = workloads.pairs_all_types(40000, seed=53, types=types)
+    st = ColliderStore(cs)
+    f = host(mpr_batch(st, i1, i2))
+    m = host(mpr_batch(st, i1, i2, precision="mixed"))
+    g = host(gjk_distance_batch(st, i1, i2))
+    assert np.all(m["status"] == 0)
+    # flags: wherever FP64 GJK separates the pair by more than 1e-6, or FP64
+    # EPA finds it more than 1e-6 deep, both forms decide alike (the
+    # reference's MPR itself misses a few pairs that EPA finds deep)
+    sep = g["dist"] > FLAG_MARGIN
+    full = np.flatnonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4))
+    e = host(epa_batch(st, i1[full], i2[full], g["simplex"][full], max_faces=256, max_loose_edges=128))
+    deep = np.zeros(len(i1), bool)
+    deep[full] = (e["status"] == 0) & (np.linalg.norm(e["mtv"], axis=1) > FLAG_MARGIN)
+    assert np.array_equal(m["hit"][sep | deep], f["hit"][sep | deep])
+    assert not np.any(m["hit"][sep])
+    poses = cs.poses.copy()
+    poses[:, 9:] += 1e-9
+    verts = cs.vertices.copy()
+    verts[:, :3] += 1e-9
+    moved = ColliderSet(cs.types, poses, cs.params, cs.hull_offset, cs.hull_count, verts, cs.links)
+    q = host(mpr_batch(ColliderStore(moved), i1, i2))
+    err_m, both = rel_depth_err(m, f)
+    err_q, _ = rel_depth_err(q, f)
+    assert np.quantile(err_q, 0.999) > 1e-4  # the FP64 form's own sensitivity
+    for p, floor in ((0.99, 1e-3), (0.999, 1e-2)):
+        assert np.quantile(err_m, p) <= max(floor, 5 * np.quantile(err_q, p)), (p, np.quantile(err_m, p))
+    nd = np.linalg.norm(m["dir"][both], axis=1)
+    assert np.all((np.abs(nd - 1.0) < 1e-12) | (nd == 0.0))
+    mi = host(mpr_batch(st, i1, i2, precision="mixed", penetration=False))
+    assert np.array_equal(mi["hit"], m["hit"])

@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch parameters (profiling runs)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the broad+narrow, robot and MPR sections (profiling runs)")
+    ap.add_argument("--mpr-only", action="store_true",
+                    help="run only the MPR section on the workload, without its CPU leg (profiling runs)")
     return ap.parse_args()
 
 
@@ -410,7 +412,7 @@ def robot_report(dev, n_configs=16384, seed=0, reps=3):
     return out
 
 
-def mpr_report(store, cs, i1_np, i2_np, dev, reps=3, check_pairs=20000, cpu_pairs=262144):
+def mpr_report(store, cs, i1_np, i2_np, dev, reps=3, check_pairs=20000, cpu_pairs=262144, cpu=True):
     """MPR on the batched workload: device time for all pairs (best of `reps`
     after a warm-up), both forms (plain FP64, the reference bit for bit; mixed)
     and both calls (mpr_penetration, mpr_intersection); the oracle (C
@@ -478,6 +480,8 @@ def mpr_report(store, cs, i1_np, i2_np, dev, reps=3, check_pairs=20000, cpu_pair
         np.array_equal(got["hit"], ref["hit"]) and np.array_equal(got["status"], ref["status"])
         and all(np.array_equal(got[key], ref[key], equal_nan=True) for key in ("depth", "dir", "pos")))
     out["check_pairs"] = check_pairs
+    if not cpu:
+        return out
     t0 = time.perf_counter()
     oracle.mpr(cs, i1_np[:cpu_pairs], i2_np[:cpu_pairs])
     cpu_s = time.perf_counter() - t0
@@ -503,6 +507,11 @@ def run_ours(args):
     cs, i1_np, i2_np = make_workload(args.pairs, rank)
     n = len(i1_np)
     store = ColliderStore(cs, device=dev)
+    if args.mpr_only:
+        if rank == 0:
+            print(json.dumps({"mpr": mpr_report(store, cs, i1_np, i2_np, dev, reps=max(1, args.steps),
+                                                check_pairs=min(n, 20000), cpu=False)}), flush=True)
+        return 0
     i1 = torch.as_tensor(i1_np, device=dev)
     i2 = torch.as_tensor(i2_np, device=dev)
     stream = torch.cuda.current_stream(dev)

@@ -38,6 +38,14 @@ Inputs come from ``distance3d_gb300.workloads`` (seeded).  Outputs:
   here every support call restarts from the mesh's start vertex, the
   semantics of the GPU path, so that the fixture does not depend on the
   order of the calls.
+* ``edge.npz``        -- degenerate and boundary colliders built one by one
+  (zero radii and lengths, flat boxes, axis-aligned and tied disk normals, a
+  zero normal, a zero-height cone, point / segment / coplanar hulls, a
+  tetrahedron and a cube MeshGraph with tied vertices, margins of 0): their
+  supports along axis, diagonal, tiny and zero directions, their AABBs, and
+  GJK, EPA and MPR on every pair of the colliders whose supports are finite.
+  Calls on which the reference raises its sanity assertion are recorded as
+  such (status 2).
 * ``aabb_tree.npz``   -- a 400-collider scene: reference AabbTree self overlap
   (both orders, i == j dropped, reduced to i < j), brute force
   ``all_aabbs_overlap``, BoundingVolumeHierarchy.aabb_overlapping_with_self on
@@ -344,13 +352,149 @@ def make_mesh(mods, workloads):
     np.savez_compressed(os.path.join(HERE, "mpr_mesh10.npz"), **mpr_fixture(cols, gf))
 
 
+def edge_colliders(colliders):
+    """(reference collider objects, mask of those with finite supports)."""
+    def pose(t=(0.0, 0.0, 0.0), axis=None, angle=0.0):
+        m = np.eye(4)
+        if axis is not None:
+            a = np.asarray(axis, dtype=float) / np.linalg.norm(axis)
+            K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+            m[:3, :3] = np.eye(3) + np.sin(angle) * K + (1 - np.cos(angle)) * K @ K
+        m[:3, 3] = t
+        return m
+    C = colliders
+    cube_v = np.array([[x, y, z] for x in (-0.5, 0.5) for y in (-0.5, 0.5) for z in (-0.5, 0.5)])
+    cube_t = np.array([[0, 1, 3], [0, 3, 2], [4, 6, 7], [4, 7, 5], [0, 4, 5], [0, 5, 1],
+                       [2, 3, 7], [2, 7, 6], [0, 2, 6], [0, 6, 4], [1, 5, 7], [1, 7, 3]])
+    tet_v = np.array([[0.0, 0.0, 0.0], [0.4, 0.0, 0.0], [0.0, 0.4, 0.0], [0.0, 0.0, 0.4]])
+    tet_t = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 3]])
+    finite = []
+    out = []
+
+    def add(c, ok=True):
+        out.append(c)
+        finite.append(ok)
+    add(C.Sphere(np.zeros(3), 0.0))
+    add(C.Sphere(np.array([0.2, -0.1, 0.3]), 0.5))
+    add(C.Capsule(pose((0.1, 0.0, 0.0)), 0.2, 0.0))
+    add(C.Capsule(pose((0.0, 0.3, 0.0), (1, 0, 0), 0.7), 0.0, 0.6))
+    add(C.Cylinder(pose((0.0, 0.0, 0.2)), 0.0, 0.5))
+    add(C.Cylinder(pose((-0.2, 0.0, 0.0), (0, 1, 0), 1.1), 0.3, 0.0))
+    add(C.Box(pose((0.0, 0.1, 0.0)), np.array([0.6, 0.0, 0.4])))
+    add(C.Box(pose((0.3, 0.3, 0.3), (1, 1, 1), 0.5), np.array([0.2, 0.2, 0.2])))
+    add(C.Ellipsoid(pose((0.0, -0.2, 0.1), (0, 0, 1), 0.3), np.array([0.3, 0.0, 0.2])))
+    for n in ((0, 0, 1), (1, 0, 0), (0, 1, 0), (1, 1, 0), (0, 0, -1), (-1, 0, 0), (1, -1, 1)):
+        nn = np.asarray(n, dtype=float)
+        add(C.Disk(np.array([0.05, 0.1, -0.05]), 0.35, nn / np.linalg.norm(nn)))
+    add(C.Disk(np.zeros(3), 0.0, np.array([0.0, 0.0, 1.0])))
+    add(C.Disk(np.zeros(3), 0.3, np.zeros(3)), ok=False)
+    add(C.Ellipse(np.array([0.1, 0.0, 0.0]), np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0]]), np.array([0.3, 0.0])))
+    add(C.Ellipse(np.zeros(3), np.array([[0.6, 0.8, 0.0], [0.0, 0.0, 1.0]]), np.array([0.25, 0.4])))
+    add(C.Cone(pose((0.0, 0.0, -0.3)), 0.0, 0.5))
+    add(C.Cone(pose((0.1, 0.1, 0.0), (1, 0, 0), 3.0), 0.3, 0.0))
+    add(C.Cone(pose((0.0, 0.0, 0.0), (0, 1, 1), 0.4), 0.25, 0.6))
+    add(C.ConvexHullVertices(np.array([[0.1, 0.2, 0.3]])))
+    add(C.ConvexHullVertices(np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]])))
+    add(C.ConvexHullVertices(np.array([[0.0, 0.0, 0.1], [0.4, 0.0, 0.1], [0.0, 0.4, 0.1], [0.4, 0.4, 0.1]])))
+    add(C.MeshGraph(pose((0.0, 0.0, 0.0)), tet_v, tet_t))
+    add(C.MeshGraph(pose((0.1, -0.1, 0.2), (0, 0, 1), 0.25), cube_v * 0.6, cube_t))
+    add(C.Margin(C.Sphere(np.zeros(3), 0.2), 0.0))
+    add(C.Margin(C.Box(pose(), np.array([0.3, 0.3, 0.3])), 0.2))
+    add(C.Margin(C.ConvexHullVertices(np.array([[0.0, 0.0, 0.0]])), 0.5))
+    add(C.Margin(C.Disk(np.zeros(3), 0.3, np.array([0.0, 1.0, 0.0])), 0.1))
+    add(C.Margin(C.MeshGraph(pose((0.0, 0.2, 0.0)), tet_v, tet_t), 0.05))
+    add(C.Margin(C.Cone(pose(), 0.2, 0.4), 0.0))
+    for c in out:  # MeshGraph supports restart from the start vertex in every call
+        inner = c.collider if type(c).__name__ == "Margin" else c
+        if type(inner).__name__ == "MeshGraph":
+            m, start = inner, np.min(inner.triangles)
+
+            def support_function(d, m=m, start=start):
+                m._support_function.first_idx = start
+                return m._support_function(d)[1]
+            m.support_function = support_function
+    return out, np.array(finite)
+
+
+def make_edge(mods, workloads):
+    import signal
+    from distance3d_gb300.collider_set import ColliderSet
+    gjk, epa, colliders, _, _ = mods
+    mpr = import_mpr()
+    cols, finite = edge_colliders(colliders)
+    cs = ColliderSet.from_colliders(cols)
+    dirs = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1], [1, 1, 1],
+                     [-1, 1, 0], [0.3, -0.4, 1.2], [1e-300, 0, 0], [0, 0, 0], [2.5, 1.0, -0.5],
+                     [0, 1, 1], [1, 1, 0]], dtype=float)
+    supports = np.array([[c.support_function(d.copy()) for d in dirs] for c in cols])
+    aabbs = np.stack([c.aabb() for c in cols])
+    ok = np.flatnonzero(finite)
+    i1, i2 = np.triu_indices(len(ok), k=1)
+    i1, i2 = ok[i1].astype(np.int32), ok[i2].astype(np.int32)
+
+    def timeout(signum, frame):
+        raise TimeoutError()
+    signal.signal(signal.SIGALRM, timeout)
+    n = len(i1)
+    keep = np.ones(n, bool)
+    sanity = np.zeros(n, bool)
+    dist = np.full(n, np.nan)
+    cp1 = np.full((n, 3), np.nan)
+    cp2 = np.full((n, 3), np.nan)
+    simplex = np.full((n, 4, 3), np.nan)
+    n_simplex = np.zeros(n, np.int8)
+    iters = np.zeros(n, np.int32)
+    hit = np.zeros(n, bool)
+    mhit = np.zeros(n, bool)
+    mhit_i = np.zeros(n, bool)
+    mdepth = np.full(n, np.nan)
+    mdir = np.full((n, 3), np.nan)
+    mpos = np.full((n, 3), np.nan)
+    for k in range(n):
+        c1, c2 = cols[i1[k]], cols[i2[k]]
+        signal.alarm(5)
+        try:
+            d, a, b, Y, m, it = ref_distance(gjk, c1, c2)
+            try:
+                gjk.gjk_distance_jolt(c1, c2)
+            except AssertionError:
+                sanity[k] = True
+            dist[k], simplex[k], n_simplex[k], iters[k] = d, Y, m, it
+            if a is not None:
+                cp1[k], cp2[k] = a, b
+            hit[k] = gjk.gjk_intersection_jolt(c1, c2)
+            h, dd, p, c = mpr.mpr_penetration(c1, c2)
+            mhit[k] = h
+            if dd is not None:
+                mdepth[k], mdir[k], mpos[k] = dd, p, c
+            mhit_i[k] = mpr.mpr_intersection(c1, c2)
+        except TimeoutError:
+            keep[k] = False
+        finally:
+            signal.alarm(0)
+    print(f"  edge: {len(cols)} colliders, {n} pairs, {np.sum(~keep)} dropped (reference did not return in 5 s), "
+          f"{sanity.sum()} sanity assertions, {hit.sum()} intersecting")
+    i1, i2 = i1[keep], i2[keep]
+    gf = dict(types=cs.types, poses=cs.poses, params=cs.params, hull_offset=cs.hull_offset,
+              hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), links=cs.links, i1=i1, i2=i2,
+              dist=dist[keep], cp1=cp1[keep], cp2=cp2[keep], simplex=simplex[keep], n_simplex=n_simplex[keep],
+              iterations=iters[keep], intersect=hit[keep], sanity=sanity[keep], aabbs=aabbs,
+              support_dirs=dirs, supports=supports, finite=finite,
+              mpr_hit=mhit[keep], mpr_depth=mdepth[keep], mpr_dir=mdir[keep], mpr_pos=mpos[keep],
+              mpr_hit_intersection=mhit_i[keep])
+    ef = epa_fixture(mods, cols, gf)
+    gf.update({"epa_" + key: v for key, v in ef.items()})
+    np.savez_compressed(os.path.join(HERE, "edge.npz"), **gf)
+
+
 def make_tree(mods, workloads):
     print("aabb tree scene")
     scene = workloads.scene_mixed_six(400, seed=4321, half_width=3.0)
     np.savez_compressed(os.path.join(HERE, "aabb_tree.npz"), **tree_fixture(mods, scene))
 
 
-FIXTURES = {"mixed6": make_mixed6, "scb": make_scb, "all9": make_all9, "mesh10": make_mesh, "tree": make_tree}
+FIXTURES = {"mixed6": make_mixed6, "scb": make_scb, "all9": make_all9, "mesh10": make_mesh, "edge": make_edge,
+            "tree": make_tree}
 
 
 def main(ref_root, names):

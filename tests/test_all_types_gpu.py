@@ -181,3 +181,38 @@ def test_collide_all_types_equals_separate_calls():
             assert np.array_equal(r[k], g[k], equal_nan=True), k
         assert np.array_equal(r["epa_status"][hit], e["status"])
         assert np.array_equal(r["mtv"][hit], e["mtv"], equal_nan=True)
+
+
+def test_edge_colliders_match_reference(golden):
+    """Degenerate and boundary colliders on the GPU, FP64 form: supports,
+    AABBs, GJK, intersection, EPA and MPR equal the reference's."""
+    from distance3d_gb300.mpr import mpr_batch
+    g, cs = golden("edge")
+    st = ColliderStore(cs)
+    n, k = len(cs), len(g["support_dirs"])
+    idx = np.repeat(np.arange(n), k).astype(np.int32)
+    got = st.support(idx, np.tile(g["support_dirs"], (n, 1))).cpu().numpy().reshape(n, k, 3)
+    assert np.array_equal(got, g["supports"], equal_nan=True)
+    assert np.array_equal(st.aabbs().cpu().numpy(), g["aabbs"], equal_nan=True)
+    r = host(gjk_distance_batch(st, g["i1"], g["i2"]))
+    ok = ~g["sanity"]
+    assert np.all(r["status"][ok] == 0)
+    for key in ("dist", "n_simplex", "iterations"):
+        assert np.array_equal(r[key][ok], g[key][ok]), key
+    assert np.array_equal(r["cp1"][ok], g["cp1"][ok], equal_nan=True)
+    assert np.array_equal(r["cp2"][ok], g["cp2"][ok], equal_nan=True)
+    h = gjk_intersection_batch(st, g["i1"], g["i2"])["hit"].cpu().numpy()
+    assert np.array_equal(h, g["intersect"])
+    m = host(mpr_batch(st, g["i1"], g["i2"]))
+    assert np.array_equal(m["hit"], g["mpr_hit"])
+    for key in ("depth", "dir", "pos"):
+        assert np.array_equal(m[key], g["mpr_" + key], equal_nan=True), key
+    p = g["epa_pair"]
+    for tag, kw in (("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))):
+        e = host(epa_batch(st, g["i1"][p], g["i2"][p], g["simplex"][p], **kw))
+        s = g[f"epa_status_{tag}"]
+        assert np.array_equal(e["status"], s)
+        assert np.array_equal(e["mtv"][s == 0], g[f"epa_mtv_{tag}"][s == 0])
+    # the mixed forms on the same pairs: GJK within tolerance, MPR flags
+    mg = host(gjk_distance_batch(st, g["i1"], g["i2"], precision="mixed"))
+    mixed_check(mg, g, cs, g["i1"], g["i2"])

@@ -92,3 +92,35 @@ def test_mpr_bit_exact(golden, fixture):
     assert np.array_equal(r["pos"], m["pos"], equal_nan=True)
     ri = oracle.mpr(cs, m["i1"], m["i2"], penetration=False)
     assert np.array_equal(ri["hit"], m["hit_intersection"])
+
+
+def test_edge_colliders_bit_exact(golden):
+    """Degenerate and boundary colliders (zero sizes, tied and zero disk
+    normals, flat and point hulls, tied mesh vertices, margins of 0):
+    supports, AABBs (NaN where the reference's are), GJK, EPA and MPR."""
+    g, cs = golden("edge")
+    n = len(cs)
+    k = len(g["support_dirs"])
+    got = oracle.support_batch(cs, np.repeat(np.arange(n), k), np.tile(g["support_dirs"], (n, 1))).reshape(n, k, 3)
+    assert np.array_equal(got, g["supports"], equal_nan=True)
+    assert np.array_equal(oracle.aabbs(cs), g["aabbs"], equal_nan=True)
+    r = oracle.gjk_distance(cs, g["i1"], g["i2"])
+    ok = ~g["sanity"]
+    assert np.array_equal(r["status"][~ok], np.full((~ok).sum(), 2))
+    for key in ("dist", "n_simplex", "iterations"):
+        assert np.array_equal(r[key][ok], g[key][ok]), key
+    assert np.array_equal(r["cp1"][ok], g["cp1"][ok], equal_nan=True)
+    written = ~np.isnan(g["simplex"])
+    assert np.array_equal(r["simplex"][written], g["simplex"][written])
+    assert np.array_equal(oracle.gjk_intersection(cs, g["i1"], g["i2"])["hit"], g["intersect"])
+    m = oracle.mpr(cs, g["i1"], g["i2"])
+    assert np.array_equal(m["hit"], g["mpr_hit"])
+    for key in ("depth", "dir", "pos"):
+        assert np.array_equal(m[key], g["mpr_" + key], equal_nan=True), key
+    assert np.array_equal(oracle.mpr(cs, g["i1"], g["i2"], penetration=False)["hit"], g["mpr_hit_intersection"])
+    p = g["epa_pair"]
+    for tag, kw in (("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))):
+        e = oracle.epa(cs, g["i1"][p], g["i2"][p], g["simplex"][p], **kw)
+        st = g[f"epa_status_{tag}"]
+        assert np.array_equal(e["status"], st)
+        assert np.array_equal(e["mtv"][st == 0], g[f"epa_mtv_{tag}"][st == 0])

@@ -449,30 +449,38 @@ def mpr_report(store, cs, i1_np, i2_np, dev, reps=3, check_pairs=20000, cpu_pair
     f, m = res["fp64"], res["mixed"]
     both = f["hit"] & m["hit"]
     err = np.abs(m["depth"][both] - f["depth"][both]) / np.maximum(1.0, f["depth"][both])
-    # where the flags differ: how far the pair is from touching, by FP64 GJK
-    # (separation) and FP64 EPA (penetration depth)
+    # where the flags differ: how far each pair is from touching (FP64 GJK
+    # separation, FP64 EPA depth), and which form agrees with GJK there
     from distance3d_gb300.epa import epa_batch
     from distance3d_gb300.gjk import gjk_distance_batch
     diff = np.flatnonzero(f["hit"] != m["hit"]).astype(np.int32)
-    margin = 0.0
+    mixed_wrong_margin, mixed_right, fp64_right = 0.0, 0, 0
     if len(diff):
         g = {k: v.cpu().numpy() for k, v in gjk_distance_batch(store, i1_np[diff], i2_np[diff]).items()}
-        margin = float(np.max(g["dist"]))
+        margin = np.where(g["dist"] > 0.0, g["dist"], 0.0)
         full = np.flatnonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4))
         if len(full):
             e = {k: v.cpu().numpy() for k, v in epa_batch(store, i1_np[diff][full], i2_np[diff][full],
                                                              g["simplex"][full], **EPA_KW).items()}
             ok = e["status"] == 0
-            if ok.any():
-                margin = max(margin, float(np.max(np.linalg.norm(e["mtv"][ok], axis=1))))
+            margin[full[ok]] = np.linalg.norm(e["mtv"][ok], axis=1)
+        gjk_hit = g["dist"] == 0.0
+        mixed_ok = m["hit"][diff] == gjk_hit
+        mixed_right, fp64_right = int(mixed_ok.sum()), int((f["hit"][diff] == gjk_hit).sum())
+        if (~mixed_ok).any():
+            mixed_wrong_margin = float(margin[~mixed_ok].max())
     out["mixed_accuracy"] = {
         "flags_differ": int(len(diff)),
-        "flags_differ_max_distance_from_touching": margin,
+        "flags_differ_mixed_agrees_with_gjk": mixed_right,
+        "flags_differ_fp64_agrees_with_gjk": fp64_right,
+        "flags_differ_mixed_wrong_max_distance_from_touching": mixed_wrong_margin,
         "depth_rel_err_frac_above_1e-5": float(np.mean(err > 1e-5)),
         "depth_rel_err_p99": float(np.quantile(err, 0.99)),
         "depth_rel_err_p999": float(np.quantile(err, 0.999)),
-        "note": "MPR's depth depends on the final portal face; moving every collider by 1e-9 changes "
-                "the FP64 depth by >1e-5 on ~2% of pairs (tests/test_mpr_gpu.py)"}
+        "note": "MPR's flag is defined up to its tolerance (1e-4): within it, a pair is a hit if the "
+                "portal can still expand by more than the tolerance; MPR's depth depends on the final "
+                "portal face: moving every collider by 1e-9 changes the FP64 depth by >1e-5 on ~2% "
+                "of pairs (tests/test_mpr_gpu.py)"}
     k = np.arange(check_pairs)
     got = {key: v[:check_pairs].cpu().numpy() for key, v in mpr_batch(store, i1[:check_pairs], i2[:check_pairs]).items()}
     ref = oracle.mpr(cs, i1_np[k], i2_np[k])

@@ -38,8 +38,8 @@ EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 # DRAM bytes per pair of the mixed kernels from one ncu capture of the
 # 131,072-pair workload (k_gjk_mixed_a + k_gjk_mixed_b per pair; k_epa_warp
 # per EPA pair, 38,718 of them); traffic grows in proportion to the pairs
-NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78149376 + 3651840 + 139727616 + 12017664) / 131072,
-                           "epa_mixed": (46287616 + 118784) / 38718}
+NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78166272 + 3525888 + 141310208 + 12496128) / 131072,
+                           "epa_mixed": (46292224 + 158208) / 38814}
 # this library's kernels per timed mixed step (one graph replay): k_pair_keys,
 # k_gjk_mixed_a, k_gjk_mixed_b, k_gjk_distance_f64 (fallback list),
 # k_epa_select, k_epa_warp<float>, k_epa_warp<double> (fallback list), k_epa

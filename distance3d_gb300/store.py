@@ -119,7 +119,6 @@ class ColliderStore:
                                           _ptr(offs), _ptr(cnts), nv_hull, _stream(dev)))
 
     def _init_pinned(self, p, device):
-        lib = _lib.load()
         self.device = torch.device(device)
         if self.device.index is None:
             self.device = torch.device("cuda", torch.cuda.current_device())
@@ -134,20 +133,38 @@ class ColliderStore:
             self.meta = torch.empty((max(n, 1), 4), dtype=torch.int32, device=dev)
             self.verts64 = torch.empty((max(nv, 1), 4), dtype=torch.float64, device=dev)
             self.verts32 = torch.empty((max(nv, 1), 4), dtype=torch.float32, device=dev)
-            if p.n_hull_vertices:
-                self.verts64[:p.n_hull_vertices].copy_(p.vertices, non_blocking=True)
-            self.links = p.links.to(dev, non_blocking=True) if p.links.numel() else None
-            types = p.types.to(dev, non_blocking=True)
-            poses = p.poses.to(dev, non_blocking=True)
-            params = p.params.to(dev, non_blocking=True)
-            offs = p.offsets.to(dev, non_blocking=True)
-            cnts = p.counts.to(dev, non_blocking=True)
+            self.links = torch.empty(p.links.numel(), dtype=torch.int32, device=dev) if p.links.numel() else None
+            self._staging = {k: torch.empty(getattr(p, k).shape, dtype=getattr(p, k).dtype, device=dev)
+                             for k in ("types", "poses", "params", "offsets", "counts")}
             self._view = _lib.D3DStore(n, nv, self.rec64.data_ptr(), self.rec32.data_ptr(),
                                        self.meta.data_ptr(), self.verts64.data_ptr(), self.verts32.data_ptr(),
                                        self.links.data_ptr() if self.links is not None else None,
                                        p.links.numel())
-            _lib.check(lib.d3d_store_pack(ctypes.byref(self._view), _ptr(types), _ptr(poses), _ptr(params),
-                                          _ptr(offs), _ptr(cnts), p.n_hull_vertices, _stream(dev)))
+        self._shape = (p.n, p.n_vertices, p.n_hull_vertices, p.links.numel())
+        self.update(p)
+
+    def update(self, p):
+        """Copy the colliders of a PinnedColliderSet of this store's shape
+        (same collider, vertex and link counts, the same boxes) into this
+        store and pack them again, asynchronously on the current stream (the
+        packing validates the records and synchronises with that stream).
+        The store's device buffers stay the same, so CUDA graphs captured on
+        it (``serve.CollisionBatch``) serve the new colliders."""
+        if not isinstance(p, PinnedColliderSet) or getattr(self, "_shape", None) != (
+                p.n, p.n_vertices, p.n_hull_vertices, p.links.numel()):
+            raise ValueError("update() needs a PinnedColliderSet of the shape this store was built from")
+        dev = self.device
+        with torch.cuda.device(dev):
+            if p.n_hull_vertices:
+                self.verts64[:p.n_hull_vertices].copy_(p.vertices, non_blocking=True)
+            if self.links is not None:
+                self.links.copy_(p.links, non_blocking=True)
+            st = self._staging
+            for k in st:
+                st[k].copy_(getattr(p, k), non_blocking=True)
+            _lib.check(_lib.load().d3d_store_pack(ctypes.byref(self._view), _ptr(st["types"]), _ptr(st["poses"]),
+                                                  _ptr(st["params"]), _ptr(st["offsets"]), _ptr(st["counts"]),
+                                                  p.n_hull_vertices, _stream(dev)))
 
     def __len__(self):
         return self.n_colliders

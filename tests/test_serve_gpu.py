@@ -121,3 +121,32 @@ def test_native_server_rejects_bad_pairs(scene):
         assert out["dist"].shape == (10,)
     finally:
         srv.close()
+
+
+def test_store_update_keeps_graphs_valid():
+    """ColliderStore.update packs new colliders of the same shape into the
+    same device buffers: a CollisionBatch captured before the update gives
+    what a fresh store gives for the new colliders."""
+    from distance3d_gb300.store import PinnedColliderSet
+    from distance3d_gb300.collider_set import ColliderSet
+    a_cs, i1, i2 = workloads.pairs_mixed_six(5000, seed=61, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    # the second colliders of every pair moved by 0.05 along x: same shape, new distances
+    poses, verts = a_cs.poses.copy(), a_cs.vertices.copy()
+    poses[1::2, 9] += 0.05
+    moved = np.zeros(len(verts), bool)
+    for c in range(1, len(a_cs), 2):
+        if a_cs.hull_offset[c] >= 0 and a_cs.types[c] == 5:
+            moved[a_cs.hull_offset[c]:a_cs.hull_offset[c] + a_cs.hull_count[c]] = True
+    verts[moved, 0] += 0.05
+    b_cs = ColliderSet(a_cs.types, poses, a_cs.params, a_cs.hull_offset, a_cs.hull_count, verts)
+    st = ColliderStore(PinnedColliderSet(a_cs))
+    batch = CollisionBatch(st, 5000, precision="mixed", epa_kw=EPA_KW, graphs=True)
+    ra = batch.run(i1, i2)
+    st.update(PinnedColliderSet(b_cs))
+    rb = batch.run(i1, i2)
+    want = CollisionBatch(ColliderStore(b_cs), 5000, precision="mixed", epa_kw=EPA_KW, graphs=False).run(i1, i2)
+    for k in ("dist", "simplex", "mtv", "epa_status"):
+        assert np.array_equal(rb[k], want[k], equal_nan=True), k
+    assert not np.array_equal(ra["dist"], rb["dist"])
+    with pytest.raises(ValueError):
+        st.update(PinnedColliderSet(workloads.pairs_mixed_six(100, seed=63)[0]))

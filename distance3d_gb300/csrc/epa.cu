@@ -17,6 +17,8 @@
 // next one.  Each thread owns one scratch slot of max_faces faces and
 // max_loose_edges edges (d3d_epa_scratch_bytes), reused across its pairs, so
 // the scratch is bounded by the slot count, not by n.
+#include <cmath>
+#include <cstring>
 #include <mutex>
 
 #include "capi_util.h"
@@ -52,6 +54,37 @@ __device__ __forceinline__ void face_normal(double* f) {
     d3 v0 = ld(f), v1 = ld(f + 3), v2 = ld(f + 6);
     st(f + 9, norm_vec(cross(v1 - v0, v2 - v0)));
 }
+
+// The smallest x >= 0 with sqrt(x) >= e.  IEEE sqrt is correctly rounded on
+// the host and on the device, hence monotonic, so for every x >= 0 and NaN
+//     sqrt(x) < e   <=>   x < sqrt_less_bound(e),
+// which lets the kernels compare squared lengths with the reference's
+// sqrt(...) < e tests, bit for bit.
+double sqrt_less_bound(double e) {
+    if (!(e > 0.0)) return 0.0;
+    if (e == INFINITY) return INFINITY;
+    uint64_t lo = 0, hi = 0x7ff0000000000000ull;  // sqrt(+inf) >= e
+    while (lo < hi) {
+        const uint64_t mid = lo + (hi - lo) / 2;
+        double x;
+        memcpy(&x, &mid, sizeof x);
+        if (std::sqrt(x) >= e)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    double t;
+    memcpy(&t, &hi, sizeof t);
+    return t;
+}
+
+// squared-length bounds of epa.py's two length tests
+struct LengthBounds {
+    double edge;  // epa.py:189-191: norm(edge end difference) < epsilon
+    double keep;  // epa.py:134: norm(face normal) < 0.5
+};
+
+LengthBounds length_bounds(double epsilon) { return LengthBounds{sqrt_less_bound(epsilon), sqrt_less_bound(0.5)}; }
 
 __device__ __forceinline__ void copy12(double* dst, const double* src) {
 #pragma unroll
@@ -225,6 +258,337 @@ __global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __re
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same EPA with one warp per pair.  The polytope (faces of 12 doubles)
+// and the loose edges live in the warp's shared memory; the steps whose
+// order does not matter run across the lanes -- the closest-face scan, the
+// visibility of every face, the normals of the new faces -- and the
+// order-dependent bookkeeping keeps the reference's order exactly: faces are
+// removed by moving the last face into the first visible slot and testing
+// that slot again, each removed face's edges are matched against the loose
+// list in list order (the first match is overwritten by the last edge), and
+// new faces are appended in loose-edge order.  Results are those of k_epa
+// (and of the reference) bit for bit.
+
+constexpr unsigned kWarpAll = 0xffffffffu;
+
+__device__ __forceinline__ int lane_of() { return threadIdx.x & 31; }
+
+// Storage of one warp's polytope: cap_f faces (12 doubles and an ordering
+// key each), cap_e loose edges (6 doubles), cap_f visibility flags.
+__host__ __device__ inline int exact_warp_bytes(int cap_f, int cap_e) {
+    const int e = cap_e > 0 ? cap_e : 1;
+    return (104 * cap_f + 48 * e + cap_f + 15) & ~15;
+}
+__host__ __device__ inline int exact_warp_bytes(const d3d_epa_options& o) {
+    return exact_warp_bytes(o.max_faces, o.max_loose_edges);
+}
+
+// Ordering key of a face distance: unsigned order equals the order of the
+// doubles (-0 as +0); NaN sorts last.
+__device__ __forceinline__ unsigned long long dist_key(double d) {
+    if (d != d) return ~0ull;
+    if (d == 0.0) d = 0.0;
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// the face distance of epa.py:104-106, np.sum(v0 * n) over the row
+__device__ __forceinline__ double face_dist(const double* f) { return (f[0] * f[9] + f[1] * f[10]) + f[2] * f[11]; }
+
+// w = s_a(d) - s_b(-d) with the reference's supports: lanes 0-15 evaluate
+// collider a, lanes 16-31 collider b; a box or hull's first-maximum vertex is
+// found by the 16 lanes of its half (np.argmax).  Every lane returns w.
+__device__ d3 minkowski_exact_warp(const d3d_store& st, int a, int b, d3 d) {
+    const int ln = lane_of();
+    const bool up = ln & 16;
+    // the two halves may take different branches: the shuffles and votes
+    // below stay within this half
+    const unsigned half = up ? 0xffff0000u : 0x0000ffffu;
+    Col<double> c;
+    load_col(st, up ? b : a, c);
+    const d3 dd = up ? -d : d;
+    d3 s;
+    if (c.type == D3D_BOX || c.type == D3D_HULL) {
+        if (c.nv < 1) {
+            s = mk(double(NAN), double(NAN), double(NAN));
+        } else {
+            // first maximum of V . d (dot102); a NaN at vertex 0 wins, later NaNs never do
+            const int h = ln & 15;
+            double bv = 0.0;
+            int bi = -1;
+            bool nan0 = false;
+            for (int k = h; k < c.nv; k += 16) {
+                const d3 v = load_vertex(st.verts64, c.off + k);
+                const double x = dot102(v.x, v.y, v.z, dd.x, dd.y, dd.z);
+                if (k == 0 && x != x) nan0 = true;
+                if (bi < 0 ? x == x : x > bv) {
+                    bv = x;
+                    bi = k;
+                }
+            }
+            for (int m = 8; m; m >>= 1) {
+                const double ov = __shfl_xor_sync(half, bv, m);
+                const int oi = __shfl_xor_sync(half, bi, m);
+                if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            const bool any_nan0 = __ballot_sync(half, nan0) != 0u;
+            const int k = (c.nv == 1 || any_nan0 || bi < 0 || bi >= c.nv) ? 0 : bi;
+            s = add_margin(c, load_vertex(st.verts64, c.off + k), dd);
+        }
+    } else {
+        s = support(c, st, dd);
+    }
+    const d3 o = mk(__shfl_xor_sync(kWarpAll, s.x, 16), __shfl_xor_sync(kWarpAll, s.y, 16),
+                    __shfl_xor_sync(kWarpAll, s.z, 16));
+    return up ? o - s : s - o;
+}
+
+// One pair's EPA by one warp (epa.py:9-78).  F, E, vis: the warp's faces,
+// loose edges and visibility flags in shared memory.  Returns the status;
+// mtv and nf (faces left) as k_epa sets them.
+// F: max_faces faces, K: their ordering keys, E: max_loose_edges edges,
+// vis: max_faces flags, all in the warp's shared memory.
+__device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double* simplex,
+                             const d3d_epa_options& o, LengthBounds lb, double* F, unsigned long long* K, double* E,
+                             unsigned char* vis, d3& mtv, int& nf_out) {
+    const int ln = lane_of();
+    const double eps = o.epsilon;
+    // epa.py:56-57, 89-97: faces ABC, ACD, ADB, BDC
+    if (ln < 4) {
+        const int init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
+        double* f = F + 12 * ln;
+        for (int j = 0; j < 3; ++j) st(f + 3 * j, ld(simplex + 3 * init[ln][j]));
+        face_normal(f);
+        K[ln] = dist_key(face_dist(f));
+    }
+    __syncwarp();
+    int nf = 4, closest = 0;
+    for (int it = 0;; ++it) {
+        if (it >= o.max_iterations) {
+            // epa.py:77: closest_face is a view, read after the last iteration's edits
+            const double* f = F + 12 * closest;
+            const d3 n = ld(f + 9);
+            mtv = n * dot(ld(f), n);
+            nf_out = nf;
+            return D3D_STATUS_EPA_NOT_CONVERGED;
+        }
+        if (nf == 0) {
+            mtv = mk(double(NAN), double(NAN), double(NAN));
+            nf_out = nf;
+            return D3D_STATUS_EPA_DEGENERATE;
+        }
+        // epa.py:104-109: np.sum(v0 * n, axis=1), first minimum (k_epa's
+        // scan: a NaN at face 0 wins, later NaNs never do), on the faces'
+        // ordering keys
+        unsigned long long bk = ~0ull;
+        int bi = 0x7fffffff;
+        for (int i = ln; i < nf; i += 32) {
+            const unsigned long long k = K[i];
+            if (k < bk) {
+                bk = k;
+                bi = i;
+            }
+        }
+        for (int m = 16; m; m >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(kWarpAll, bk, m);
+            const int oi = __shfl_xor_sync(kWarpAll, bi, m);
+            if (ok < bk || (ok == bk && oi < bi)) {
+                bk = ok;
+                bi = oi;
+            }
+        }
+        closest = (K[0] == ~0ull || bk == ~0ull) ? 0 : bi;
+        const double* cf = F + 12 * closest;
+        const double md = face_dist(cf);
+        const d3 sd = ld(cf + 9);
+        const d3 w = minkowski_exact_warp(store, a, b, sd);
+        const double pd = dot(w, sd);
+        if (pd - md < eps) {  // epa.py:67-70
+            mtv = sd * pd;
+            nf_out = nf;
+            return D3D_STATUS_OK;
+        }
+        // epa.py:157-165: visibility of every face (epa.py:122-124)
+        for (int i = ln; i < nf; i += 32) {
+            const double* f = F + 12 * i;
+            vis[i] = dot(ld(f + 9), w - ld(f)) > eps ? 1 : 0;
+        }
+        __syncwarp();
+        // remove visible faces in the reference's order, collecting edges
+        int ne = 0, i = 0;
+        while (true) {
+            int p = -1;
+            for (int base = i; base < nf; base += 32) {
+                const int j = base + ln;
+                const unsigned m = __ballot_sync(kWarpAll, j < nf && vis[j]);
+                if (m) {
+                    p = base + __ffs(m) - 1;
+                    break;
+                }
+            }
+            if (p < 0) break;
+            const double* f = F + 12 * p;
+            for (int j = 0; j < 3; ++j) {  // epa.py:167-187
+                const d3 e0 = ld(f + 3 * j), e1 = ld(f + 3 * ((j + 1) % 3));
+                int found = -1;
+                for (int kb = 0; kb < ne; kb += 32) {
+                    const int k = kb + ln;
+                    bool match = false;
+                    if (k < ne) {
+                        const double* e = E + 6 * k;
+                        const d3 d1 = ld(e + 3) - e0, d0 = ld(e) - e1;
+                        match = dot(d1, d1) < lb.edge && dot(d0, d0) < lb.edge;
+                    }
+                    const unsigned m = __ballot_sync(kWarpAll, match);
+                    if (m) {
+                        found = kb + __ffs(m) - 1;
+                        break;
+                    }
+                }
+                if (found >= 0) {
+                    if (ln < 6) E[6 * found + ln] = E[6 * (ne - 1) + ln];
+                    --ne;
+                } else {
+                    if (ne >= o.max_loose_edges) break;  // epa.py:193-198
+                    if (ln < 3) {
+                        E[6 * ne + ln] = f[3 * j + ln];
+                        E[6 * ne + 3 + ln] = f[3 * ((j + 1) % 3) + ln];
+                    }
+                    ++ne;
+                }
+                __syncwarp();
+            }
+            // epa.py:118-120: the last face moves into slot p, which is tested again
+            if (ln < 12) F[12 * p + ln] = F[12 * (nf - 1) + ln];
+            if (ln == 0) {
+                vis[p] = vis[nf - 1];
+                K[p] = K[nf - 1];
+            }
+            --nf;
+            i = p;
+            __syncwarp();
+        }
+        // epa.py:126-137 extend_with_point, in loose-edge order
+        int kept = 0;
+        for (int kb = 0; kb < ne; kb += 32) {
+            const int k = kb + ln;
+            double nfa[12];
+            bool keep = false;
+            if (k < ne) {
+                const double* e = E + 6 * k;
+                for (int q = 0; q < 6; ++q) nfa[q] = e[q];
+                nfa[6] = w.x;
+                nfa[7] = w.y;
+                nfa[8] = w.z;
+                face_normal(nfa);
+                const d3 n = ld(nfa + 9);
+                keep = !(dot(n, n) < lb.keep);
+                // epa.py:139-146: the reference swaps through a NumPy view of
+                // row 0, so the net effect is v0 := v1 (v1 unchanged), n := -n
+                if (keep && dot(ld(nfa), n) + 1e-6 < 0.0) {
+                    st(nfa, ld(nfa + 3));
+                    st(nfa + 9, -n);
+                }
+            }
+            const unsigned km = __ballot_sync(kWarpAll, keep);
+            const int before = __popc(km & ((1u << ln) - 1u));
+            // epa.py:128: the face buffer is checked before every loose edge
+            const bool over = k < ne && nf + kept + before >= o.max_faces;
+            const unsigned om = __ballot_sync(kWarpAll, over);
+            const int limit = om ? __ffs(om) - 1 : 32;  // edges of this chunk written before the overflow
+            if (keep && ln < limit) {
+                const int idx = nf + kept + before;
+                double* dst = F + 12 * idx;
+                for (int q = 0; q < 12; ++q) dst[q] = nfa[q];
+                K[idx] = dist_key(face_dist(nfa));
+            }
+            if (om) {
+                nf += kept + __popc(km & ((1u << limit) - 1u));
+                __syncwarp();
+                mtv = mk(double(NAN), double(NAN), double(NAN));
+                nf_out = nf;
+                return D3D_STATUS_EPA_FACE_OVERFLOW;
+            }
+            kept += __popc(km);
+        }
+        nf += kept;
+        __syncwarp();
+    }
+}
+
+// One warp per block; each warp takes pairs from the cursor and holds its
+// polytope in the block's dynamic shared memory.
+__global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, const int32_t* __restrict__ i2,
+                                 const int32_t* __restrict__ list, int64_t n,
+                                 const unsigned long long* __restrict__ n_dev,
+                                 unsigned long long* __restrict__ cursor, const double* __restrict__ simplex,
+                                 d3d_epa_options o, LengthBounds lb, double* __restrict__ mtv,
+                                 int8_t* __restrict__ status, int32_t* __restrict__ n_faces,
+                                 double* __restrict__ faces) {
+    extern __shared__ __align__(16) unsigned char smem_epa[];
+    const int ln = lane_of();
+    const int e = o.max_loose_edges > 0 ? o.max_loose_edges : 1;
+    double* F = reinterpret_cast<double*>(smem_epa);
+    unsigned long long* K = reinterpret_cast<unsigned long long*>(F + 12 * (int64_t)o.max_faces);
+    double* E = reinterpret_cast<double*>(K + o.max_faces);
+    unsigned char* vis = reinterpret_cast<unsigned char*>(E + 6 * (int64_t)e);
+    if (n_dev) n = (int64_t)*n_dev;
+    while (true) {
+        long long slot = 0;
+        if (ln == 0) slot = (long long)atomicAdd(cursor, 1ull);
+        slot = __shfl_sync(kWarpAll, slot, 0);
+        if (slot >= n) break;
+        const int64_t pid = list ? list[slot] : slot;
+        d3 m;
+        int nf = 0;
+        const int stt = epa_pair_warp(s, i1[pid], i2[pid], simplex + 12 * pid, o, lb, F, K, E, vis, m, nf);
+        if (ln == 0) {
+            mtv[3 * pid] = m.x;
+            mtv[3 * pid + 1] = m.y;
+            mtv[3 * pid + 2] = m.z;
+            status[pid] = (int8_t)stt;
+            n_faces[pid] = stt == D3D_STATUS_EPA_DEGENERATE ? 0 : nf;
+        }
+        if (faces && stt != D3D_STATUS_EPA_DEGENERATE) {
+            double* out = faces + pid * 12 * (int64_t)o.max_faces;
+            for (int j = ln; j < 12 * nf; j += 32) out[j] = F[j];
+        }
+        __syncwarp();
+    }
+}
+
+constexpr int64_t kExactSmemPerBlock = 227 * 1024;
+
+bool exact_warp_supported(const d3d_epa_options& o) {
+    return o.max_faces <= 65536 && o.max_loose_edges <= 65536 && (int64_t)exact_warp_bytes(o) <= kExactSmemPerBlock;
+}
+
+// One warp per block, each block holding one polytope, as many per SM as
+// shared memory and registers allow.
+int exact_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                      const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                      const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                      cudaStream_t stream) {
+    const int smem = exact_warp_bytes(o);
+    const void* fn = (const void*)k_epa_exact_warp;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) {
+        set_error("d3d_epa: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    const int blocks = persistent_blocks(fn, 32, n, 0, smem);
+    k_epa_exact_warp<<<blocks, 32, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o,
+                                                   length_bounds(o.epsilon), mtv, status, n_faces, faces);
+    return check_launch("d3d_epa");
+}
+
 int64_t slot_doubles(const d3d_epa_options& o) {
     return 12 * (int64_t)o.max_faces + 6 * (int64_t)o.max_loose_edges;
 }
@@ -257,6 +621,9 @@ int epa_f64_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2,
                    const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                    const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
                    void* scratch, int64_t slots, cudaStream_t stream) {
+    if (exact_warp_supported(o))  // the polytopes in shared memory: no slot scratch
+        return exact_warp_launch(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces,
+                                 stream);
     int blocks = persistent_blocks((const void*)k_epa, kBlock, n);
     if (blocks > slots / kBlock) blocks = (int)(slots / kBlock);
     if (blocks < 1) {
@@ -292,11 +659,11 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     cudaStream_t st = d3d::as_stream(stream);
     const bool mixed = options->precision == D3D_PRECISION_MIXED;
     const bool warp = mixed && d3d::epa_warp_supported(*options);
-    const bool sched = n >= kScheduleMin && !warp;
+    const bool sched = n >= kScheduleMin && !warp && !exact_warp_supported(*options);
     const size_t up_n = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
     const size_t order_bytes = sched ? up_n : 0;
     const size_t fb_bytes = mixed ? 2 * up_n : 0;  // fallback lists of the FP32 and FP64 warp searches
-    const size_t temp_bytes = sched ? d3d::pair_order_temp_bytes(n) : 0;
+    const size_t temp_bytes = sched ? (d3d::pair_order_temp_bytes(n) + 255) & ~size_t(255) : 0;
     void* block = nullptr;
     rc = d3d::scratch_alloc(&block, 256 + order_bytes + fb_bytes + temp_bytes, st);
     if (rc) return rc;
@@ -318,14 +685,19 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     } else if (!rc && mixed)
         rc = d3d::epa_mixed_launch(*store, i1, i2, order, n, ctr, simplex, *options, mtv, status, n_faces, faces,
                                    scratch, slots_for(n), fallback, ctr + 2, st);
-    if (!rc) {
+    const int32_t* f64_list = warp64 ? fallback2 : (mixed ? fallback : order);
+    const unsigned long long* f64_count = warp64 ? ctr + 4 : (mixed ? ctr + 2 : nullptr);
+    if (!rc && exact_warp_supported(*options)) {
+        // the FP64 EPA, one warp per pair: every pair, or the mixed form's fallback pairs
+        rc = exact_warp_launch(*store, i1, i2, f64_list, n, f64_count, mixed ? ctr + 1 : ctr, simplex, *options, mtv,
+                               status, n_faces, faces, st);
+    } else if (!rc) {
         // the FP64 EPA: every pair, or the mixed form's fallback pairs
         int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
         const int64_t max_blocks = slots_for(n) / kBlock;  // the scratch holds this many slots
         if (blocks > max_blocks) blocks = (int)max_blocks;
-        const int32_t* list = warp64 ? fallback2 : (mixed ? fallback : order);
-        const unsigned long long* count = warp64 ? ctr + 4 : (mixed ? ctr + 2 : nullptr);
-        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, list, n, count, mixed ? ctr + 1 : ctr, simplex, *options,
+        k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, f64_list, n, f64_count, mixed ? ctr + 1 : ctr, simplex,
+                                         *options,
                                          mtv, status, n_faces, faces, static_cast<double*>(scratch),
                                          slot_doubles(*options));
         rc = d3d::check_launch("d3d_epa");
@@ -423,6 +795,9 @@ extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const 
         d3d::set_error("d3d_epa_noalloc: %s", cudaGetErrorString(e));
         return D3D_ERR_CUDA;
     }
+    if (exact_warp_supported(*options))  // the polytopes in shared memory: the static array holds the counter
+        return exact_warp_launch(*store, i1, i2, nullptr, n, nullptr, cursor, simplex, *options, mtv, status,
+                                 n_faces, faces, st);
     int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);
     if (blocks > slots / kBlock) blocks = (int)(slots / kBlock);
     k_epa<<<blocks, kBlock, 0, st>>>(*store, i1, i2, nullptr, n, nullptr, cursor, simplex, *options, mtv, status,

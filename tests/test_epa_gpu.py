@@ -48,6 +48,28 @@ def test_epa_matches_oracle_with_faces(max_faces, max_edges):
         assert np.array_equal(r["faces"][k, :nf], ref["faces"][k, :nf])
 
 
+@pytest.mark.parametrize("max_faces,max_edges", [(100, 40), (64, 128), (256, 128)])
+def test_epa_polytope_sizes(max_faces, max_edges):
+    """Polytope storage of other sizes than the defaults (the face and edge
+    limits bind on different pairs) on the nine-type workload, against the
+    oracle bit for bit."""
+    cs, i1, i2 = workloads.pairs_all_types(6000, seed=33)
+    st = ColliderStore(cs)
+    g = host(gjk_distance_batch(st, i1, i2))
+    hit = np.flatnonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4))
+    kw = dict(max_faces=max_faces, max_loose_edges=max_edges)
+    r = host(epa_batch(st, i1[hit], i2[hit], g["simplex"][hit], return_faces=True, **kw))
+    ref = oracle.epa(cs, i1[hit], i2[hit], g["simplex"][hit], want_faces=True, **kw)
+    assert np.array_equal(r["status"], ref["status"])
+    assert np.array_equal(r["n_faces"], ref["n_faces"])
+    assert np.array_equal(r["mtv"], ref["mtv"], equal_nan=True)
+    for k in range(len(hit)):
+        nf = r["n_faces"][k]
+        assert np.array_equal(r["faces"][k, :nf], ref["faces"][k, :nf])
+    if max_faces > 64:
+        assert (ref["n_faces"] > 64).sum() > 10
+
+
 def test_epa_many_pairs_reuse_slots():
     """More pairs than scratch slots: every pair still gets its own answer."""
     cs, i1, i2 = workloads.pairs_mixed_six(200000, seed=32, center_half_width=workloads.INTERSECT30_HALF_WIDTH)

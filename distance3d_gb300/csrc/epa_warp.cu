@@ -64,20 +64,35 @@ __device__ __forceinline__ float eps_of<float>() { return FLT_EPSILON; }
 template <>
 __device__ __forceinline__ double eps_of<double>() { return DBL_EPSILON; }
 
+// Storage bounds of one polytope.  The search adds one vertex per iteration
+// (nv <= max_iterations + 4) and keeps a closed triangulated surface (the
+// visible faces are validated to be a disk), so its live faces number
+// 2 V - 4 <= 2 nv - 4 for its V <= nv vertices in use (Euler), and a horizon
+// loop visits distinct vertices (ne <= nv).  The face slots and horizon
+// edges are bounded by those numbers as well as by max_faces and
+// max_loose_edges; the search checks both bounds before it writes.
+__host__ __device__ inline int vertex_cap(const d3d_epa_options& o) { return o.max_iterations + 4; }
+__host__ __device__ inline int face_cap(const d3d_epa_options& o) {
+    const int euler = 2 * vertex_cap(o) - 4;
+    return o.max_faces < euler ? o.max_faces : euler;
+}
+__host__ __device__ inline int edge_cap(const d3d_epa_options& o) {
+    const int e = o.max_loose_edges < vertex_cap(o) ? o.max_loose_edges : vertex_cap(o);
+    return e > 0 ? e : 1;
+}
+
 // Byte offsets of one warp's polytope in shared memory.
 struct Layout {
-    int vy, vd, fn, fv, adj, hz, freel, vis, se, ee, bytes;
+    int vy, fn, fv, adj, hz, freel, vis, se, ee, bytes;
 };
 
 template <typename T>
 __host__ __device__ inline Layout layout_for(const d3d_epa_options& o) {
-    const int nv = o.max_iterations + 4, F = o.max_faces, E = o.max_loose_edges > 0 ? o.max_loose_edges : 1;
+    const int nv = vertex_cap(o), F = face_cap(o), E = edge_cap(o);
     const int q = (int)sizeof(Q4<T>);
     Layout L;
     int p = 0;
     L.vy = p;
-    p += q * nv;
-    L.vd = p;
     p += q * nv;
     L.fn = p;
     p += q * F;
@@ -102,7 +117,6 @@ __host__ __device__ inline Layout layout_for(const d3d_epa_options& o) {
 template <typename T>
 struct Poly {
     Q4<T>* vy;             // vertex y.xyz
-    Q4<T>* vd;             // search direction .xyz; w: input simplex row (0..3), -1 for found vertices
     Q4<T>* fn;             // unit normal .xyz, w = offset n . y_a
     ushort4* adj;          // faces across edges (a,b), (b,c), (c,a)
     int2* hz;              // horizon edge e: x = a | b << 8 | k << 16 (edge k of g faces it), y = g
@@ -117,7 +131,6 @@ template <typename T>
 __device__ __forceinline__ Poly<T> poly_at(unsigned char* base, const Layout& L) {
     Poly<T> P;
     P.vy = reinterpret_cast<Q4<T>*>(base + L.vy);
-    P.vd = reinterpret_cast<Q4<T>*>(base + L.vd);
     P.fn = reinterpret_cast<Q4<T>*>(base + L.fn);
     P.adj = reinterpret_cast<ushort4*>(base + L.adj);
     P.hz = reinterpret_cast<int2*>(base + L.hz);
@@ -318,7 +331,6 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
     if (ln < 4) {
         const V3<T> y = mk((T)simplex[3 * ln], (T)simplex[3 * ln + 1], (T)simplex[3 * ln + 2]);
         P.vy[ln] = q4(y.x, y.y, y.z, T(0));
-        P.vd[ln] = q4(T(0), T(0), T(0), (T)ln);
         scale = sqrt_t(dot(y, y));
     }
 #pragma unroll
@@ -407,7 +419,6 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
         unsigned short* const vl = P.freel + nfree;
         if (ln == 0) {
             P.vy[vn] = q4(w.x, w.y, w.z, T(0));
-            P.vd[vn] = q4(sd.x, sd.y, sd.z, T(-1));
             P.vis[cf] = stamp;
             vl[0] = (unsigned short)cf;
         }
@@ -454,7 +465,8 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
             for (int i = ln; i < 3 * nvis; i += 32) ne_l += P.vis[adj_at(P.adj[vl[i / 3]], i % 3)] != stamp;
             int eb = warp_excl(ne_l);
             ne = __shfl_sync(kFull, eb + ne_l, 31);
-            if (ne > o.max_loose_edges || ne < 3) return R;
+            // more than edge_cap(o) < max_loose_edges edges: not one loop
+            if (ne > o.max_loose_edges || ne > edge_cap(o) || ne < 3) return R;
             for (int i = ln; i < 3 * nvis; i += 32) {
                 const int f = vl[i / 3], j = i % 3;
                 const int h = adj_at(P.adj[f], j);
@@ -515,6 +527,7 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
         }
         // new faces (a, b, w): slots from the top of the free list, then fresh
         const int nft = nfree + nvis;
+        if (ne > nft && nslots + (ne - nft) > face_cap(o)) return R;  // beyond the Euler bound: never for a closed surface
         for (int e = ln; e < ne; e += 32) {
             const int2 h = P.hz[e];
             const int ea = h.x & 0xff, eb2 = (h.x >> 8) & 0xff, k = (h.x >> 16) & 3;
@@ -563,8 +576,14 @@ __device__ __forceinline__ d3 refine_face(const Poly<double>& P, const d3d_store
     return n * dot(w, n);
 }
 
+// Resident warps per SM the register budget is set for: the FP32 search runs
+// 32 (64 registers, a few spilled: latency hiding outweighs the spills), the
+// FP64 search, which takes few pairs, 16.
+template <typename T>
+constexpr int kWarpsPerSm = sizeof(T) == 4 ? 32 : 16;
+
 template <typename T, int WARPS, bool MESH>
-__global__ void __launch_bounds__(32 * WARPS, 16 / WARPS) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
+__global__ void __launch_bounds__(32 * WARPS, kWarpsPerSm<T> / WARPS) k_epa_warp(d3d_store st, const int32_t* __restrict__ i1,
                                                           const int32_t* __restrict__ i2,
                                                           const int32_t* __restrict__ list, int64_t n,
                                                           const unsigned long long* __restrict__ n_dev,

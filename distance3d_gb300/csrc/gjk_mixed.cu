@@ -8,12 +8,12 @@
 //    (80 bytes/pair) and appends the pair to the refinement list (separated
 //    or touching) or the fallback list (clipped / not converged).
 // B  refines in FP64, one round per lane and iteration (pb_round): A's
-//    final simplex rows are re-evaluated in FP64 along their FP32 directions
-//    (polytope supports choose their vertex by an FP32 argmax and return the
-//    FP64 vertex); if that simplex encloses or touches the origin the pair is
-//    done, otherwise the reference's loop continues from it until the duality
-//    gap brackets the distance within 1e-7 of itself or 1e-9 of the scene's
-//    scale.
+//    final simplex rows are re-evaluated in FP64 along their FP32 directions,
+//    all in the first round (polytope supports choose their vertex by an FP32
+//    argmax and return the FP64 vertex); if that simplex encloses or touches
+//    the origin the pair is done, otherwise the reference's loop continues
+//    from it until the duality gap brackets the distance within 1e-6 of
+//    itself or 1e-9 of the scene's scale.
 // C  is the plain FP64 kernel over the fallback list (the reference's
 //    arithmetic; CLIPPED and MAX_ITER keep their FP64 meaning).
 //

@@ -268,15 +268,15 @@ enum PhaseBMode { PB_RUN = 0, PB_DONE = 1, PB_FALLBACK = 2, PB_REPLAY = 3 };
 
 // FP64 refinement of one pair, a per-lane state machine.  REPLAY: A's final
 // simplex rows are re-evaluated in FP64 along the FP32 directions that
-// produced them, one row per round; after the last row the simplex is solved
-// as the loop's first iteration would (nothing to beat yet).  If it encloses
+// produced them, all in one round, and the simplex is solved as the loop's
+// first iteration would (nothing to beat yet).  If it encloses
 // or touches the origin the pair is done; otherwise RUN continues the
 // reference's loop from there, stopped by the duality gap.
 template <typename Rows>
 struct PhaseB {
     GjkLoop<double, Rows> g;
     int mode;
-    int row, rows;
+    int rows;
 };
 
 template <typename Rows>
@@ -285,56 +285,59 @@ __device__ __forceinline__ void pb_begin(PhaseB<Rows>& B, float4 v) {
     B.g.it = 0;
     B.g.state = GJK_RUNNING;
     B.g.status = D3D_STATUS_OK;
-    B.row = 0;
     const int outcome = __float_as_int(v.w) & 0xff;
     B.rows = (__float_as_int(v.w) >> 8) & 0xff;
     B.mode = (outcome == PA_SEPARATED || outcome == PA_TOUCHING) && B.rows > 0 ? PB_REPLAY : PB_FALLBACK;
 }
 
-// One round for one lane: one pair of FP64 supports, along the next replayed
-// row direction (REPLAY, from `dirs`) or the loop's direction (RUN), then the
-// simplex update (_gjk_jolt.py:224-288).  Returns true once the loop has
-// ended: g.state is GJK_INTERSECTION or GJK_NO_INTERSECTION (pb_end finishes
-// the pair), or B.mode is PB_FALLBACK (clipped, iteration bound, failed
-// replay).
+// One round for one lane: FP64 supports along every replayed row direction
+// (REPLAY, from `dirs`: all of A's rows in one round) or one pair along the
+// loop's direction (RUN), then the simplex update (_gjk_jolt.py:224-288).
+// Every round ends in the simplex solve, so a warp's lanes reach it together
+// whatever mode each is in.  Returns true once the loop has ended: g.state
+// is GJK_INTERSECTION or GJK_NO_INTERSECTION (pb_end finishes the pair), or
+// B.mode is PB_FALLBACK (clipped, iteration bound, failed replay).
 template <bool MESH = true, typename Rows>
 __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, int a, int b,
                                          const float4* __restrict__ dirs, double tol_sq, const d3d_gjk_options& opt,
                                          const JoltEps<double>& E) {
     GjkLoop<double, Rows>& g = B.g;
     const bool replay = B.mode == PB_REPLAY;
-    d3 d = g.dir;
-    if (replay) {
-        const float4 f = dirs[B.row];
-        d = mk((double)f.x, (double)f.y, (double)f.z);
-    } else {
+    if (!replay) {
         if (g.it >= opt.max_iterations) {
             B.mode = PB_FALLBACK;
             return true;
         }
         ++g.it;
     }
-    d3 p, q;
-    pair_supports<double, RefineSupportT<MESH>>(s, a, b, d, p, q);
-    const d3 w = p - q;
-    if (!replay) {
-        const double dd = dot(g.dir, w);
-        if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
-            B.mode = PB_FALLBACK;  // clipped: the FP64 kernel reports it
-            return true;
+    const int count = replay ? B.rows : 1;
+    for (int r = 0; r < count; ++r) {
+        d3 d = g.dir;
+        if (replay) {
+            const float4 f = dirs[r];
+            d = mk((double)f.x, (double)f.y, (double)f.z);
         }
-        if (g.S.n > 0) {
-            // duality gap: |v| - (|v|^2 - v.w) / |v| <= distance <= |v|
-            const double gap = g.vl + dd;
-            if (gap <= kMixedRelGap * g.vl || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl) {
-                g.dir = -g.dir;
-                g.state = GJK_NO_INTERSECTION;
+        d3 p, q;
+        pair_supports<double, RefineSupportT<MESH>>(s, a, b, d, p, q);
+        const d3 w = p - q;
+        if (!replay) {
+            const double dd = dot(g.dir, w);
+            if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
+                B.mode = PB_FALLBACK;  // clipped: the FP64 kernel reports it
                 return true;
             }
+            if (g.S.n > 0) {
+                // duality gap: |v| - (|v|^2 - v.w) / |v| <= distance <= |v|
+                const double gap = g.vl + dd;
+                if (gap <= kMixedRelGap * g.vl || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl) {
+                    g.dir = -g.dir;
+                    g.state = GJK_NO_INTERSECTION;
+                    return true;
+                }
+            }
         }
+        simplex_push(g.S, w, p, q);
     }
-    simplex_push(g.S, w, p, q);
-    if (replay && ++B.row < B.rows) return false;
     d3 nv;
     double nl;
     int set;

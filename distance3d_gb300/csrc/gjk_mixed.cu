@@ -5,9 +5,11 @@
 // A  runs the Jolt loop in FP32 on the FP32 mirror of the store, with
 //    thresholds scaled to single precision, hands each pair's outcome, final
 //    closest point and the search direction of each final simplex row to B
-//    (80 bytes/pair) and appends the pair to the refinement list (separated
-//    or touching) or the fallback list (clipped / not converged).
-// B  refines in FP64, one round per lane and iteration (pb_round): A's
+//    (80 bytes/pair) and appends clipped and unconverged pairs to the
+//    fallback list.
+// B  walks the same type-sorted order (lanes of a warp then mostly hold
+//    pairs of the same collider types) and refines A's separated and
+//    touching pairs in FP64, one round per lane and iteration (pb_round): A's
 //    final simplex rows are re-evaluated in FP64 along their FP32 directions,
 //    all in the first round (polytope supports choose their vertex by an FP32
 //    argmax and return the FP64 vertex); if that simplex encloses or touches
@@ -40,11 +42,10 @@ using namespace d3d;
 
 
 // Per-call counters (one 256-byte block): cursors of A, B and C, then the
-// lengths of the refinement and fallback lists.
-enum { kCurA = 0, kCurB, kCurC, kNumRefine, kNumFallback, kCounters };
+// length of the fallback list.
+enum { kCurA = 0, kCurB, kCurC, kNumFallback, kCounters };
 
 struct Lists {
-    int32_t* refine;
     int32_t* fallback;
     unsigned long long* ctr;
 };
@@ -80,21 +81,20 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
         const int o = pa_step<MESH>(L, s, a, b, tol_sq, max_d2, max_iter);
         const bool done = o >= 0;
         if (done) hand[pid] = pa_handoff(L, o);
-        if (__any_sync(__activemask(), done)) {
-            append_warp(lists.refine, lists.ctr + kNumRefine, o == PA_SEPARATED || o == PA_TOUCHING,
-                        (int32_t)pid);
+        if (__any_sync(__activemask(), done))
             append_warp(lists.fallback, lists.ctr + kNumFallback, o >= PA_CLIPPED, (int32_t)pid);
-        }
         need = done;
     }
 }
 
 template <int BLOCK, bool MESH>
 __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_t* __restrict__ i1,
-                                                        const int32_t* __restrict__ i2, d3d_gjk_options opt,
+                                                        const int32_t* __restrict__ i2,
+                                                        const int32_t* __restrict__ order, int64_t n,
+                                                        const int64_t* __restrict__ n_dev, d3d_gjk_options opt,
                                                         const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
     __shared__ double rows[24 * BLOCK];
-    const int64_t n = (int64_t)lists.ctr[kNumRefine];
+    if (n_dev) n = *n_dev;
     const JoltEps<double> E = reference_eps<double>();
     const double tol_sq = opt.tolerance * opt.tolerance;
     PhaseB<SmemRows<double, BLOCK>> B;
@@ -107,10 +107,13 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
         const long long slot = fetch_slot(lists.ctr + kCurB, need);
         if (need) {
             if (slot >= n) break;
-            pid = lists.refine[slot];
+            // the pairs in the collider-type order, A's separated and touching ones
+            pid = order ? order[slot] : (int32_t)slot;
+            const float4 v = hand[pid].v;
+            const int outcome = __float_as_int(v.w) & 0xff;
+            if (outcome != PA_SEPARATED && outcome != PA_TOUCHING) continue;
             a = i1[pid];
             b = i2[pid];
-            const float4 v = hand[pid].v;
             it_a = handoff_iters(v);
             pb_begin(B, v);
             need = false;
@@ -136,7 +139,7 @@ namespace d3d {
 
 size_t gjk_mixed_scratch_bytes(int64_t capacity) {
     return 256 + up(sizeof(int32_t) * (size_t)capacity) + pair_order_temp_bytes(capacity) +
-           up(sizeof(Handoff) * (size_t)capacity) + 2 * up(sizeof(int32_t) * (size_t)capacity);
+           up(sizeof(Handoff) * (size_t)capacity) + up(sizeof(int32_t) * (size_t)capacity);
 }
 
 template <int BLOCK, bool MESH>
@@ -150,8 +153,8 @@ int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, c
     int rc = check_launch("d3d_gjk_distance (mixed, FP32 phase)");
     if (rc) return rc;
     const void* kb = (const void*)k_gjk_mixed_b<BLOCK, MESH>;
-    k_gjk_mixed_b<BLOCK, MESH><<<persistent_blocks(kb, BLOCK, n, per_sm), BLOCK, 0, stream>>>(store, i1, i2, opt,
-                                                                                             hand, o, lists);
+    k_gjk_mixed_b<BLOCK, MESH><<<persistent_blocks(kb, BLOCK, n, per_sm), BLOCK, 0, stream>>>(
+        store, i1, i2, order, n, n_dev, opt, hand, o, lists);
     return check_launch("d3d_gjk_distance (mixed, FP64 phase)");
 }
 
@@ -171,7 +174,6 @@ int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, 
     const bool sched = n >= t.sort_min;
     const size_t order_bytes = up(sizeof(int32_t) * (size_t)n);
     const size_t temp_bytes = pair_order_temp_bytes(n);
-    const size_t list_bytes = up(sizeof(int32_t) * (size_t)n);
     char* p = static_cast<char*>(scratch);
     Lists lists;
     lists.ctr = reinterpret_cast<unsigned long long*>(p);
@@ -182,8 +184,7 @@ int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, 
     p += temp_bytes;
     Handoff* hand = reinterpret_cast<Handoff*>(p);
     p += up(sizeof(Handoff) * (size_t)n);
-    lists.refine = reinterpret_cast<int32_t*>(p);
-    lists.fallback = reinterpret_cast<int32_t*>(p + list_bytes);
+    lists.fallback = reinterpret_cast<int32_t*>(p);
     cudaError_t e = cudaMemsetAsync(lists.ctr, 0, kCounters * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) {
         set_error("d3d_gjk_distance (mixed): %s", cudaGetErrorString(e));

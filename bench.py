@@ -37,13 +37,14 @@ UNIT = "pairs/s"
 EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 # DRAM bytes per pair of the mixed kernels from one ncu capture of the
 # 131,072-pair workload (k_gjk_mixed_a + k_gjk_mixed_b per pair; k_epa_warp
-# per EPA pair, 38,718 of them); traffic grows in proportion to the pairs
-NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78166272 + 3525888 + 141310208 + 12496128) / 131072,
-                           "epa_mixed": (46292224 + 158208) / 38814}
+# per EPA pair, 38,814 of them); traffic grows in proportion to the pairs
+NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78182400 + 3321856 + 135840512 + 12765696) / 131072,
+                           "epa_mixed": (46323200 + 1211648) / 38814}
 # this library's kernels per timed mixed step (one graph replay): k_pair_keys,
 # k_gjk_mixed_a, k_gjk_mixed_b, k_gjk_distance_f64 (fallback list),
-# k_epa_select, k_epa_warp<float>, k_epa_warp<double> (fallback list), k_epa
-# (second fallback list); the CUB sort kernels are the toolkit's
+# k_epa_select, k_epa_warp<float>, k_epa_warp<double> (fallback list),
+# k_epa_exact_warp (second fallback list); the CUB sort kernels are the
+# toolkit's
 MIXED_STEP_LAUNCHES = 8
 
 # Algorithmic bytes per pair (counted once): two collider records, the hull
@@ -285,7 +286,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": "1,048,576 six-type pairs, GJK distance + EPA (256 faces) on intersecting pairs",
+        "config": {"workload": f"{len(i1):,} six-type pairs, GJK distance + EPA (256 faces) on intersecting pairs",
                    "pairs": len(i1)},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
                          "sample": f"{args.steps} full passes over {len(i1)} pairs"},
@@ -705,7 +706,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
-            "config": {"workload": "1,048,576 six-type pairs, GJK distance + EPA (256 faces) on "
+            "config": {"workload": f"{n:,} six-type pairs, GJK distance + EPA (256 faces) on "
                                    "intersecting pairs, centers in [-0.38,0.38]^3",
                        "pairs_per_gpu": n, "intersecting_fraction": n_epa / n, "epa_pairs": n_epa,
                        "l2": "inputs 1.6 GB > L2, no flush", "parallelism": f"replicas x{world}"},

@@ -50,6 +50,9 @@ struct Lists {
     unsigned long long* ctr;
 };
 
+// slots a warp claims from the type-sorted order at a time
+constexpr int kChunk = 32;
+
 // Phase A's register budget: at least 12 resident warps per SM (16 for
 // 256-thread blocks), which ptxas would otherwise trade for a few more
 // registers per thread.
@@ -68,10 +71,15 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
     int64_t pid = 0;
     int a = 0, b = 0;
     bool need = true;
+    unsigned live = __activemask();  // the warp's lanes still in the loop
+    WarpChunk chunk;
     while (true) {
-        const long long slot = fetch_slot(lists.ctr + kCurA, need);
+        __syncwarp(live);
+        const long long slot = fetch_slot_chunked(lists.ctr + kCurA, need, chunk, live, kChunk);
+        const bool quit = need && slot >= n;
+        live = __ballot_sync(live, !quit);
+        if (quit) break;
         if (need) {
-            if (slot >= n) break;
             pid = order ? order[slot] : slot;
             a = i1[pid];
             b = i2[pid];
@@ -81,8 +89,7 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
         const int o = pa_step<MESH>(L, s, a, b, tol_sq, max_d2, max_iter);
         const bool done = o >= 0;
         if (done) hand[pid] = pa_handoff(L, o);
-        if (__any_sync(__activemask(), done))
-            append_warp(lists.fallback, lists.ctr + kNumFallback, o >= PA_CLIPPED, (int32_t)pid);
+        append_lanes(live, lists.fallback, lists.ctr + kNumFallback, done && o >= PA_CLIPPED, (int32_t)pid);
         need = done;
     }
 }
@@ -103,10 +110,15 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
     int a = 0, b = 0;
     int it_a = 0;
     bool need = true;
+    unsigned live = __activemask();  // the warp's lanes still in the loop
+    WarpChunk chunk;
     while (true) {
-        const long long slot = fetch_slot(lists.ctr + kCurB, need);
+        __syncwarp(live);
+        const long long slot = fetch_slot_chunked(lists.ctr + kCurB, need, chunk, live, kChunk);
+        const bool quit = need && slot >= n;
+        live = __ballot_sync(live, !quit);
+        if (quit) break;
         if (need) {
-            if (slot >= n) break;
             // the pairs in the collider-type order, A's separated and touching ones
             pid = order ? order[slot] : (int32_t)slot;
             const float4 v = hand[pid].v;

@@ -28,6 +28,44 @@ __device__ __forceinline__ long long fetch_slot(unsigned long long* cursor, bool
     return slot;
 }
 
+// A warp's share of the global order: the slots [next, end) it has claimed
+// and not yet handed to a lane.  Every lane holds the same copy.
+struct WarpChunk {
+    long long next = 0, end = 0;
+};
+
+// Lanes with `need` set receive consecutive slots (-1 for the others), taken
+// from the warp's chunk; when the chunk runs out the warp claims the next
+// `chunk` (>= 32) slots of *cursor.  A warp's lanes then hold pairs from at
+// most two chunks of the order at a time, instead of from anywhere in the
+// span all resident lanes of the GPU have fetched, which keeps the lanes of
+// a warp on pairs of the same collider types in a type-sorted order.
+// Every lane of `live` must call it together (converged), so that the
+// lanes' copies of `w` stay equal.
+__device__ __forceinline__ long long fetch_slot_chunked(unsigned long long* cursor, bool need, WarpChunk& w,
+                                                        unsigned live, int chunk) {
+    const unsigned want = __ballot_sync(live, need);
+    if (!want) return -1;
+    const int lane = threadIdx.x & 31;
+    const int rank = __popc(want & ((1u << lane) - 1u));
+    const int cnt = __popc(want);
+    const long long avail = w.end - w.next;
+    long long slot;
+    if (avail >= cnt) {
+        slot = w.next + rank;
+        w.next += cnt;
+    } else {
+        const int leader = __ffs(live) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(cursor, (unsigned long long)chunk);
+        base = __shfl_sync(live, base, leader);
+        slot = rank < avail ? w.next + rank : (long long)base + (rank - avail);
+        w.next = (long long)base + (cnt - avail);
+        w.end = (long long)base + chunk;
+    }
+    return need ? slot : -1;
+}
+
 // Lanes with `take` set append `value` to list[*count ...], one atomic per
 // warp, in lane order.  Must be called by every active lane of the warp.
 __device__ __forceinline__ void append_warp(int32_t* list, unsigned long long* count, bool take, int32_t value) {
@@ -39,6 +77,19 @@ __device__ __forceinline__ void append_warp(int32_t* list, unsigned long long* c
     unsigned long long base = 0;
     if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(want));
     base = __shfl_sync(active, base, leader);
+    if (take) list[base + __popc(want & ((1u << lane) - 1u))] = value;
+}
+
+// The same for the lanes of `mask`, all of which must call it together.
+__device__ __forceinline__ void append_lanes(unsigned mask, int32_t* list, unsigned long long* count, bool take,
+                                             int32_t value) {
+    const unsigned want = __ballot_sync(mask, take);
+    if (!want) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(want) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(want));
+    base = __shfl_sync(mask, base, leader);
     if (take) list[base + __popc(want & ((1u << lane) - 1u))] = value;
 }
 

@@ -13,6 +13,9 @@ namespace {
 
 using namespace d3d;
 
+// slots a warp claims from the type-sorted order at a time
+constexpr int kChunk = 32;
+
 
 // Persistent FP64 GJK distance: each lane runs the reference's loop for one
 // pair at a time (one iteration per round) and fetches the next pair, in the
@@ -34,10 +37,15 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_distance_f64(d3d_store s, const i
     int64_t pid = 0;
     int a = 0, b = 0;
     bool need = true;
+    unsigned live = __activemask();  // the warp's lanes still in the loop
+    WarpChunk chunk;
     while (true) {
-        const long long slot = fetch_slot(cursor, need);
+        __syncwarp(live);
+        const long long slot = fetch_slot_chunked(cursor, need, chunk, live, kChunk);
+        const bool quit = need && slot >= n;
+        live = __ballot_sync(live, !quit);
+        if (quit) break;
         if (need) {
-            if (slot >= n) break;
             pid = order ? order[slot] : slot;
             a = i1[pid];
             b = i2[pid];

@@ -25,6 +25,7 @@ namespace {
 using namespace d3d;
 
 constexpr int kBlock = 128;
+constexpr int kChunk = 32;  // slots a warp claims from the type-sorted order at a time
 
 // Persistent MPR: each lane runs one pair's MPR one support evaluation per
 // round and fetches the next pair (in the type-sorted `order`) when its pair
@@ -44,10 +45,15 @@ __global__ void __launch_bounds__(kBlock) k_mpr(d3d_store st, const int32_t* __r
     int64_t pid = 0;
     int i = 0, j = 0;
     bool need = true;
+    unsigned live = __activemask();  // the warp's lanes still in the loop
+    WarpChunk chunk;
     while (true) {
-        const long long slot = fetch_slot(cursor, need);
+        __syncwarp(live);
+        const long long slot = fetch_slot_chunked(cursor, need, chunk, live, kChunk);
+        const bool quit = need && slot >= n;
+        live = __ballot_sync(live, !quit);
+        if (quit) break;
         if (need) {
-            if (slot >= n) break;
             pid = order ? order[slot] : slot;
             i = i1[pid];
             j = i2[pid];

@@ -275,11 +275,37 @@ constexpr unsigned kWarpAll = 0xffffffffu;
 __device__ __forceinline__ int lane_of() { return threadIdx.x & 31; }
 
 // Storage of one warp's polytope: cap_f faces (12 doubles and an ordering
-// key each), cap_e loose edges (6 doubles), cap_f visibility flags.
+// key each), cap_e loose edges (6 doubles, an id and 3 match flags each),
+// 3 flags, cap_f visibility flags.
 __host__ __device__ inline int exact_warp_bytes(int cap_f, int cap_e) {
     const int e = cap_e > 0 ? cap_e : 1;
-    return (104 * cap_f + 48 * e + cap_f + 15) & ~15;
+    return (104 * cap_f + 55 * e + 4 + cap_f + 15) & ~15;
 }
+
+struct WarpPoly {
+    double* F;               // faces: v0, v1, v2, n (12 doubles)
+    unsigned long long* K;   // ordering key of each face's distance
+    double* E;               // loose edges: a, b (6 doubles)
+    int* id;                 // the loose edge in each slot (see epa_pair_warp)
+    unsigned char* mf;       // mf[j * cap_e + k]: edge j of the face being removed matches loose edge k
+    unsigned char* sf;       // sf[j' + j - 1]: its edge j matches its own edge j' < j added as a loose edge
+    unsigned char* vis;      // visibility flags of the faces
+    int cap_e;
+
+    __device__ static WarpPoly at(unsigned char* base, int cap_f, int cap_e) {
+        const int e = cap_e > 0 ? cap_e : 1;
+        WarpPoly P;
+        P.F = reinterpret_cast<double*>(base);
+        P.K = reinterpret_cast<unsigned long long*>(P.F + 12 * (int64_t)cap_f);
+        P.E = reinterpret_cast<double*>(P.K + cap_f);
+        P.id = reinterpret_cast<int*>(P.E + 6 * (int64_t)e);
+        P.mf = reinterpret_cast<unsigned char*>(P.id + e);
+        P.sf = P.mf + 3 * e;
+        P.vis = P.sf + 4;
+        P.cap_e = e;
+        return P;
+    }
+};
 __host__ __device__ inline int exact_warp_bytes(const d3d_epa_options& o) {
     return exact_warp_bytes(o.max_faces, o.max_loose_edges);
 }
@@ -350,11 +376,14 @@ __device__ d3 minkowski_exact_warp(const d3d_store& st, int a, int b, d3 d) {
 // One pair's EPA by one warp (epa.py:9-78).  F, E, vis: the warp's faces,
 // loose edges and visibility flags in shared memory.  Returns the status;
 // mtv and nf (faces left) as k_epa sets them.
-// F: max_faces faces, K: their ordering keys, E: max_loose_edges edges,
-// vis: max_faces flags, all in the warp's shared memory.
+// The polytope of max_faces faces and max_loose_edges loose edges lives in
+// the warp's shared memory (WarpPoly).
 __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double* simplex,
-                             const d3d_epa_options& o, LengthBounds lb, double* F, unsigned long long* K, double* E,
-                             unsigned char* vis, d3& mtv, int& nf_out) {
+                             const d3d_epa_options& o, LengthBounds lb, const WarpPoly& P, d3& mtv, int& nf_out) {
+    double* const F = P.F;
+    unsigned long long* const K = P.K;
+    double* const E = P.E;
+    unsigned char* const vis = P.vis;
     const int ln = lane_of();
     const double eps = o.epsilon;
     // epa.py:56-57, 89-97: faces ABC, ACD, ADB, BDC
@@ -432,16 +461,49 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             }
             if (p < 0) break;
             const double* f = F + 12 * p;
-            for (int j = 0; j < 3; ++j) {  // epa.py:167-187
-                const d3 e0 = ld(f + 3 * j), e1 = ld(f + 3 * ((j + 1) % 3));
+            // epa.py:167-187 walks the face's edges j = 0, 1, 2 in order and
+            // takes, for each, the first loose edge it matches
+            // (epa.py:189-191), which the list then loses by a swap with its
+            // last edge, or else appends the edge.  Every match test is
+            // evaluated up front, in one pass over (edge, loose edge) pairs
+            // across the lanes: edge j against each loose edge k present now
+            // (mf), and against the face's own edges j' < j, which may be
+            // appended before edge j is looked up (sf).  The walk itself then
+            // follows the list's slots through their ids: k for loose edge k,
+            // ne0 + j' for the face's edge j'.
+            const int ne0 = ne;
+            for (int base = 0; base < 3 * ne0 + 3; base += 32) {
+                const int q = base + ln;
+                if (q < 3 * ne0 + 3) {
+                    int j, jj = 0;
+                    const double* e = nullptr;
+                    if (q < 3 * ne0) {
+                        j = q / ne0;
+                        e = E + 6 * (q - j * ne0);
+                    } else {
+                        jj = q - 3 * ne0 == 2 ? 1 : 0;     // (j', j): (0, 1), (0, 2), (1, 2)
+                        j = q - 3 * ne0 == 0 ? 1 : 2;
+                    }
+                    const d3 e0 = ld(f + 3 * j), e1 = ld(f + 3 * ((j + 1) % 3));
+                    const d3 ea = e ? ld(e) : ld(f + 3 * jj), eb = e ? ld(e + 3) : ld(f + 3 * (jj + 1));
+                    const d3 d1 = eb - e0, d0 = ea - e1;
+                    const unsigned char match = dot(d1, d1) < lb.edge && dot(d0, d0) < lb.edge;
+                    if (e)
+                        P.mf[j * P.cap_e + (q - j * ne0)] = match;
+                    else
+                        P.sf[jj + j - 1] = match;
+                }
+            }
+            for (int k = ln; k < ne0; k += 32) P.id[k] = k;
+            __syncwarp();
+            for (int j = 0; j < 3; ++j) {
                 int found = -1;
                 for (int kb = 0; kb < ne; kb += 32) {
                     const int k = kb + ln;
                     bool match = false;
                     if (k < ne) {
-                        const double* e = E + 6 * k;
-                        const d3 d1 = ld(e + 3) - e0, d0 = ld(e) - e1;
-                        match = dot(d1, d1) < lb.edge && dot(d0, d0) < lb.edge;
+                        const int id = P.id[k];
+                        match = id < ne0 ? P.mf[j * P.cap_e + id] != 0 : P.sf[(id - ne0) + j - 1] != 0;
                     }
                     const unsigned m = __ballot_sync(kWarpAll, match);
                     if (m) {
@@ -451,6 +513,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 }
                 if (found >= 0) {
                     if (ln < 6) E[6 * found + ln] = E[6 * (ne - 1) + ln];
+                    if (ln == 0) P.id[found] = P.id[ne - 1];
                     --ne;
                 } else {
                     if (ne >= o.max_loose_edges) break;  // epa.py:193-198
@@ -458,6 +521,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                         E[6 * ne + ln] = f[3 * j + ln];
                         E[6 * ne + 3 + ln] = f[3 * ((j + 1) % 3) + ln];
                     }
+                    if (ln == 0) P.id[ne] = ne0 + j;
                     ++ne;
                 }
                 __syncwarp();
@@ -531,11 +595,7 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
                                  double* __restrict__ faces) {
     extern __shared__ __align__(16) unsigned char smem_epa[];
     const int ln = lane_of();
-    const int e = o.max_loose_edges > 0 ? o.max_loose_edges : 1;
-    double* F = reinterpret_cast<double*>(smem_epa);
-    unsigned long long* K = reinterpret_cast<unsigned long long*>(F + 12 * (int64_t)o.max_faces);
-    double* E = reinterpret_cast<double*>(K + o.max_faces);
-    unsigned char* vis = reinterpret_cast<unsigned char*>(E + 6 * (int64_t)e);
+    const WarpPoly P = WarpPoly::at(smem_epa, o.max_faces, o.max_loose_edges);
     if (n_dev) n = (int64_t)*n_dev;
     while (true) {
         long long slot = 0;
@@ -545,7 +605,7 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
         const int64_t pid = list ? list[slot] : slot;
         d3 m;
         int nf = 0;
-        const int stt = epa_pair_warp(s, i1[pid], i2[pid], simplex + 12 * pid, o, lb, F, K, E, vis, m, nf);
+        const int stt = epa_pair_warp(s, i1[pid], i2[pid], simplex + 12 * pid, o, lb, P, m, nf);
         if (ln == 0) {
             mtv[3 * pid] = m.x;
             mtv[3 * pid + 1] = m.y;
@@ -555,7 +615,7 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
         }
         if (faces && stt != D3D_STATUS_EPA_DEGENERATE) {
             double* out = faces + pid * 12 * (int64_t)o.max_faces;
-            for (int j = ln; j < 12 * nf; j += 32) out[j] = F[j];
+            for (int j = ln; j < 12 * nf; j += 32) out[j] = P.F[j];
         }
         __syncwarp();
     }

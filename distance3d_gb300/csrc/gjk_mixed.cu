@@ -42,11 +42,25 @@ using namespace d3d;
 
 
 // Per-call counters (one 256-byte block): cursors of A, B and C, then the
-// length of the fallback list.
-enum { kCurA = 0, kCurB, kCurC, kNumFallback, kCounters };
+// lengths of the fallback and finished lists.
+enum { kCurA = 0, kCurB, kCurC, kNumFallback, kNumEnd, kCounters };
+
+// B's state of a pair whose loop has ended, for the end pass (the simplex's
+// Y rows and row count go to the outputs directly).
+struct alignas(16) EndRecord {
+    double pq[4][6];  // P and Q rows below n
+    double dir[3];
+    double vl;
+    int it;  // A's and B's iterations
+    int state;
+    int status;
+    int n;
+};
 
 struct Lists {
     int32_t* fallback;
+    int32_t* ends;         // pairs whose FP64 loop ended in B, for the end pass
+    EndRecord* records;    // their state, by pair
     unsigned long long* ctr;
 };
 
@@ -131,14 +145,86 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
             need = false;
         }
         if (B.mode == PB_FALLBACK || pb_round<MESH>(B, s, a, b, hand[pid].d, tol_sq, opt, E)) {
-            GjkResult<double> r;
-            if (B.mode != PB_FALLBACK && pb_end(B.g, opt, E, r) == PB_DONE) {
-                r.iters += it_a;
-                store_result(o, pid, r, B.g.S);
+            if (B.mode != PB_FALLBACK) {
+                // The closest points and checks of the pair (pb_end) run in
+                // the end pass, where a warp's lanes all hold finished pairs;
+                // here only a few lanes finish per round.
+                const GjkLoop<double, SmemRows<double, BLOCK>>& g = B.g;
+                EndRecord& e = lists.records[pid];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (k < g.S.n) {
+                        const d3 pk = g.S.R.p(k), qk = g.S.R.q(k);
+                        e.pq[k][0] = pk.x;
+                        e.pq[k][1] = pk.y;
+                        e.pq[k][2] = pk.z;
+                        e.pq[k][3] = qk.x;
+                        e.pq[k][4] = qk.y;
+                        e.pq[k][5] = qk.z;
+                    }
+                }
+                e.dir[0] = g.dir.x;
+                e.dir[1] = g.dir.y;
+                e.dir[2] = g.dir.z;
+                e.vl = g.vl;
+                e.it = g.it + it_a;
+                e.state = g.state;
+                e.status = g.status;
+                e.n = g.S.n;
+                double* sp = o.simplex + 12 * (int64_t)pid;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    sp[3 * j] = g.S.Y[j].x;
+                    sp[3 * j + 1] = g.S.Y[j].y;
+                    sp[3 * j + 2] = g.S.Y[j].z;
+                }
+                o.n_simplex[pid] = (int8_t)g.S.n;
+                append_warp(lists.ends, lists.ctr + kNumEnd, true, pid);
             } else {
                 lists.fallback[atomicAdd(lists.ctr + kNumFallback, 1ull)] = pid;
             }
             need = true;
+        }
+    }
+}
+
+// The end pass over B's finished pairs: closest points, sanity and
+// consistency checks (pb_end) and the outputs; pairs failing a check go to
+// the fallback list.
+__global__ void __launch_bounds__(128) k_gjk_mixed_end(d3d_gjk_options opt, DistanceOut o, Lists lists) {
+    const int64_t n = (int64_t)lists.ctr[kNumEnd];
+    const JoltEps<double> E = reference_eps<double>();
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t pid = lists.ends[k];
+        const EndRecord& e = lists.records[pid];
+        GjkLoop<double, RegRows<double>> g;
+        g.S.n = e.n;
+        const double* sp = o.simplex + 12 * (int64_t)pid;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            g.S.Y[j] = mk(sp[3 * j], sp[3 * j + 1], sp[3 * j + 2]);
+            if (j < e.n)
+                g.S.R.put(j, mk(e.pq[j][0], e.pq[j][1], e.pq[j][2]), mk(e.pq[j][3], e.pq[j][4], e.pq[j][5]));
+        }
+        g.dir = mk(e.dir[0], e.dir[1], e.dir[2]);
+        g.vl = e.vl;
+        g.prev = 0.0;
+        g.it = e.it;
+        g.state = e.state;
+        g.status = e.status;
+        GjkResult<double> r;
+        if (pb_end(g, opt, E, r) == PB_DONE) {
+            o.dist[pid] = r.dist;
+            o.cp1[3 * (int64_t)pid] = r.a.x;
+            o.cp1[3 * (int64_t)pid + 1] = r.a.y;
+            o.cp1[3 * (int64_t)pid + 2] = r.a.z;
+            o.cp2[3 * (int64_t)pid] = r.b.x;
+            o.cp2[3 * (int64_t)pid + 1] = r.b.y;
+            o.cp2[3 * (int64_t)pid + 2] = r.b.z;
+            o.status[pid] = (int8_t)r.status;
+            if (o.iterations) o.iterations[pid] = r.iters;
+        } else {
+            lists.fallback[atomicAdd(lists.ctr + kNumFallback, 1ull)] = pid;
         }
     }
 }
@@ -151,7 +237,8 @@ namespace d3d {
 
 size_t gjk_mixed_scratch_bytes(int64_t capacity) {
     return 256 + up(sizeof(int32_t) * (size_t)capacity) + pair_order_temp_bytes(capacity) +
-           up(sizeof(Handoff) * (size_t)capacity) + up(sizeof(int32_t) * (size_t)capacity);
+           up(sizeof(Handoff) * (size_t)capacity) + 2 * up(sizeof(int32_t) * (size_t)capacity) +
+           up(sizeof(EndRecord) * (size_t)capacity);
 }
 
 template <int BLOCK, bool MESH>
@@ -167,7 +254,10 @@ int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, c
     const void* kb = (const void*)k_gjk_mixed_b<BLOCK, MESH>;
     k_gjk_mixed_b<BLOCK, MESH><<<persistent_blocks(kb, BLOCK, n, per_sm), BLOCK, 0, stream>>>(
         store, i1, i2, order, n, n_dev, opt, hand, o, lists);
-    return check_launch("d3d_gjk_distance (mixed, FP64 phase)");
+    rc = check_launch("d3d_gjk_distance (mixed, FP64 phase)");
+    if (rc) return rc;
+    k_gjk_mixed_end<<<persistent_blocks((const void*)k_gjk_mixed_end, 128, n), 128, 0, stream>>>(opt, o, lists);
+    return check_launch("d3d_gjk_distance (mixed, end pass)");
 }
 
 // The kernels without the MeshGraph branch serve stores without meshes.
@@ -197,6 +287,10 @@ int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, 
     Handoff* hand = reinterpret_cast<Handoff*>(p);
     p += up(sizeof(Handoff) * (size_t)n);
     lists.fallback = reinterpret_cast<int32_t*>(p);
+    p += up(sizeof(int32_t) * (size_t)n);
+    lists.ends = reinterpret_cast<int32_t*>(p);
+    p += up(sizeof(int32_t) * (size_t)n);
+    lists.records = reinterpret_cast<EndRecord*>(p);
     cudaError_t e = cudaMemsetAsync(lists.ctr, 0, kCounters * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) {
         set_error("d3d_gjk_distance (mixed): %s", cudaGetErrorString(e));

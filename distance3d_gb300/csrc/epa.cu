@@ -274,41 +274,51 @@ constexpr unsigned kWarpAll = 0xffffffffu;
 
 __device__ __forceinline__ int lane_of() { return threadIdx.x & 31; }
 
-// Storage of one warp's polytope: cap_f faces (12 doubles and an ordering
-// key each), cap_e loose edges (6 doubles, an id and 3 match flags each),
-// 3 flags, cap_f visibility flags.
-__host__ __device__ inline int exact_warp_bytes(int cap_f, int cap_e) {
+// Storage of one warp's polytope, for cap_f faces, cap_e loose edges and
+// nvc vertices (see WarpPoly).
+__host__ __device__ inline int pm_words(int nvc) { return (nvc + 31) / 32; }
+__host__ __device__ inline int exact_warp_bytes(int cap_f, int cap_e, int nvc) {
     const int e = cap_e > 0 ? cap_e : 1;
-    return (104 * cap_f + 55 * e + 4 + cap_f + 15) & ~15;
+    return (104 * cap_f + 48 * e + 24 * nvc + 4 * nvc * pm_words(nvc) + 4 * cap_f + 2 * e + cap_f + 15) & ~15;
+}
+__host__ __device__ inline int exact_warp_bytes(const d3d_epa_options& o) {
+    return exact_warp_bytes(o.max_faces, o.max_loose_edges, o.max_iterations + 4);
 }
 
+// One warp's polytope in shared memory.  Every point of the polytope is one
+// of its vertices: the simplex's four points and one support point per
+// iteration (at most nvc = max_iterations + 4), and faces and loose edges
+// hold bit-exact copies of them.  Vertex ids ride along with the copies, and
+// pm holds the reference's closeness test between two points
+// (norm(x - y) < epsilon, epa.py:189-191) for every pair of vertices, so
+// that matching loose edges needs no arithmetic.
 struct WarpPoly {
-    double* F;               // faces: v0, v1, v2, n (12 doubles)
-    unsigned long long* K;   // ordering key of each face's distance
-    double* E;               // loose edges: a, b (6 doubles)
-    int* id;                 // the loose edge in each slot (see epa_pair_warp)
-    unsigned char* mf;       // mf[j * cap_e + k]: edge j of the face being removed matches loose edge k
-    unsigned char* sf;       // sf[j' + j - 1]: its edge j matches its own edge j' < j added as a loose edge
-    unsigned char* vis;      // visibility flags of the faces
-    int cap_e;
+    double* F;              // faces: v0, v1, v2, n (12 doubles)
+    unsigned long long* K;  // ordering key of each face's distance
+    double* E;              // loose edges: a, b (6 doubles)
+    double* V;              // vertices (3 doubles)
+    unsigned* pm;           // bit y of row x (words x * W ...): vertices x and y are close
+    unsigned* fid;          // vertex ids of each face's corners, 8 bits each
+    unsigned short* eid;    // vertex ids of each loose edge's ends, 8 bits each
+    unsigned char* vis;     // visibility flags of the faces
+    int W;                  // words per row of pm
 
-    __device__ static WarpPoly at(unsigned char* base, int cap_f, int cap_e) {
+    __device__ static WarpPoly at(unsigned char* base, int cap_f, int cap_e, int nvc) {
         const int e = cap_e > 0 ? cap_e : 1;
         WarpPoly P;
         P.F = reinterpret_cast<double*>(base);
         P.K = reinterpret_cast<unsigned long long*>(P.F + 12 * (int64_t)cap_f);
         P.E = reinterpret_cast<double*>(P.K + cap_f);
-        P.id = reinterpret_cast<int*>(P.E + 6 * (int64_t)e);
-        P.mf = reinterpret_cast<unsigned char*>(P.id + e);
-        P.sf = P.mf + 3 * e;
-        P.vis = P.sf + 4;
-        P.cap_e = e;
+        P.V = P.E + 6 * (int64_t)e;
+        P.W = pm_words(nvc);
+        P.pm = reinterpret_cast<unsigned*>(P.V + 3 * nvc);
+        P.fid = P.pm + nvc * P.W;
+        P.eid = reinterpret_cast<unsigned short*>(P.fid + cap_f);
+        P.vis = reinterpret_cast<unsigned char*>(P.eid + e);
         return P;
     }
+    __device__ bool close(int x, int y) const { return (pm[x * W + (y >> 5)] >> (y & 31)) & 1u; }
 };
-__host__ __device__ inline int exact_warp_bytes(const d3d_epa_options& o) {
-    return exact_warp_bytes(o.max_faces, o.max_loose_edges);
-}
 
 // Ordering key of a face distance: unsigned order equals the order of the
 // doubles (-0 as +0); NaN sorts last.
@@ -386,16 +396,25 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
     unsigned char* const vis = P.vis;
     const int ln = lane_of();
     const double eps = o.epsilon;
+    // vertices 0-3: the simplex's rows, and their closeness
+    if (ln < 12) P.V[ln] = simplex[ln];
+    __syncwarp();
+    {
+        const d3 d = ld(P.V + 3 * ((ln >> 2) & 3)) - ld(P.V + 3 * (ln & 3));
+        const unsigned m = __ballot_sync(kWarpAll, ln < 16 && dot(d, d) < lb.edge);
+        if (ln < 4) P.pm[ln * P.W] = (m >> (4 * ln)) & 0xfu;
+    }
     // epa.py:56-57, 89-97: faces ABC, ACD, ADB, BDC
     if (ln < 4) {
         const int init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
         double* f = F + 12 * ln;
-        for (int j = 0; j < 3; ++j) st(f + 3 * j, ld(simplex + 3 * init[ln][j]));
+        for (int j = 0; j < 3; ++j) st(f + 3 * j, ld(P.V + 3 * init[ln][j]));
         face_normal(f);
         K[ln] = dist_key(face_dist(f));
+        P.fid[ln] = (unsigned)init[ln][0] | ((unsigned)init[ln][1] << 8) | ((unsigned)init[ln][2] << 16);
     }
     __syncwarp();
-    int nf = 4, closest = 0;
+    int nf = 4, closest = 0, nv = 4;
     for (int it = 0;; ++it) {
         if (it >= o.max_iterations) {
             // epa.py:77: closest_face is a view, read after the last iteration's edits
@@ -441,6 +460,25 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             nf_out = nf;
             return D3D_STATUS_OK;
         }
+        // w becomes vertex wv: its closeness to every vertex (itself
+        // included) fills row wv and column wv of pm
+        const int wv = nv++;
+        if (ln < 3) P.V[3 * wv + ln] = ln == 0 ? w.x : (ln == 1 ? w.y : w.z);
+        for (int kb = 0; kb <= wv; kb += 32) {
+            const int k = kb + ln;
+            bool c = false;
+            if (k <= wv) {
+                const d3 d = (k == wv ? w : ld(P.V + 3 * k)) - w;
+                c = dot(d, d) < lb.edge;
+            }
+            const unsigned m = __ballot_sync(kWarpAll, c);
+            if (ln == 0) P.pm[wv * P.W + (kb >> 5)] = m;
+            if (k < wv) {
+                unsigned& word = P.pm[k * P.W + (wv >> 5)];
+                const unsigned bit = (c ? 1u : 0u) << (wv & 31);
+                word = (wv & 31) == 0 ? bit : (word | bit);
+            }
+        }
         // epa.py:157-165: visibility of every face (epa.py:122-124)
         for (int i = ln; i < nf; i += 32) {
             const double* f = F + 12 * i;
@@ -461,49 +499,20 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             }
             if (p < 0) break;
             const double* f = F + 12 * p;
-            // epa.py:167-187 walks the face's edges j = 0, 1, 2 in order and
-            // takes, for each, the first loose edge it matches
-            // (epa.py:189-191), which the list then loses by a swap with its
-            // last edge, or else appends the edge.  Every match test is
-            // evaluated up front, in one pass over (edge, loose edge) pairs
-            // across the lanes: edge j against each loose edge k present now
-            // (mf), and against the face's own edges j' < j, which may be
-            // appended before edge j is looked up (sf).  The walk itself then
-            // follows the list's slots through their ids: k for loose edge k,
-            // ne0 + j' for the face's edge j'.
-            const int ne0 = ne;
-            for (int base = 0; base < 3 * ne0 + 3; base += 32) {
-                const int q = base + ln;
-                if (q < 3 * ne0 + 3) {
-                    int j, jj = 0;
-                    const double* e = nullptr;
-                    if (q < 3 * ne0) {
-                        j = q / ne0;
-                        e = E + 6 * (q - j * ne0);
-                    } else {
-                        jj = q - 3 * ne0 == 2 ? 1 : 0;     // (j', j): (0, 1), (0, 2), (1, 2)
-                        j = q - 3 * ne0 == 0 ? 1 : 2;
-                    }
-                    const d3 e0 = ld(f + 3 * j), e1 = ld(f + 3 * ((j + 1) % 3));
-                    const d3 ea = e ? ld(e) : ld(f + 3 * jj), eb = e ? ld(e + 3) : ld(f + 3 * (jj + 1));
-                    const d3 d1 = eb - e0, d0 = ea - e1;
-                    const unsigned char match = dot(d1, d1) < lb.edge && dot(d0, d0) < lb.edge;
-                    if (e)
-                        P.mf[j * P.cap_e + (q - j * ne0)] = match;
-                    else
-                        P.sf[jj + j - 1] = match;
-                }
-            }
-            for (int k = ln; k < ne0; k += 32) P.id[k] = k;
-            __syncwarp();
+            const unsigned fv = P.fid[p];
+            // epa.py:167-187: edge j = (v_j, v_j+1) of the face matches loose
+            // edge (a, b) when b is close to v_j and a to v_j+1
+            // (epa.py:189-191); the first match leaves the list by a swap with
+            // its last edge, no match appends the edge
             for (int j = 0; j < 3; ++j) {
+                const int x0 = (fv >> (8 * j)) & 0xff, x1 = (fv >> (8 * ((j + 1) % 3))) & 0xff;
                 int found = -1;
                 for (int kb = 0; kb < ne; kb += 32) {
                     const int k = kb + ln;
                     bool match = false;
                     if (k < ne) {
-                        const int id = P.id[k];
-                        match = id < ne0 ? P.mf[j * P.cap_e + id] != 0 : P.sf[(id - ne0) + j - 1] != 0;
+                        const unsigned e = P.eid[k];
+                        match = P.close(e >> 8, x0) && P.close(e & 0xff, x1);
                     }
                     const unsigned m = __ballot_sync(kWarpAll, match);
                     if (m) {
@@ -513,7 +522,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 }
                 if (found >= 0) {
                     if (ln < 6) E[6 * found + ln] = E[6 * (ne - 1) + ln];
-                    if (ln == 0) P.id[found] = P.id[ne - 1];
+                    if (ln == 0) P.eid[found] = P.eid[ne - 1];
                     --ne;
                 } else {
                     if (ne >= o.max_loose_edges) break;  // epa.py:193-198
@@ -521,7 +530,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                         E[6 * ne + ln] = f[3 * j + ln];
                         E[6 * ne + 3 + ln] = f[3 * ((j + 1) % 3) + ln];
                     }
-                    if (ln == 0) P.id[ne] = ne0 + j;
+                    if (ln == 0) P.eid[ne] = (unsigned short)(x0 | (x1 << 8));
                     ++ne;
                 }
                 __syncwarp();
@@ -531,6 +540,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             if (ln == 0) {
                 vis[p] = vis[nf - 1];
                 K[p] = K[nf - 1];
+                P.fid[p] = P.fid[nf - 1];
             }
             --nf;
             i = p;
@@ -542,12 +552,15 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             const int k = kb + ln;
             double nfa[12];
             bool keep = false;
+            unsigned ids = 0;
             if (k < ne) {
                 const double* e = E + 6 * k;
                 for (int q = 0; q < 6; ++q) nfa[q] = e[q];
                 nfa[6] = w.x;
                 nfa[7] = w.y;
                 nfa[8] = w.z;
+                const unsigned ev = P.eid[k];
+                ids = (ev & 0xffu) | (ev & 0xff00u) | ((unsigned)wv << 16);
                 face_normal(nfa);
                 const d3 n = ld(nfa + 9);
                 keep = !(dot(n, n) < lb.keep);
@@ -556,6 +569,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 if (keep && dot(ld(nfa), n) + 1e-6 < 0.0) {
                     st(nfa, ld(nfa + 3));
                     st(nfa + 9, -n);
+                    ids = (ids & ~0xffu) | ((ids >> 8) & 0xffu);
                 }
             }
             const unsigned km = __ballot_sync(kWarpAll, keep);
@@ -569,6 +583,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 double* dst = F + 12 * idx;
                 for (int q = 0; q < 12; ++q) dst[q] = nfa[q];
                 K[idx] = dist_key(face_dist(nfa));
+                P.fid[idx] = ids;
             }
             if (om) {
                 nf += kept + __popc(km & ((1u << limit) - 1u));
@@ -595,7 +610,7 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
                                  double* __restrict__ faces) {
     extern __shared__ __align__(16) unsigned char smem_epa[];
     const int ln = lane_of();
-    const WarpPoly P = WarpPoly::at(smem_epa, o.max_faces, o.max_loose_edges);
+    const WarpPoly P = WarpPoly::at(smem_epa, o.max_faces, o.max_loose_edges, o.max_iterations + 4);
     if (n_dev) n = (int64_t)*n_dev;
     while (true) {
         long long slot = 0;
@@ -624,7 +639,9 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
 constexpr int64_t kExactSmemPerBlock = 227 * 1024;
 
 bool exact_warp_supported(const d3d_epa_options& o) {
-    return o.max_faces <= 65536 && o.max_loose_edges <= 65536 && (int64_t)exact_warp_bytes(o) <= kExactSmemPerBlock;
+    // vertex ids fit in 8 bits
+    return o.max_iterations <= 251 && o.max_faces <= 65536 && o.max_loose_edges <= 65536 &&
+           (int64_t)exact_warp_bytes(o) <= kExactSmemPerBlock;
 }
 
 // One warp per block, each block holding one polytope, as many per SM as

@@ -70,6 +70,27 @@ def test_epa_polytope_sizes(max_faces, max_edges):
         assert (ref["n_faces"] > 64).sum() > 10
 
 
+@pytest.mark.parametrize("kw,with_faces", [(dict(max_iter=300, max_faces=256, max_loose_edges=128), True),
+                                           (dict(max_faces=4096, max_loose_edges=512), False)])
+def test_epa_beyond_warp_form(kw, with_faces):
+    """Options the one-warp-per-pair kernel does not take (more than 251
+    iterations: vertex ids beyond 8 bits; a polytope beyond the shared memory
+    of a block) run in the thread-per-pair kernel, bit for bit the oracle's."""
+    cs, i1, i2 = workloads.pairs_all_types(3000, seed=35)
+    st = ColliderStore(cs)
+    g = host(gjk_distance_batch(st, i1, i2))
+    hit = np.flatnonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4))
+    r = host(epa_batch(st, i1[hit], i2[hit], g["simplex"][hit], return_faces=with_faces, **kw))
+    ref = oracle.epa(cs, i1[hit], i2[hit], g["simplex"][hit], want_faces=with_faces, **kw)
+    assert np.array_equal(r["status"], ref["status"])
+    assert np.array_equal(r["n_faces"], ref["n_faces"])
+    assert np.array_equal(r["mtv"], ref["mtv"], equal_nan=True)
+    if with_faces:
+        for k in range(len(hit)):
+            nf = r["n_faces"][k]
+            assert np.array_equal(r["faces"][k, :nf], ref["faces"][k, :nf])
+
+
 def test_epa_many_pairs_reuse_slots():
     """More pairs than scratch slots: every pair still gets its own answer."""
     cs, i1, i2 = workloads.pairs_mixed_six(200000, seed=32, center_half_width=workloads.INTERSECT30_HALF_WIDTH)

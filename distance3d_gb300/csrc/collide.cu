@@ -25,7 +25,7 @@ constexpr int64_t kFallbackSlots = 2048;  // FP64 EPA polytopes for the mixed fo
 
 // counters: EPA cursor, FP64 cursor, fallback count, EPA list length, FP64
 // warp cursor, second fallback count
-enum { kEpaCur = 0, kF64Cur, kNumFallback, kNumEpa, kW64Cur, kNumFallback2, kCounters };
+enum { kEpaCur = 0, kF64Cur, kNumFallback, kNumEpa, kW64Cur, kNumFallback2, kNumRefine, kCounters };
 
 inline size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -68,7 +68,7 @@ __global__ void k_epa_select(int64_t cap, const int64_t* __restrict__ n_dev, con
 extern "C" size_t d3d_collide_scratch_bytes(int64_t capacity, const d3d_gjk_options* gjk,
                                             const d3d_epa_options* epa) {
     if (capacity <= 0 || !gjk || !epa || epa->max_faces < 4) return 0;
-    return 256 + 3 * up(sizeof(int32_t) * (size_t)capacity) + up(gjk_bytes(capacity, *gjk)) +
+    return 256 + 4 * up(sizeof(int32_t) * (size_t)capacity) + up(gjk_bytes(capacity, *gjk)) +
            (size_t)(f64_slots(capacity, *epa) * epa_f64_slot_bytes(*epa));
 }
 
@@ -106,6 +106,8 @@ extern "C" int d3d_collide(const d3d_store* store, const int32_t* i1, const int3
     p += up(sizeof(int32_t) * (size_t)capacity);
     int32_t* fallback2 = reinterpret_cast<int32_t*>(p);
     p += up(sizeof(int32_t) * (size_t)capacity);
+    int32_t* refine = reinterpret_cast<int32_t*>(p);
+    p += up(sizeof(int32_t) * (size_t)capacity);
     void* gjk_scratch = p;
     p += up(gjk_bytes(capacity, *gjk));
     void* slots = p;
@@ -128,7 +130,8 @@ extern "C" int d3d_collide(const d3d_store* store, const int32_t* i1, const int3
     const int64_t nslots = f64_slots(capacity, *epa);
     if (warp_form(*epa)) {
         rc = d3d::epa_warp_launch(*store, i1, i2, list, capacity, ctr + kNumEpa, ctr + kEpaCur, simplex, *epa, mtv,
-                                  epa_status, n_faces, nullptr, fallback, ctr + kNumFallback, st);
+                                  epa_status, n_faces, nullptr, fallback, ctr + kNumFallback, st, false, refine,
+                                  ctr + kNumRefine);
         const bool w64 = d3d::epa_warp_supported(*epa, true);
         if (!rc && w64)
             rc = d3d::epa_warp_launch(*store, i1, i2, fallback, capacity, ctr + kNumFallback, ctr + kW64Cur, simplex,

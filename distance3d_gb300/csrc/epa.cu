@@ -739,23 +739,26 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
     const bool sched = n >= kScheduleMin && !warp && !exact_warp_supported(*options);
     const size_t up_n = (sizeof(int32_t) * (size_t)n + 255) & ~size_t(255);
     const size_t order_bytes = sched ? up_n : 0;
-    const size_t fb_bytes = mixed ? 2 * up_n : 0;  // fallback lists of the FP32 and FP64 warp searches
+    // fallback lists of the FP32 and FP64 warp searches, the FP32 search's refinement list
+    const size_t fb_bytes = mixed ? 3 * up_n : 0;
     const size_t temp_bytes = sched ? (d3d::pair_order_temp_bytes(n) + 255) & ~size_t(255) : 0;
     void* block = nullptr;
     rc = d3d::scratch_alloc(&block, 256 + order_bytes + fb_bytes + temp_bytes, st);
     if (rc) return rc;
     char* p = static_cast<char*>(block);
-    // counters: cursor, FP64 EPA cursor, fallback count, FP64 warp cursor, second fallback count
+    // counters: cursor, FP64 EPA cursor, fallback count, FP64 warp cursor, second fallback count,
+    // refinement count
     unsigned long long* ctr = reinterpret_cast<unsigned long long*>(p);
     int32_t* order = sched ? reinterpret_cast<int32_t*>(p + 256) : nullptr;
     int32_t* fallback = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes) : nullptr;
     int32_t* fallback2 = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes + up_n) : nullptr;
+    int32_t* refine = mixed ? reinterpret_cast<int32_t*>(p + 256 + order_bytes + 2 * up_n) : nullptr;
     const bool warp64 = warp && d3d::epa_warp_supported(*options, true);
-    cudaMemsetAsync(ctr, 0, 5 * sizeof(unsigned long long), st);
+    cudaMemsetAsync(ctr, 0, 6 * sizeof(unsigned long long), st);
     if (sched) rc = d3d::pair_order(*store, i1, i2, n, order, p + 256 + order_bytes + fb_bytes, temp_bytes, st);
     if (!rc && warp) {
         rc = d3d::epa_warp_launch(*store, i1, i2, nullptr, n, nullptr, ctr, simplex, *options, mtv, status, n_faces,
-                                  faces, fallback, ctr + 2, st);
+                                  faces, fallback, ctr + 2, st, false, refine, ctr + 5);
         if (!rc && warp64)
             rc = d3d::epa_warp_launch(*store, i1, i2, fallback, n, ctr + 2, ctr + 3, simplex, *options, mtv, status,
                                       n_faces, faces, fallback2, ctr + 4, st, true);

@@ -28,12 +28,16 @@ int epa_mixed_launch(const d3d_store& store, const int32_t* i1, const int32_t* i
 // max_iterations <= 250, max_loose_edges <= 255 and four polytopes fit in a
 // block's shared memory.  Runs pairs list[k] (or k) for k < n, or
 // k < *n_dev if n_dev is given (n then only sizes the launch); fallback pairs
-// as above.
+// as above.  With `refine` (FP32 form only), each converged pair's FP32 face
+// normal goes to mtv and the pair to refine[*n_refine ...] (the caller zeroes
+// the count), and a second kernel then computes the pairs' FP64 depths along
+// those normals, one pair per thread.
 bool epa_warp_supported(const d3d_epa_options& o, bool fp64 = false);
 int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                     const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                     const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64 = false);
+                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64 = false,
+                    int32_t* refine = nullptr, unsigned long long* n_refine = nullptr);
 
 // The FP64 EPA (epa.cu) over list[k] (or k) for k < n or < *n_dev, on
 // `slots` polytope slots of slot_bytes(o) in `scratch`.

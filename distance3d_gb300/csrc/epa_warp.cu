@@ -592,7 +592,9 @@ __global__ void __launch_bounds__(32 * WARPS, kWarpsPerSm<T> / WARPS) k_epa_warp
                                                           double* __restrict__ mtv, int8_t* __restrict__ status,
                                                           int32_t* __restrict__ n_faces, double* __restrict__ faces,
                                                           int32_t* __restrict__ fallback,
-                                                          unsigned long long* __restrict__ n_fallback) {
+                                                          unsigned long long* __restrict__ n_fallback,
+                                                          int32_t* __restrict__ refine,
+                                                          unsigned long long* __restrict__ n_refine) {
     extern __shared__ __align__(16) unsigned char smem[];
     const Layout L = layout_for<T>(o);
     const Poly<T> P = poly_at<T>(smem + (threadIdx.x >> 5) * L.bytes, L);
@@ -613,7 +615,16 @@ __global__ void __launch_bounds__(32 * WARPS, kWarpsPerSm<T> / WARPS) k_epa_warp
             continue;
         }
         d3 m = mk(double(NAN), double(NAN), double(NAN));
-        if (R.status == D3D_STATUS_OK || R.status == D3D_STATUS_EPA_NOT_CONVERGED) m = refine_face<MESH>(P, st, a, b, R.closest);
+        const bool ended = R.status == D3D_STATUS_OK || R.status == D3D_STATUS_EPA_NOT_CONVERGED;
+        if (ended) {
+            if (refine) {
+                // the face's normal now; the FP64 depth along it in k_epa_refine
+                const Q4<T> q = P.fn[R.closest];
+                m = mk((double)q.x, (double)q.y, (double)q.z);
+            } else {
+                m = refine_face<MESH>(P, st, a, b, R.closest);
+            }
+        }
         const int nf = R.status == D3D_STATUS_EPA_DEGENERATE ? 0 : R.live;
         if (ln == 0) {
             mtv[3 * k] = m.x;
@@ -621,6 +632,7 @@ __global__ void __launch_bounds__(32 * WARPS, kWarpsPerSm<T> / WARPS) k_epa_warp
             mtv[3 * k + 2] = m.z;
             status[k] = (int8_t)R.status;
             n_faces[k] = nf;
+            if (refine && ended) refine[atomicAdd(n_refine, 1ull)] = (int32_t)k;
         }
         if (faces && nf > 0) {
             // live faces in slot order: three vertices and the normal
@@ -652,6 +664,29 @@ __global__ void __launch_bounds__(32 * WARPS, kWarpsPerSm<T> / WARPS) k_epa_warp
     }
 }
 
+// The FP64 refinement of the FP32 search's converged faces (refine_face),
+// one pair per thread: the normal the search left in mtv, renormalised in
+// FP64, and mtv = n (n . w(n)) with RefineSupport.  In the search kernel the
+// whole warp waited on each pair's FP64 support chain.
+template <bool MESH>
+__global__ void __launch_bounds__(128) k_epa_refine(d3d_store st, const int32_t* __restrict__ i1,
+                                                    const int32_t* __restrict__ i2, const int32_t* __restrict__ list,
+                                                    const unsigned long long* __restrict__ n_dev,
+                                                    double* __restrict__ mtv) {
+    const int64_t n = (int64_t)*n_dev;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = list[j];
+        d3 nrm = mk(mtv[3 * k], mtv[3 * k + 1], mtv[3 * k + 2]);
+        nrm = nrm * (1.0 / sqrt(dot(nrm, nrm)));
+        d3 p, q;
+        pair_supports<double, RefineSupportT<MESH>>(st, i1[k], i2[k], nrm, p, q);
+        const d3 m = nrm * dot(p - q, nrm);
+        mtv[3 * k] = m.x;
+        mtv[3 * k + 1] = m.y;
+        mtv[3 * k + 2] = m.z;
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -660,7 +695,8 @@ template <typename T, int WARPS, bool MESH>
 int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                 const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                 const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
+                int32_t* fallback, unsigned long long* n_fallback, int32_t* refine, unsigned long long* n_refine,
+                cudaStream_t stream) {
     const void* fn = (const void*)k_epa_warp<T, WARPS, MESH>;
     const int smem = layout_for<T>(o).bytes * WARPS;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -674,8 +710,12 @@ int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, co
     const int blocks = persistent_blocks(fn, 32 * WARPS, n * 32, 0, smem);
     k_epa_warp<T, WARPS, MESH><<<blocks, 32 * WARPS, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex,
                                                                      o, mtv, status, n_faces, faces, fallback,
-                                                                     n_fallback);
-    return check_launch("d3d_epa (mixed)");
+                                                                     n_fallback, refine, n_refine);
+    int rc = check_launch("d3d_epa (mixed)");
+    if (rc || !refine) return rc;
+    const void* kr = (const void*)k_epa_refine<MESH>;
+    k_epa_refine<MESH><<<persistent_blocks(kr, 128, n), 128, 0, stream>>>(store, i1, i2, refine, n_refine, mtv);
+    return check_launch("d3d_epa (mixed, refinement)");
 }
 
 // The kernels without the MeshGraph branch serve stores without meshes.
@@ -683,12 +723,13 @@ template <typename T, int WARPS>
 int launch_warp(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                 const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                 const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream) {
+                int32_t* fallback, unsigned long long* n_fallback, int32_t* refine, unsigned long long* n_refine,
+                cudaStream_t stream) {
     if (store.n_links > 0)
         return launch_warp<T, WARPS, true>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces,
-                                           faces, fallback, n_fallback, stream);
+                                           faces, fallback, n_fallback, refine, n_refine, stream);
     return launch_warp<T, WARPS, false>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces,
-                                        faces, fallback, n_fallback, stream);
+                                        faces, fallback, n_fallback, refine, n_refine, stream);
 }
 
 }  // namespace
@@ -706,15 +747,17 @@ bool epa_warp_supported(const d3d_epa_options& o, bool fp64) {
 int epa_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                     const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                     const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
-                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64) {
+                    int32_t* fallback, unsigned long long* n_fallback, cudaStream_t stream, bool fp64,
+                    int32_t* refine, unsigned long long* n_refine) {
     // pairs per block as tuned, fewer if their polytopes do not fit in one block
     const int64_t bytes = fp64 ? layout_for<double>(o).bytes : layout_for<float>(o).bytes;
     int w = tuning().epa_warps;
     while (w > 2 && bytes * w > kSmemPerBlock) w /= 2;
 #define D3D_WARP_LAUNCH(T, W)                                                                                      \
     return launch_warp<T, W>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces, fallback, \
-                             n_fallback, stream)
+                             n_fallback, refine, n_refine, stream)
     if (fp64) {
+        refine = nullptr;  // the FP64 search refines with exact supports itself
         if (w == 2) D3D_WARP_LAUNCH(double, 2);
         if (w == 8) D3D_WARP_LAUNCH(double, 8);
         D3D_WARP_LAUNCH(double, 4);

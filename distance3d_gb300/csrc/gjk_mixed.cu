@@ -87,9 +87,12 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
     bool need = true;
     unsigned live = __activemask();  // the warp's lanes still in the loop
     WarpChunk chunk;
+    // per-lane claims for the last slots: the pairs are short, and slots left in a busy warp's chunk
+    // would hold up the end of the launch
+    const long long split = n - 2LL * gridDim.x * blockDim.x;
     while (true) {
         __syncwarp(live);
-        const long long slot = fetch_slot_chunked(lists.ctr + kCurA, need, chunk, live, kChunk);
+        const long long slot = fetch_slot_chunked(lists.ctr + kCurA, need, chunk, live, kChunk, split);
         const bool quit = need && slot >= n;
         live = __ballot_sync(live, !quit);
         if (quit) break;
@@ -126,9 +129,12 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
     bool need = true;
     unsigned live = __activemask();  // the warp's lanes still in the loop
     WarpChunk chunk;
+    // per-lane claims for the last slots: the pairs are short, and slots left in a busy warp's chunk
+    // would hold up the end of the launch
+    const long long split = n - 2LL * gridDim.x * blockDim.x;
     while (true) {
         __syncwarp(live);
-        const long long slot = fetch_slot_chunked(lists.ctr + kCurB, need, chunk, live, kChunk);
+        const long long slot = fetch_slot_chunked(lists.ctr + kCurB, need, chunk, live, kChunk, split);
         const bool quit = need && slot >= n;
         live = __ballot_sync(live, !quit);
         if (quit) break;

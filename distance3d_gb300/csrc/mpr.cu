@@ -47,9 +47,12 @@ __global__ void __launch_bounds__(kBlock) k_mpr(d3d_store st, const int32_t* __r
     bool need = true;
     unsigned live = __activemask();  // the warp's lanes still in the loop
     WarpChunk chunk;
+    // whole chunks to the end of the order: with long pairs, the lanes' coherence outweighs the slots
+    // left in busy warps' chunks at the end (per-lane claims for the last slots measured slower)
+    const long long split = n;
     while (true) {
         __syncwarp(live);
-        const long long slot = fetch_slot_chunked(cursor, need, chunk, live, kChunk);
+        const long long slot = fetch_slot_chunked(cursor, need, chunk, live, kChunk, split);
         const bool quit = need && slot >= n;
         live = __ballot_sync(live, !quit);
         if (quit) break;

@@ -39,11 +39,14 @@ struct WarpChunk {
 // `chunk` (>= 32) slots of *cursor.  A warp's lanes then hold pairs from at
 // most two chunks of the order at a time, instead of from anywhere in the
 // span all resident lanes of the GPU have fetched, which keeps the lanes of
-// a warp on pairs of the same collider types in a type-sorted order.
+// a warp on pairs of the same collider types in a type-sorted order.  Once
+// the cursor has passed `split` (the caller's n minus a few slots per
+// resident lane) a warp claims only the slots its lanes ask for, so that no
+// slot waits in the chunk of a busy warp at the end of the order.
 // Every lane of `live` must call it together (converged), so that the
 // lanes' copies of `w` stay equal.
 __device__ __forceinline__ long long fetch_slot_chunked(unsigned long long* cursor, bool need, WarpChunk& w,
-                                                        unsigned live, int chunk) {
+                                                        unsigned live, int chunk, long long split) {
     const unsigned want = __ballot_sync(live, need);
     if (!want) return -1;
     const int lane = threadIdx.x & 31;
@@ -57,11 +60,18 @@ __device__ __forceinline__ long long fetch_slot_chunked(unsigned long long* curs
     } else {
         const int leader = __ffs(live) - 1;
         unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(cursor, (unsigned long long)chunk);
+        int size = 0;
+        if (lane == leader) {
+            // the cursor's value is only a hint for the claim's size
+            const long long seen = (long long)*reinterpret_cast<volatile unsigned long long*>(cursor);
+            size = seen + chunk <= split ? chunk : cnt - (int)avail;
+            base = atomicAdd(cursor, (unsigned long long)size);
+        }
         base = __shfl_sync(live, base, leader);
+        size = __shfl_sync(live, size, leader);
         slot = rank < avail ? w.next + rank : (long long)base + (rank - avail);
         w.next = (long long)base + (cnt - avail);
-        w.end = (long long)base + chunk;
+        w.end = (long long)base + size;
     }
     return need ? slot : -1;
 }

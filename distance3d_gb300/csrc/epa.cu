@@ -799,11 +799,13 @@ extern "C" int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t*
 // pairs run in input order).
 //
 // The array is kNoAllocBytes = 16 MiB on every GPU that loads the library,
-// held until the process exits.  It bounds the per-pair polytope, not the
-// number of pairs: each of the array's slots is reused across pairs, and a
-// call fails with D3D_ERR_CAPACITY when a single slot of
-// (12 * max_faces + 6 * max_loose_edges) doubles leaves room for fewer than
-// 128 slots (with the defaults, 64 faces and 32 edges, there are 2,184).
+// held until the process exits.  Options the one-warp-per-pair kernel takes
+// (the defaults and the bench's 256 faces among them) keep each polytope in
+// shared memory and use the array only for the work counter.  Otherwise the
+// array holds the polytope slots: it bounds the per-pair polytope, not the
+// number of pairs (each slot is reused across pairs), and a call fails with
+// D3D_ERR_CAPACITY when a single slot of (12 * max_faces + 6 *
+// max_loose_edges) doubles leaves room for fewer than 128 slots.
 //
 // Every call shares the array, and the array keeps the previous call's
 // contents (the work counter is cleared on the stream at the start of each
@@ -854,9 +856,10 @@ extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const 
     D3D_REQUIRE(valid(options) && options->precision == D3D_PRECISION_FP64,
                 "d3d_epa_noalloc: invalid options (need the FP64 form, max_faces >= 4, limits >= 0, epsilon >= 0)");
     D3D_REQUIRE(n >= 0, "d3d_epa_noalloc: n < 0");
+    const bool warp = exact_warp_supported(*options);  // the polytopes in shared memory
     const int64_t slot_bytes = slot_doubles(*options) * (int64_t)sizeof(double);
     const int64_t slots = (int64_t)(kNoAllocBytes - 256) / slot_bytes;
-    if (slots < kBlock) {
+    if (!warp && slots < kBlock) {
         d3d::set_error("d3d_epa_noalloc: max_faces=%d, max_loose_edges=%d need %lld bytes per pair; the static "
                        "scratch of %zu bytes holds fewer than %d pairs at a time (use d3d_epa)",
                        options->max_faces, options->max_loose_edges, (long long)slot_bytes, kNoAllocBytes, kBlock);
@@ -875,7 +878,7 @@ extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const 
         d3d::set_error("d3d_epa_noalloc: %s", cudaGetErrorString(e));
         return D3D_ERR_CUDA;
     }
-    if (exact_warp_supported(*options))  // the polytopes in shared memory: the static array holds the counter
+    if (warp)  // the static array holds the counter only
         return exact_warp_launch(*store, i1, i2, nullptr, n, nullptr, cursor, simplex, *options, mtv, status,
                                  n_faces, faces, st);
     int blocks = d3d::persistent_blocks((const void*)k_epa, kBlock, n);

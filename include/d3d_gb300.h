@@ -181,15 +181,19 @@ int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_
 /* EPA that allocates nothing, for callers that may not allocate device memory
  * while they run (a control loop on a fixed memory budget, a plugin whose host
  * application owns every GPU allocation).  It has no counterpart in the
- * reference.  Same arguments and results as d3d_epa, without the scratch: the
- * polytopes live in a 16 MiB array inside the library, present on every GPU
- * that loads it until the process exits.  Fails with D3D_ERR_CAPACITY when
- * max_faces / max_loose_edges leave room for fewer than 128 pairs at a time
- * (12 * max_faces + 6 * max_loose_edges doubles per pair; the defaults fit
- * 2,184).  The first call on a device (with that device current) looks up the
- * array's address; make that first call before any stream capture.  All calls
- * share the array: calls whose work overlaps on the GPU race and must be
- * serialised by the caller.  Pairs run in input order (no scheduling sort). */
+ * reference.  Same arguments and results as d3d_epa, without the scratch.
+ * Options of up to 251 iterations whose polytope fits a block's shared memory
+ * (the defaults, and 256 faces with 128 loose edges) keep each polytope in
+ * shared memory; for other options the polytopes live in a 16 MiB array
+ * inside the library, present on every GPU that loads it until the process
+ * exits, and the call fails with D3D_ERR_CAPACITY when max_faces /
+ * max_loose_edges leave room for fewer than 128 pairs at a time there
+ * (12 * max_faces + 6 * max_loose_edges doubles per pair).  The array also
+ * holds the work counter.  The first call on a device (with that device
+ * current) looks up the array's address; make that first call before any
+ * stream capture.  All calls share the array: calls whose work overlaps on
+ * the GPU race and must be serialised by the caller.  Pairs run in input
+ * order (no scheduling sort). */
 int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
                     const double* simplex, const d3d_epa_options* options, double* mtv, int8_t* status,
                     int32_t* n_faces, double* faces, void* stream);

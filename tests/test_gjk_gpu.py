@@ -200,3 +200,26 @@ def test_drop_in_api_matches_batch():
     assert gjk.gjk_intersection(c1, c2) == (d == 0.0)
     far = colliders.ConvexHullVertices(np.array([[1e8, 0.0, 0.0]]))
     assert gjk.gjk(c1, far) == (np.finfo(float).max, None, None, None)
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 4097, 150001])
+def test_every_pair_processed_at_any_count(n):
+    """The persistent kernels hand out the type-sorted pairs in warp chunks
+    of 32 and, near the end of the order, one lane at a time: at counts
+    around those boundaries every pair is processed once.  The FP64 GJK and
+    MPR equal the oracle for every pair, the mixed GJK stays near the FP64
+    distances (its outputs start out uninitialised)."""
+    from distance3d_gb300.mpr import mpr_batch
+    cs, i1, i2 = workloads.pairs_mixed_six(n, seed=41, center_half_width=workloads.INTERSECT30_HALF_WIDTH)
+    st = ColliderStore(cs)
+    ref = oracle.gjk_distance(cs, i1, i2)
+    g = host(gjk_distance_batch(st, i1, i2))
+    assert np.array_equal(g["dist"], ref["dist"])
+    assert np.array_equal(g["n_simplex"], ref["n_simplex"])
+    m = host(gjk_distance_batch(st, i1, i2, precision="mixed"))
+    assert np.all(np.isfinite(m["dist"]))
+    assert np.all(np.abs(m["dist"] - ref["dist"]) <= 1e-2 * np.maximum(1.0, ref["dist"]))
+    r = host(mpr_batch(st, i1, i2))
+    mref = oracle.mpr(cs, i1, i2)
+    assert np.array_equal(r["hit"], mref["hit"])
+    assert np.array_equal(r["depth"], mref["depth"], equal_nan=True)

@@ -1,4 +1,7 @@
-// epa.cu -- batched FP64 EPA (expanding polytope), one thread per pair.
+// epa.cu -- batched FP64 EPA (expanding polytope): one warp per pair
+// (k_epa_exact_warp, the polytope in shared memory) for every option set of up
+// to 251 iterations whose polytope fits a block's shared memory, one thread
+// per pair (k_epa, the polytope in caller scratch) for the others.
 //
 // Restates distance3d epa.py (Kevin Moran's formulation): the polytope is an
 // unordered array of faces (3 vertices + unit normal), the face closest to the
@@ -12,11 +15,11 @@
 // Where the reference raises (face buffer full, epa.py:128; np.argmin on an
 // empty polytope) the pair gets a status code instead.
 //
-// Scheduling: pairs are sorted by collider types, and a persistent grid runs
-// one EPA iteration per round per lane; a lane whose pair ends fetches the
-// next one.  Each thread owns one scratch slot of max_faces faces and
-// max_loose_edges edges (d3d_epa_scratch_bytes), reused across its pairs, so
-// the scratch is bounded by the slot count, not by n.
+// Thread form scheduling: pairs are sorted by collider types, and a
+// persistent grid runs one EPA iteration per round per lane; a lane whose pair
+// ends fetches the next one.  Each thread owns one scratch slot of max_faces
+// faces and max_loose_edges edges (d3d_epa_scratch_bytes), reused across its
+// pairs, so the scratch is bounded by the slot count, not by n.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -261,14 +264,15 @@ __global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __re
 // ---------------------------------------------------------------------------
 // The same EPA with one warp per pair.  The polytope (faces of 12 doubles)
 // and the loose edges live in the warp's shared memory; the steps whose
-// order does not matter run across the lanes -- the closest-face scan, the
-// visibility of every face, the normals of the new faces -- and the
-// order-dependent bookkeeping keeps the reference's order exactly: faces are
-// removed by moving the last face into the first visible slot and testing
-// that slot again, each removed face's edges are matched against the loose
-// list in list order (the first match is overwritten by the last edge), and
-// new faces are appended in loose-edge order.  Results are those of k_epa
-// (and of the reference) bit for bit.
+// order does not matter run across the lanes -- the closest-face scan (on
+// integer keys of the face distances), the visibility of every face, the
+// normals of the new faces, the closeness of a new vertex to the others --
+// and the order-dependent bookkeeping keeps the reference's order exactly:
+// faces are removed by moving the last face into the first visible slot and
+// testing that slot again, each removed face's edges are matched against the
+// loose list in list order (the first match is overwritten by the last
+// edge), and new faces are appended in loose-edge order.  Results are those
+// of k_epa (and of the reference) bit for bit.
 
 constexpr unsigned kWarpAll = 0xffffffffu;
 

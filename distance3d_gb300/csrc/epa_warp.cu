@@ -27,7 +27,9 @@
 // in epa_mixed.cu.  A pair whose polytope fails validation (degenerate face,
 // horizon not one loop, more horizon edges than max_loose_edges) goes to the
 // fallback list.  The converged face is refined along its FP32 normal with
-// FP64 supports (refine_face).
+// FP64 supports: in a second pass, one pair per thread (k_epa_refine), or in
+// the search kernel itself (refine_face) when the caller gives no list for
+// that pass.
 //
 // The same search is instantiated with an FP64 polytope and exact FP64
 // supports.  It takes the FP32 search's fallback pairs: the plane tests

@@ -1,6 +1,6 @@
 // gjk_mixed.cu -- mixed-precision GJK distance.
 //
-// Three kernels over the type-sorted pair order:
+// Four kernels over the type-sorted pair order:
 //
 // A  runs the Jolt loop in FP32 on the FP32 mirror of the store, with
 //    thresholds scaled to single precision, hands each pair's outcome, final
@@ -15,15 +15,18 @@
 //    argmax and return the FP64 vertex); if that simplex encloses or touches
 //    the origin the pair is done, otherwise the reference's loop continues
 //    from it until the duality gap brackets the distance within 1e-6 of
-//    itself or 1e-9 of the scene's scale.
+//    itself or 1e-9 of the scene's scale.  A pair whose loop ends leaves its
+//    simplex in the outputs and the rest of its state in an end record.
+// E  (the end pass) computes the closest points and the checks of B's
+//    finished pairs (pb_end), every lane on a finished pair.
 // C  is the plain FP64 kernel over the fallback list (the reference's
 //    arithmetic; CLIPPED and MAX_ITER keep their FP64 meaning).
 //
 // B keeps the simplex P/Q rows in shared memory and has one support call
 // site, so that a warp's lanes share the support and simplex code whatever
-// mode and simplex size each holds.  A pair leaves B for the fallback list
-// only if its result fails the consistency check (closest points vs |v|),
-// the sanity check or the iteration bound.
+// mode and simplex size each holds.  A pair goes to the fallback list only if
+// its result fails the consistency check (closest points vs |v|) or the
+// sanity check in E, or hits the iteration bound in B.
 //
 // On the six-type workloads A takes ~11 FP32 iterations and B replays ~3
 // rows and runs ~2 FP64 iterations, against ~17-19 FP64 iterations for the

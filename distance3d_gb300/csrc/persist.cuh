@@ -3,7 +3,10 @@
 // Every lane owns one pair at a time and fetches the next as soon as its pair
 // finishes, so a warp stays full while work remains instead of waiting for
 // its slowest pair.  Fetches are warp-aggregated: one atomic per warp per
-// round, slots handed out in lane order.
+// round, slots handed out in lane order (fetch_slot), or one atomic per warp
+// per chunk of slots that the warp then hands to its lanes
+// (fetch_slot_chunked), which keeps a warp's lanes on neighbouring pairs of a
+// sorted order.
 #pragma once
 
 #include <cstdint>

@@ -219,12 +219,21 @@ def gjk_fixture(mods, cs, i1, i2):
                 iterations=iters, intersect=hit, aabbs=aabbs), cols
 
 
+# EPA limit settings of the fixtures: the reference's defaults, the bench's
+# polytope, and limits under which the face buffer (tight), the iteration
+# bound (short) and the loose-edge list (edges) run out on some pairs
+EPA_SETTINGS = (("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
+                ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
+                ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
+                ("edges", dict(max_faces=256, max_loose_edges=4)))
+
+
 def epa_fixture(mods, cols, gf):
     _, epa, _, _, _ = mods
     sel = np.flatnonzero((gf["dist"] == 0.0) & ~np.isnan(gf["simplex"]).any(axis=(1, 2)))
     n = len(sel)
     out = {"pair": sel.astype(np.int32)}
-    for tag, kw in (("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))):
+    for tag, kw in EPA_SETTINGS:
         mtv = np.full((n, 3), np.nan)
         status = np.zeros(n, np.int8)   # 0 converged, 4 max_iter, 5 face overflow, 6 other error
         nfaces = np.zeros(n, np.int32)

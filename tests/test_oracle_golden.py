@@ -44,9 +44,18 @@ def test_supports_bit_exact(golden, name):
     assert np.unique(cs.base_types).size >= 9 and cs.wrapped.any()
 
 
+# the EPA limit settings of the fixtures (tests/golden/make_golden.py): the
+# reference's defaults, the bench's polytope, and limits under which the face
+# buffer (tight), the iteration bound (short) and the loose-edge list (edges)
+# run out on some pairs
+EPA_SETTINGS = [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
+                ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
+                ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
+                ("edges", dict(max_faces=256, max_loose_edges=4))]
+
+
 @pytest.mark.parametrize("fixture", ["mixed6", "all9", "mesh10"])
-@pytest.mark.parametrize("tag,kw", [("default", {}),
-                                    ("large", dict(max_faces=256, max_loose_edges=128))])
+@pytest.mark.parametrize("tag,kw", EPA_SETTINGS)
 def test_epa_bit_exact(golden, fixture, tag, kw):
     g, cs = golden("gjk_" + fixture)
     e, _ = golden("epa_" + fixture)
@@ -54,8 +63,14 @@ def test_epa_bit_exact(golden, fixture, tag, kw):
     r = oracle.epa(cs, g["i1"][p], g["i2"][p], g["simplex"][p], **kw)
     st = e[f"status_{tag}"]
     assert np.array_equal(r["status"], st)
-    ok = st == 0
-    assert ok.sum() > 100
+    # converged, and stopped at the iteration bound (epa.py:76-78 returns the
+    # closest face's MTV unconverged)
+    ok = (st == 0) | (st == 4)
+    assert ok.sum() >= 20
+    if tag == "tight":
+        assert (st == 5).sum() > 100  # face buffer full (epa.py:128)
+    if tag == "short":
+        assert (st == 4).sum() > 100  # iteration bound
     assert np.array_equal(r["mtv"][ok], e[f"mtv_{tag}"][ok])
     assert np.array_equal(r["n_faces"][ok], e[f"n_faces_{tag}"][ok])
 

@@ -596,6 +596,14 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 nf_out = nf;
                 return D3D_STATUS_EPA_FACE_OVERFLOW;
             }
+            // epa.py:131-135 writes each new face into slot n_faces before testing it, so a degenerate
+            // face stays in the slot past the live faces until the next face takes that slot: after the
+            // loop the slot holds the last loose edge's face if that one was not kept.  An unconverged
+            // pair's MTV can read it (closest_face is a view into the faces, epa.py:77).
+            if (k == ne - 1 && !keep) {
+                double* dst = F + 12 * (nf + kept + before);
+                for (int q = 0; q < 12; ++q) dst[q] = nfa[q];
+            }
             kept += __popc(km);
         }
         nf += kept;

@@ -47,7 +47,10 @@ def test_fp64_gjk_matches_reference_golden(golden, fx):
 
 
 @pytest.mark.parametrize("fx", FIXTURES)
-@pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))])
+@pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
+                                    ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
+                                    ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
+                                    ("edges", dict(max_faces=256, max_loose_edges=4))])
 def test_fp64_epa_matches_reference_golden(golden, fx, tag, kw):
     g, cs = golden("gjk_" + fx)
     e, _ = golden("epa_" + fx)
@@ -55,7 +58,7 @@ def test_fp64_epa_matches_reference_golden(golden, fx, tag, kw):
     r = host(epa_batch(ColliderStore(cs), g["i1"][p], g["i2"][p], g["simplex"][p], **kw))
     st = e[f"status_{tag}"]
     assert np.array_equal(r["status"], st)
-    ok = st == 0
+    ok = (st == 0) | (st == 4)  # converged, or the closest face's MTV at the iteration bound
     assert np.array_equal(r["mtv"][ok], e[f"mtv_{tag}"][ok])
     assert np.array_equal(r["n_faces"][ok], e[f"n_faces_{tag}"][ok])
 

@@ -17,7 +17,10 @@ def host(r):
     return {k: v.cpu().numpy() for k, v in r.items()}
 
 
-@pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128))])
+@pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
+                                    ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
+                                    ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
+                                    ("edges", dict(max_faces=256, max_loose_edges=4))])
 def test_epa_matches_reference_golden(golden, tag, kw):
     g, cs = golden("gjk_mixed6")
     e, _ = golden("epa_mixed6")
@@ -25,7 +28,7 @@ def test_epa_matches_reference_golden(golden, tag, kw):
     r = host(epa_batch(ColliderStore(cs), g["i1"][p], g["i2"][p], g["simplex"][p], **kw))
     st = e[f"status_{tag}"]
     assert np.array_equal(r["status"], st)
-    ok = st == 0
+    ok = (st == 0) | (st == 4)  # converged, or the closest face's MTV at the iteration bound
     assert np.array_equal(r["mtv"][ok], e[f"mtv_{tag}"][ok])
     assert np.array_equal(r["n_faces"][ok], e[f"n_faces_{tag}"][ok])
 

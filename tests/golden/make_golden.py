@@ -274,7 +274,24 @@ def mpr_fixture(cols, gf):
             depth[k], pdir[k], pos[k] = d, p, c
         hit_i[k] = mpr.mpr_intersection(c1, c2)
     print(f"  mpr: {n} pairs in {time.time() - t0:.1f}s, {hit.sum()} intersecting")
-    return dict(i1=gf["i1"], i2=gf["i2"], hit=hit, depth=depth, dir=pdir, pos=pos, hit_intersection=hit_i)
+    out = dict(i1=gf["i1"], i2=gf["i2"], hit=hit, depth=depth, dir=pdir, pos=pos, hit_intersection=hit_i)
+    # other options: a coarse tolerance, and an iteration bound that the
+    # portal discovery and refinement run into
+    for tag, kw in MPR_SETTINGS:
+        h2 = np.zeros(n, bool)
+        d2 = np.full(n, np.nan)
+        for k in range(n):
+            h, d, _, _ = mpr.mpr_penetration(cols[gf["i1"][k]], cols[gf["i2"][k]], **kw)
+            h2[k] = h
+            if d is not None:
+                d2[k] = d
+        out[f"hit_{tag}"] = h2
+        out[f"depth_{tag}"] = d2
+        print(f"  mpr[{tag}]: {h2.sum()} intersecting")
+    return out
+
+
+MPR_SETTINGS = (("coarse", dict(mpr_tolerance=1e-2)), ("short", dict(max_iterations=3)))
 
 
 class _FakeTM:

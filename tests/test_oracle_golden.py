@@ -109,6 +109,18 @@ def test_mpr_bit_exact(golden, fixture):
     assert np.array_equal(ri["hit"], m["hit_intersection"])
 
 
+@pytest.mark.parametrize("fixture", ["all9", "mesh10"])
+@pytest.mark.parametrize("tag,kw", [("coarse", dict(tolerance=1e-2)), ("short", dict(max_iterations=3))])
+def test_mpr_options_bit_exact(golden, fixture, tag, kw):
+    """mpr_penetration with a coarse tolerance and with an iteration bound the
+    search runs into (tests/golden/make_golden.py MPR_SETTINGS)."""
+    g, cs = golden("gjk_" + fixture)
+    m, _ = golden("mpr_" + fixture)
+    r = oracle.mpr(cs, m["i1"], m["i2"], **kw)
+    assert np.array_equal(r["hit"], m[f"hit_{tag}"])
+    assert np.array_equal(r["depth"], m[f"depth_{tag}"], equal_nan=True)
+
+
 def test_edge_colliders_bit_exact(golden):
     """Degenerate and boundary colliders (zero sizes, tied and zero disk
     normals, flat and point hulls, tied mesh vertices, margins of 0):

@@ -184,6 +184,9 @@ def ref_distance(gjk_mod, c1, c2, tolerance=1e-10, max_distance_squared=100000.0
         return float(dist), a, b, Y, n_points, it
 
 
+GJK_SETTINGS = (("clip", dict(max_distance_squared=0.01)), ("coarse", dict(tolerance=1e-3)))
+
+
 def gjk_fixture(mods, cs, i1, i2):
     gjk, epa, colliders, _, _ = mods
     cols = make_ref_colliders(colliders, cs)
@@ -213,8 +216,30 @@ def gjk_fixture(mods, cs, i1, i2):
     dt = time.time() - t0
     aabbs = np.stack([c.aabb() for c in cols])
     print(f"  gjk: {n} pairs in {dt:.1f}s ({n / dt:.0f} pairs/s incl. intersection)")
+    # other options: a clipping distance some pairs exceed (_gjk_jolt.py:209-210
+    # returns MAX_FLOAT and no points), and a coarse tolerance
+    extra = {}
+    for tag, kw in GJK_SETTINGS:
+        dk = np.full(n, np.nan)
+        ck = np.full((n, 3), np.nan)
+        sk = np.zeros(n, np.int8)  # 0 ok, 1 clipped, 2 the sanity assertion (_gjk_jolt.py:216)
+        for k in range(n):
+            try:
+                d, a, _, _ = gjk.gjk_distance_jolt(cols[i1[k]], cols[i2[k]], **kw)
+            except AssertionError:
+                sk[k] = 2
+                continue
+            dk[k] = d
+            if a is None:
+                sk[k] = 1
+            else:
+                ck[k] = a
+        extra[f"dist_{tag}"] = dk
+        extra[f"cp1_{tag}"] = ck
+        extra[f"status_{tag}"] = sk
+        print(f"  gjk[{tag}]: status counts {np.bincount(sk, minlength=3)}")
     return dict(types=cs.types, poses=cs.poses, params=cs.params, hull_offset=cs.hull_offset,
-                hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), links=cs.links, i1=i1, i2=i2,
+                hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(), links=cs.links, i1=i1, i2=i2, **extra,
                 dist=dist, cp1=cp1, cp2=cp2, simplex=simplex, n_simplex=n_simplex,
                 iterations=iters, intersect=hit, aabbs=aabbs), cols
 

@@ -219,3 +219,18 @@ def test_edge_colliders_match_reference(golden):
     # the mixed forms on the same pairs: GJK within tolerance, MPR flags
     mg = host(gjk_distance_batch(st, g["i1"], g["i2"], precision="mixed"))
     mixed_check(mg, g, cs, g["i1"], g["i2"])
+
+
+@pytest.mark.parametrize("fx", ["mixed6", "all9", "mesh10"])
+@pytest.mark.parametrize("tag,kw", [("clip", dict(max_distance_squared=0.01)), ("coarse", dict(tolerance=1e-3))])
+def test_fp64_gjk_options_match_reference_golden(golden, fx, tag, kw):
+    """The FP64 GJK with a clipping distance many pairs exceed and with a
+    coarse tolerance under which the reference's sanity assertion fails on
+    some pairs: statuses, distances and points of the reference."""
+    g, cs = golden("gjk_" + fx)
+    r = host(gjk_distance_batch(ColliderStore(cs), g["i1"], g["i2"], **kw))
+    st = g[f"status_{tag}"]
+    assert np.array_equal(r["status"], st)
+    ok = st != 2
+    assert np.array_equal(r["dist"][ok], g[f"dist_{tag}"][ok])
+    assert np.array_equal(r["cp1"][ok], g[f"cp1_{tag}"][ok], equal_nan=True)

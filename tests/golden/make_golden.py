@@ -245,12 +245,14 @@ def gjk_fixture(mods, cs, i1, i2):
 
 
 # EPA limit settings of the fixtures: the reference's defaults, the bench's
-# polytope, and limits under which the face buffer (tight), the iteration
-# bound (short) and the loose-edge list (edges) run out on some pairs
+# polytope, limits under which the face buffer (tight), the iteration bound
+# (short) and the loose-edge list (edges) run out on some pairs, and a coarser
+# epsilon (convergence, visibility and edge matching)
 EPA_SETTINGS = (("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
                 ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
                 ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
-                ("edges", dict(max_faces=256, max_loose_edges=4)))
+                ("edges", dict(max_faces=256, max_loose_edges=4)),
+                ("eps", dict(max_faces=256, max_loose_edges=128, epsilon=1e-4)))
 
 
 def epa_fixture(mods, cols, gf):

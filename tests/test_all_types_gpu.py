@@ -50,7 +50,8 @@ def test_fp64_gjk_matches_reference_golden(golden, fx):
 @pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
                                     ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
                                     ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
-                                    ("edges", dict(max_faces=256, max_loose_edges=4))])
+                                    ("edges", dict(max_faces=256, max_loose_edges=4)),
+                                    ("eps", dict(max_faces=256, max_loose_edges=128, epsilon=1e-4))])
 def test_fp64_epa_matches_reference_golden(golden, fx, tag, kw):
     g, cs = golden("gjk_" + fx)
     e, _ = golden("epa_" + fx)

@@ -20,7 +20,8 @@ def host(r):
 @pytest.mark.parametrize("tag,kw", [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
                                     ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
                                     ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
-                                    ("edges", dict(max_faces=256, max_loose_edges=4))])
+                                    ("edges", dict(max_faces=256, max_loose_edges=4)),
+                                    ("eps", dict(max_faces=256, max_loose_edges=128, epsilon=1e-4))])
 def test_epa_matches_reference_golden(golden, tag, kw):
     g, cs = golden("gjk_mixed6")
     e, _ = golden("epa_mixed6")

@@ -51,7 +51,8 @@ def test_supports_bit_exact(golden, name):
 EPA_SETTINGS = [("default", {}), ("large", dict(max_faces=256, max_loose_edges=128)),
                 ("tight", dict(max_iter=20, max_faces=24, max_loose_edges=6)),
                 ("short", dict(max_iter=6, max_faces=256, max_loose_edges=128)),
-                ("edges", dict(max_faces=256, max_loose_edges=4))]
+                ("edges", dict(max_faces=256, max_loose_edges=4)),
+                ("eps", dict(max_faces=256, max_loose_edges=128, epsilon=1e-4))]
 
 
 @pytest.mark.parametrize("fixture", ["mixed6", "all9", "mesh10"])

@@ -13,7 +13,8 @@ as hand-written sm_103a CUDA kernels behind the C ABI of libd3d_gb300.so
 * ``distance3d_gb300.collider_set`` -- the packed host format
 """
 from ._lib import (STATUS_OK, STATUS_CLIPPED, STATUS_SANITY, STATUS_MAX_ITER,  # noqa: F401
-                   STATUS_EPA_NOT_CONVERGED, STATUS_EPA_FACE_OVERFLOW, STATUS_EPA_DEGENERATE, D3DError)
+                   STATUS_EPA_NOT_CONVERGED, STATUS_EPA_FACE_OVERFLOW, STATUS_EPA_DEGENERATE,
+                   STATUS_BAD_INDEX, D3DError)
 from .collider_set import (ColliderSet, SPHERE, CAPSULE, BOX, CYLINDER, ELLIPSOID, HULL,  # noqa: F401
                            DISK, ELLIPSE, CONE, MARGIN)
 

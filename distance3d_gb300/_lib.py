@@ -17,6 +17,7 @@ c_int = ctypes.c_int
 D3D_SUCCESS, D3D_ERR_INVALID, D3D_ERR_CAPACITY, D3D_ERR_CUDA = 0, 1, 2, 3
 STATUS_OK, STATUS_CLIPPED, STATUS_SANITY, STATUS_MAX_ITER = 0, 1, 2, 3
 STATUS_EPA_NOT_CONVERGED, STATUS_EPA_FACE_OVERFLOW, STATUS_EPA_DEGENERATE = 4, 5, 6
+STATUS_BAD_INDEX = 7
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 

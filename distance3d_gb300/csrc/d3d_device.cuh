@@ -84,6 +84,23 @@ struct Col {
     T R[9], t[3], p[3], m;
 };
 
+// True iff both collider indices of a pair lie in [0, n_colliders).  Every
+// kernel that takes caller indices tests them before reading a record; a pair
+// that fails gets D3D_STATUS_BAD_INDEX and touches no store memory.
+__device__ __forceinline__ bool index_ok(const d3d_store& s, int i) {
+    return (unsigned long long)(unsigned)i < (unsigned long long)s.n_colliders;
+}
+__device__ __forceinline__ bool pair_ok(const d3d_store& s, int a, int b) { return index_ok(s, a) && index_ok(s, b); }
+
+// The EPA slots of such a pair.
+__device__ __forceinline__ void epa_store_bad_index(double* mtv, int8_t* status, int32_t* n_faces, int64_t k) {
+    mtv[3 * k] = NAN;
+    mtv[3 * k + 1] = NAN;
+    mtv[3 * k + 2] = NAN;
+    status[k] = (int8_t)D3D_STATUS_BAD_INDEX;
+    n_faces[k] = 0;
+}
+
 __device__ __forceinline__ void load_meta(const d3d_store& s, int idx, int& type, int& nv, int& off) {
     int4 m = __ldg(reinterpret_cast<const int4*>(s.meta) + idx);
     type = m.x;

@@ -237,6 +237,10 @@ __global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __re
             pid = order ? order[k] : k;
             a = i1[pid];
             b = i2[pid];
+            if (!pair_ok(s, a, b)) {
+                epa_store_bad_index(mtv, status, n_faces, pid);
+                continue;  // the thread fetches again
+            }
             epa_begin(L, simplex + 12 * pid, F);
             need = false;
         }
@@ -630,9 +634,15 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
         slot = __shfl_sync(kWarpAll, slot, 0);
         if (slot >= n) break;
         const int64_t pid = list ? list[slot] : slot;
+        const int a = i1[pid], b = i2[pid];
+        if (!pair_ok(s, a, b)) {  // the same for every lane
+            if (ln == 0) epa_store_bad_index(mtv, status, n_faces, pid);
+            __syncwarp();
+            continue;
+        }
         d3 m;
         int nf = 0;
-        const int stt = epa_pair_warp(s, i1[pid], i2[pid], simplex + 12 * pid, o, lb, P, m, nf);
+        const int stt = epa_pair_warp(s, a, b, simplex + 12 * pid, o, lb, P, m, nf);
         if (ln == 0) {
             mtv[3 * pid] = m.x;
             mtv[3 * pid + 1] = m.y;
@@ -882,6 +892,20 @@ extern "C" int d3d_epa_noalloc(const d3d_store* store, const int32_t* i1, const 
     void* base = nullptr;
     rc = noalloc_base(&base);
     if (rc) return rc;
+    {
+        // the array's address is the current device's: the store must live there
+        int cur = 0;
+        cudaPointerAttributes pa = {};
+        if (cudaGetDevice(&cur) == cudaSuccess) {
+            if (cudaPointerGetAttributes(&pa, store->rec64) != cudaSuccess) {
+                cudaGetLastError();  // not a pointer the runtime knows: nothing to compare, no error left behind
+            } else if (pa.type == cudaMemoryTypeDevice && pa.device != cur) {
+                d3d::set_error("d3d_epa_noalloc: the store is on device %d but device %d is current", pa.device,
+                               cur);
+                return D3D_ERR_INVALID;
+            }
+        }
+    }
     cudaStream_t st = d3d::as_stream(stream);
     unsigned long long* cursor = static_cast<unsigned long long*>(base);
     double* slot_mem = reinterpret_cast<double*>(static_cast<char*>(base) + 256);

@@ -69,6 +69,10 @@ __global__ void __launch_bounds__(kBlock) k_epa_mixed(d3d_store st, const int32_
             pid = order ? order[k] : k;
             a = i1[pid];
             b = i2[pid];
+            if (!pair_ok(st, a, b)) {
+                epa_store_bad_index(mtv, status, n_faces, pid);
+                continue;  // the thread fetches again
+            }
             mepa_begin(L, s, simplex + 12 * pid);
             need = false;
         }

@@ -609,6 +609,11 @@ __global__ void __launch_bounds__(32 * WARPS, kWarpsPerSm<T> / WARPS) k_epa_warp
         if (slot >= n) break;
         const int64_t k = list ? list[slot] : slot;
         const int a = i1[k], b = i2[k];
+        if (!pair_ok(st, a, b)) {  // the same for every lane
+            if (ln == 0) epa_store_bad_index(mtv, status, n_faces, k);
+            __syncwarp();
+            continue;
+        }
         const double* sx = simplex + 12 * k;
         const Search R = search_pair<T, MESH>(P, st, a, b, sx, o);
         if (R.status == kEpaFallback) {

@@ -52,6 +52,10 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_distance_f64(d3d_store s, const i
             pid = order ? order[slot] : slot;
             a = i1[pid];
             b = i2[pid];
+            if (!pair_ok(s, a, b)) {
+                store_bad_index(o, pid);
+                continue;  // the lane fetches again
+            }
             simplex_clear(g.S);
             const d3 dir = mk(1.0, 0.0, 0.0);
             gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
@@ -73,8 +77,14 @@ __global__ void __launch_bounds__(128) k_gjk_intersection_f64(d3d_store s, const
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     JoltEps<double> E = reference_eps<double>();
+    const int a = i1[k], b = i2[k];
+    if (!pair_ok(s, a, b)) {
+        hit[k] = 0;
+        status[k] = (int8_t)D3D_STATUS_BAD_INDEX;
+        return;
+    }
     int st;
-    hit[k] = (int8_t)gjk_intersection_loop(s, i1[k], i2[k], tol_sq, max_iter, E, st);
+    hit[k] = (int8_t)gjk_intersection_loop(s, a, b, tol_sq, max_iter, E, st);
     status[k] = (int8_t)st;
 }
 

@@ -82,12 +82,12 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
                                                         const int32_t* __restrict__ order, int64_t n,
                                                         const int64_t* __restrict__ n_dev, float tol_sq,
                                                         float max_d2, int max_iter, Handoff* __restrict__ hand,
-                                                        Lists lists) {
+                                                        DistanceOut out, Lists lists) {
     if (n_dev) n = *n_dev;
     PhaseALoop L;
     int64_t pid = 0;
     int a = 0, b = 0;
-    bool need = true;
+    bool need = true, bad = false;
     unsigned live = __activemask();  // the warp's lanes still in the loop
     WarpChunk chunk;
     // per-lane claims for the last slots: the pairs are short, and slots left in a busy warp's chunk
@@ -103,13 +103,20 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
             pid = order ? order[slot] : slot;
             a = i1[pid];
             b = i2[pid];
+            bad = !pair_ok(s, a, b);
             pa_begin(L);
             need = false;
         }
-        const int o = pa_step<MESH>(L, s, a, b, tol_sq, max_d2, max_iter);
+        // a pair with an out-of-range index ends at once; B skips it (its outcome is neither
+        // separated nor touching) and it joins no list
+        const int o = bad ? PA_BAD_INDEX : pa_step<MESH>(L, s, a, b, tol_sq, max_d2, max_iter);
         const bool done = o >= 0;
-        if (done) hand[pid] = pa_handoff(L, o);
-        append_lanes(live, lists.fallback, lists.ctr + kNumFallback, done && o >= PA_CLIPPED, (int32_t)pid);
+        if (done) {
+            hand[pid] = pa_handoff(L, o);
+            if (bad) store_bad_index(out, pid);
+        }
+        append_lanes(live, lists.fallback, lists.ctr + kNumFallback, done && (o == PA_CLIPPED || o == PA_FAILED),
+                     (int32_t)pid);
         need = done;
     }
 }
@@ -257,7 +264,8 @@ int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, c
     const float tol_sq = (float)(opt.tolerance * opt.tolerance);
     const void* ka = (const void*)k_gjk_mixed_a<BLOCK, MESH>;
     k_gjk_mixed_a<BLOCK, MESH><<<persistent_blocks(ka, BLOCK, n, per_sm), BLOCK, 0, stream>>>(
-        store, i1, i2, order, n, n_dev, tol_sq, (float)opt.max_distance_squared, opt.max_iterations, hand, lists);
+        store, i1, i2, order, n, n_dev, tol_sq, (float)opt.max_distance_squared, opt.max_iterations, hand, o,
+        lists);
     int rc = check_launch("d3d_gjk_distance (mixed, FP32 phase)");
     if (rc) return rc;
     const void* kb = (const void*)k_gjk_mixed_b<BLOCK, MESH>;

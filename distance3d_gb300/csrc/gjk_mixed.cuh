@@ -186,7 +186,7 @@ __device__ __forceinline__ JoltEps<float> fp32_eps() {
     return JoltEps<float>{4.f * e, e * e, e, 16.f * e * e, 0.f};
 }
 
-enum PhaseAOutcome { PA_SEPARATED = 0, PA_TOUCHING = 1, PA_CLIPPED = 2, PA_FAILED = 3 };
+enum PhaseAOutcome { PA_SEPARATED = 0, PA_TOUCHING = 1, PA_CLIPPED = 2, PA_FAILED = 3, PA_BAD_INDEX = 4 };
 
 // What phase A hands to phase B for one pair (80 bytes): the final closest
 // point (xyz) with the outcome, simplex size and iteration count packed in w,

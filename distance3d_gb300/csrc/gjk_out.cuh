@@ -15,6 +15,21 @@ struct DistanceOut {
     int32_t* iterations;
 };
 
+// The slots of a pair whose collider indices are out of range.
+__device__ __forceinline__ void store_bad_index(const DistanceOut& o, int64_t k) {
+    o.dist[k] = NAN;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        o.cp1[3 * k + j] = NAN;
+        o.cp2[3 * k + j] = NAN;
+    }
+#pragma unroll
+    for (int j = 0; j < 12; ++j) o.simplex[12 * k + j] = 0.0;
+    o.n_simplex[k] = 0;
+    o.status[k] = (int8_t)D3D_STATUS_BAD_INDEX;
+    if (o.iterations) o.iterations[k] = 0;
+}
+
 template <typename Rows>
 __device__ __forceinline__ void store_result(const DistanceOut& o, int64_t k, const GjkResult<double>& r,
                                              const Simplex<double, Rows>& S) {

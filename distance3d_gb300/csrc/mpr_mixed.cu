@@ -65,6 +65,11 @@ __global__ void __launch_bounds__(kBlock) k_mpr_mixed_a(d3d_store st, const int3
             pid = order ? order[slot] : slot;
             i = i1[pid];
             j = i2[pid];
+            if (!pair_ok(st, i, j)) {
+                const d3 nan3 = mk(double(NAN), double(NAN), double(NAN));
+                mpr::store(o, pid, false, D3D_STATUS_BAD_INDEX, opt.penetration, NAN, nan3, nan3);
+                continue;  // the lane fetches again
+            }
             mpr::begin(P, L, mpr::collider_center<float>(st, i), mpr::collider_center<float>(st, j));
             need = false;
         }

@@ -5,9 +5,12 @@
 #include <mutex>
 
 #include "capi_util.h"
+#include "d3d_device.cuh"
 #include "scratch.h"
 
 namespace {
+
+using d3d::pair_ok;
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
@@ -31,8 +34,13 @@ __global__ void k_pair_keys(d3d_store s, const int32_t* __restrict__ i1, const i
         keys[k] = 0x7ffu;
         return;
     }
-    int4 a = __ldg(reinterpret_cast<const int4*>(s.meta) + i1[k]);
-    int4 b = __ldg(reinterpret_cast<const int4*>(s.meta) + i2[k]);
+    const int ia = i1[k], ib = i2[k];
+    if (!pair_ok(s, ia, ib)) {  // the kernels report the pair; its place in the order does not matter
+        keys[k] = 0;
+        return;
+    }
+    int4 a = __ldg(reinterpret_cast<const int4*>(s.meta) + ia);
+    int4 b = __ldg(reinterpret_cast<const int4*>(s.meta) + ib);
     int nv = max(a.x == D3D_HULL || a.x == D3D_MESH ? a.y : 0, b.x == D3D_HULL || b.x == D3D_MESH ? b.y : 0);
     int cls = nv > 0 ? min(32 - __clz(nv), 15) : 0;
     unsigned ta = (unsigned)min(max(a.x, 0), D3D_MESH), tb = (unsigned)min(max(b.x, 0), D3D_MESH);

@@ -148,8 +148,13 @@ __global__ void k_support(d3d_store s, const int32_t* __restrict__ idx, const do
                           int64_t n, double* __restrict__ out) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const int i = idx[k];
+    if (!index_ok(s, i)) {  // out of range: NaN, no record read
+        out[3 * k] = out[3 * k + 1] = out[3 * k + 2] = NAN;
+        return;
+    }
     Col<double> c;
-    load_col(s, idx[k], c);
+    load_col(s, i, c);
     d3 r = support(c, s, mk(dirs[3 * k], dirs[3 * k + 1], dirs[3 * k + 2]));
     out[3 * k] = r.x;
     out[3 * k + 1] = r.y;
@@ -164,8 +169,13 @@ __device__ __forceinline__ double np_max(double a, double b) { return (a != a ||
 __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n, double* __restrict__ out) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
+    const int ci = idx ? idx[k] : (int)k;
+    if (!index_ok(s, ci)) {  // out of range: NaN, no record read
+        for (int j = 0; j < 6; ++j) out[6 * k + j] = NAN;
+        return;
+    }
     Col<double> c;
-    load_col(s, idx ? idx[k] : (int)k, c);
+    load_col(s, ci, c);
     const double* R = c.R;
     const double* t = c.t;
     double lo[3], hi[3];

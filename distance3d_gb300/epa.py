@@ -45,8 +45,8 @@ def epa_batch(store, i1, i2, simplex, *, max_iter=64, max_loose_edges=32, max_fa
     lib = _lib.load()
     opt = _options(max_iter, max_loose_edges, max_faces, epsilon, precision)
     with torch.cuda.device(dev):
-        a = as_index(i1, dev)
-        b = as_index(i2, dev)
+        a = as_index(i1, dev, store.n_colliders)
+        b = as_index(i2, dev, store.n_colliders)
         n = a.numel()
         s = torch.as_tensor(simplex, dtype=torch.float64).reshape(n, 4, 3).to(dev).contiguous()
         mtv = torch.empty((n, 3), dtype=torch.float64, device=dev)

@@ -42,8 +42,8 @@ def gjk_distance_batch(store, i1, i2, *, tolerance=1e-10, max_distance_squared=1
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
     dev = store.device
     with torch.cuda.device(dev):
-        a = as_index(i1, dev)
-        b = as_index(i2, dev)
+        a = as_index(i1, dev, store.n_colliders)
+        b = as_index(i2, dev, store.n_colliders)
         if a.shape != b.shape or a.ndim != 1:
             raise ValueError("i1 and i2 must be 1-D of equal length")
         n = a.numel()
@@ -69,8 +69,8 @@ def gjk_intersection_batch(store, i1, i2, *, tolerance=1e-10, max_iterations=DEF
     (n,) bool and ``status`` (n,) int8 device tensors."""
     dev = store.device
     with torch.cuda.device(dev):
-        a = as_index(i1, dev)
-        b = as_index(i2, dev)
+        a = as_index(i1, dev, store.n_colliders)
+        b = as_index(i2, dev, store.n_colliders)
         n = a.numel()
         hit = torch.empty(n, dtype=torch.int8, device=dev)
         status = torch.empty(n, dtype=torch.int8, device=dev)

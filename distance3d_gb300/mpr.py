@@ -43,8 +43,8 @@ def mpr_batch(store, i1, i2, *, mpr_tolerance=0.0001, max_iterations=100, penetr
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
     dev = store.device
     with torch.cuda.device(dev):
-        a = as_index(i1, dev)
-        b = as_index(i2, dev)
+        a = as_index(i1, dev, store.n_colliders)
+        b = as_index(i2, dev, store.n_colliders)
         if a.shape != b.shape or a.ndim != 1:
             raise ValueError("i1 and i2 must be 1-D of equal length")
         n = a.numel()

@@ -28,11 +28,24 @@ def _stream(device):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
-def as_index(x, device):
-    """int32 device tensor from an index sequence."""
-    if isinstance(x, torch.Tensor):
+def as_index(x, device, n=None):
+    """int32 device tensor from an index sequence.
+
+    A host sequence (NumPy array, list, CPU tensor) with an entry outside
+    [0, n) raises IndexError before anything is copied to the device.  Device
+    tensors are not read back here: the kernels check their entries and
+    report D3D_STATUS_BAD_INDEX for each pair with an index out of range.
+    """
+    if isinstance(x, torch.Tensor) and x.device.type != "cpu":
         return x.to(device=device, dtype=torch.int32).contiguous()
-    return torch.as_tensor(np.ascontiguousarray(x, dtype=np.int32), device=device)
+    a = np.asarray(x.numpy() if isinstance(x, torch.Tensor) else x)
+    if a.size and not np.issubdtype(a.dtype, np.integer):
+        raise TypeError(f"collider indices must be integers, got {a.dtype}")
+    if n is not None and a.size:
+        lo, hi = int(a.min()), int(a.max())
+        if lo < 0 or hi >= n:
+            raise IndexError(f"collider index {lo if lo < 0 else hi} out of range [0, {n})")
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32), device=device)
 
 
 class PinnedColliderSet:
@@ -185,13 +198,13 @@ class ColliderStore:
     def set_poses(self, idx, poses):
         """Set 4x4 (or 12-value R|t) poses of colliders ``idx`` (not hulls)."""
         idx_np = np.asarray(idx.cpu() if isinstance(idx, torch.Tensor) else idx, dtype=np.int64).reshape(-1)
+        ii = as_index(idx_np, self.device, self.n_colliders)
         if np.any((self.types_host[idx_np] & ~MARGIN) == HULL):
             raise NotImplementedError("update_pose is not implemented for ConvexHullVertices")
         p = torch.as_tensor(poses, dtype=torch.float64)
         if p.ndim == 3:
             p = torch.cat([p[:, :3, :3].reshape(-1, 9), p[:, :3, 3]], dim=1)
         p = p.reshape(-1, 12).to(self.device).contiguous()
-        ii = as_index(idx_np, self.device)
         with torch.cuda.device(self.device):
             _lib.check(_lib.load().d3d_store_set_poses(self.view, _ptr(ii), _ptr(p), len(ii), self.stream()))
 
@@ -202,7 +215,7 @@ class ColliderStore:
                 n = self.n_colliders
                 ii = None
             else:
-                ii = as_index(idx, self.device)
+                ii = as_index(idx, self.device, self.n_colliders)
                 n = len(ii)
             out = torch.empty((n, 3, 2), dtype=torch.float64, device=self.device)
             _lib.check(_lib.load().d3d_aabbs(self.view, _ptr(ii), n, _ptr(out), self.stream()))
@@ -211,7 +224,7 @@ class ColliderStore:
     def support(self, idx, directions):
         """(n,3) FP64 support points of colliders ``idx`` along ``directions``."""
         with torch.cuda.device(self.device):
-            ii = as_index(idx, self.device)
+            ii = as_index(idx, self.device, self.n_colliders)
             d = torch.as_tensor(directions, dtype=torch.float64).reshape(-1, 3).to(self.device).contiguous()
             out = torch.empty((len(ii), 3), dtype=torch.float64, device=self.device)
             _lib.check(_lib.load().d3d_support(self.view, _ptr(ii), _ptr(d), len(ii), _ptr(out), self.stream()))

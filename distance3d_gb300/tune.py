@@ -48,8 +48,8 @@ def autotune(store, i1, i2, *, precision="mixed", epa_kw=None, gjk_kw=None):
                            _PRECISIONS[precision], float(ek["epsilon"]))
     dev = store.device
     with torch.cuda.device(dev):
-        a = as_index(i1, dev)
-        b = as_index(i2, dev)
+        a = as_index(i1, dev, store.n_colliders)
+        b = as_index(i2, dev, store.n_colliders)
         t = _lib.Tuning()
         _lib.check(_lib.load().d3d_autotune(store.view, _ptr(a), _ptr(b), a.numel(), ctypes.byref(gopt),
                                             ctypes.byref(eopt), ctypes.byref(t), store.stream()))

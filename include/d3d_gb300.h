@@ -13,6 +13,12 @@
  *   the call returns without synchronising unless stated otherwise.
  * - Pair results are deterministic: one slot per pair, no atomics in result
  *   slots, the same bits for the same inputs whatever the batch around them.
+ * - Collider indices (i1, i2, idx) are device data, so they are checked on
+ *   the device: a pair with an index outside [0, n_colliders) gets
+ *   D3D_STATUS_BAD_INDEX (NaN results, hit 0) and no record is read for it;
+ *   d3d_support and d3d_aabbs write NaN for such an index and
+ *   d3d_store_set_poses skips it.  The Python layer also rejects out-of-range
+ *   host index arrays before any copy.
  *
  * Each entry point names the distance3d 0.9.0 interface it replaces
  * (path:line inside that project).
@@ -59,6 +65,9 @@ extern "C" {
 #define D3D_STATUS_EPA_NOT_CONVERGED 4  /* EPA hit max_iter (epa.py:76-78, success = False) */
 #define D3D_STATUS_EPA_FACE_OVERFLOW 5  /* the reference raises AssertionError (epa.py:128) */
 #define D3D_STATUS_EPA_DEGENERATE 6     /* every face was removed (the reference raises in np.argmin) */
+#define D3D_STATUS_BAD_INDEX 7          /* a collider index of the pair lies outside [0, n_colliders): no record
+                                           was read; distances, points and MTVs are NaN, hit flags 0 (the
+                                           reference raises IndexError on a bad list index) */
 
 #define D3D_PRECISION_FP64 0   /* plain FP64 drop-in: the reference's arithmetic, bit for bit */
 #define D3D_PRECISION_MIXED 1  /* FP32 iterations, FP64 final refinement */
@@ -188,9 +197,12 @@ int d3d_epa(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_
  * inside the library, present on every GPU that loads it until the process
  * exits, and the call fails with D3D_ERR_CAPACITY when max_faces /
  * max_loose_edges leave room for fewer than 128 pairs at a time there
- * (12 * max_faces + 6 * max_loose_edges doubles per pair).  The array also
- * holds the work counter.  The first call on a device (with that device
- * current) looks up the array's address; make that first call before any
+ * (12 * max_faces + 6 * max_loose_edges doubles per pair; the defaults with
+ * 252 or more iterations take this path, 2,184 polytopes at a time).  The
+ * array also holds the work counter.  Every call must be made with the
+ * store's device current: the array used is the current device's, and a
+ * store on another device is rejected with D3D_ERR_INVALID.  The first call
+ * on a device looks up the array's address; make that first call before any
  * stream capture.  All calls share the array: calls whose work overlaps on
  * the GPU race and must be serialised by the caller.  Pairs run in input
  * order (no scheduling sort). */

@@ -222,7 +222,7 @@ def test_edge_colliders_match_reference(golden):
     mixed_check(mg, g, cs, g["i1"], g["i2"])
 
 
-@pytest.mark.parametrize("fx", ["mixed6", "all9", "mesh10"])
+@pytest.mark.parametrize("fx", ["scb", "mixed6", "all9", "mesh10"])
 @pytest.mark.parametrize("tag,kw", [("clip", dict(max_distance_squared=0.01)), ("coarse", dict(tolerance=1e-3))])
 def test_fp64_gjk_options_match_reference_golden(golden, fx, tag, kw):
     """The FP64 GJK with a clipping distance many pairs exceed and with a

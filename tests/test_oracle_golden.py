@@ -110,18 +110,20 @@ def test_mpr_bit_exact(golden, fixture):
     assert np.array_equal(ri["hit"], m["hit_intersection"])
 
 
-@pytest.mark.parametrize("fixture", ["mixed6", "all9", "mesh10"])
+@pytest.mark.parametrize("fixture", ["scb", "mixed6", "all9", "mesh10"])
 @pytest.mark.parametrize("tag,kw", [("clip", dict(max_distance_squared=0.01)), ("coarse", dict(tolerance=1e-3))])
 def test_gjk_options_bit_exact(golden, fixture, tag, kw):
     """gjk_distance_jolt with a clipping distance many pairs exceed
     (MAX_FLOAT, no points, _gjk_jolt.py:209-210) and with a coarse tolerance
     under which the reference's sanity assertion fails on some pairs
-    (_gjk_jolt.py:216, status 2 here)."""
+    (_gjk_jolt.py:216, status 2 here; on the sphere/capsule/box set it fails
+    on none)."""
     g, cs = golden("gjk_" + fixture)
     r = oracle.gjk_distance(cs, g["i1"], g["i2"], **kw)
     st = g[f"status_{tag}"]
     assert np.array_equal(r["status"], st)
-    assert (st == (1 if tag == "clip" else 2)).sum() > 10
+    if not (fixture == "scb" and tag == "coarse"):
+        assert (st == (1 if tag == "clip" else 2)).sum() > 10
     ok = st != 2
     assert np.array_equal(r["dist"][ok], g[f"dist_{tag}"][ok])
     assert np.array_equal(r["cp1"][ok], g[f"cp1_{tag}"][ok], equal_nan=True)

@@ -75,6 +75,7 @@ _SP = ctypes.POINTER(D3DStore)
 SIGNATURES = [
     ("d3d_abi_version", c_int, []),
     ("d3d_last_error", ctypes.c_char_p, []),
+    ("d3d_graph_kernel_nodes", c_int, [c_void_p, ctypes.POINTER(c_int64), ctypes.POINTER(c_int64)]),
     ("d3d_store_pack", c_int, [_SP, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
     ("d3d_store_set_poses", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p]),
     ("d3d_support", c_int, [_SP, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),

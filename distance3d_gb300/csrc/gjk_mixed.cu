@@ -1,37 +1,50 @@
 // gjk_mixed.cu -- mixed-precision GJK distance.
 //
-// Four kernels over the type-sorted pair order:
+// Five kernels over the type-sorted pair order:
 //
 // A  runs the Jolt loop in FP32 on the FP32 mirror of the store, with
 //    thresholds scaled to single precision, hands each pair's outcome, final
-//    closest point and the search direction of each final simplex row to B
+//    closest point and the search direction of each final simplex row on
 //    (80 bytes/pair) and appends clipped and unconverged pairs to the
 //    fallback list.
-// B  walks the same type-sorted order (lanes of a warp then mostly hold
-//    pairs of the same collider types) and refines A's separated and
-//    touching pairs in FP64, one round per lane and iteration (pb_round): A's
-//    final simplex rows are re-evaluated in FP64 along their FP32 directions,
-//    all in the first round (polytope supports choose their vertex by an FP32
-//    argmax and return the FP64 vertex); if that simplex encloses or touches
-//    the origin the pair is done, otherwise the reference's loop continues
-//    from it until the duality gap brackets the distance within 1e-6 of
-//    itself or 1e-9 of the scene's scale.  A pair whose loop ends leaves its
-//    simplex in the outputs and the rest of its state in an end record.
+// R  (the refinement pass) takes one warp per 32 consecutive slots of the
+//    type-sorted order, so that a warp's lanes evaluate the same supports.
+//    Each lane re-evaluates its pair's final simplex rows in FP64 along their
+//    FP32 directions (polytope supports choose their vertex by an FP32 argmax
+//    and return the FP64 vertex) and, for a separated pair, one more support
+//    pair along -v, the closest point A ended on.  A separated pair whose
+//    origin projection lies inside its FP64 feature and whose duality gap
+//    brackets the distance within 1e-6 of itself (or 1e-9 of the scene's
+//    scale) is done there, closest points from the projection's barycentric
+//    coordinates; so is a touching pair whose FP64 tetrahedron encloses the
+//    origin.  Every other separated or touching pair is flagged, its FP64 rows
+//    in its record, and a stable compaction (CUB) lists the flagged pairs in
+//    the type-sorted order.
+// B  continues the reference's loop in FP64 for the listed pairs, one round
+//    per lane and iteration (pb_round): the first round solves the handed
+//    rows, later rounds add a support pair along -v, until the duality gap
+//    closes as in R.  A pair whose loop ends leaves its simplex in the outputs
+//    and the rest of its state in its record.
 // E  (the end pass) computes the closest points and the checks of B's
 //    finished pairs (pb_end), every lane on a finished pair.
 // C  is the plain FP64 kernel over the fallback list (the reference's
 //    arithmetic; CLIPPED and MAX_ITER keep their FP64 meaning).
 //
-// B keeps the simplex P/Q rows in shared memory and has one support call
-// site, so that a warp's lanes share the support and simplex code whatever
-// mode and simplex size each holds.  A pair goes to the fallback list only if
-// its result fails the consistency check (closest points vs |v|) or the
-// sanity check in E, or hits the iteration bound in B.
+// FP64 instructions cost the GB300's FP64 pipe the same however few lanes of
+// a warp are active, so the FP64 work sits where lanes are busy: R runs the
+// same support code on every lane of a warp and a short per-lane solve, and
+// only the pairs R cannot finish (those whose gap or feature check fails)
+// pay for B's divergent per-lane loop.  B keeps the simplex P/Q rows in
+// shared memory and has one support call site.  A pair goes to the fallback
+// list only if its result fails the consistency check (closest points vs |v|)
+// or the sanity check in E, or hits the iteration bound in B.
 //
-// On the six-type workloads A takes ~11 FP32 iterations and B replays ~3
-// rows and runs ~2 FP64 iterations, against ~17-19 FP64 iterations for the
-// plain form.  Compiled with -fmad=true: the tests bound its error against
-// the FP64 oracle.
+// On the six-type workloads A takes ~11 FP32 iterations and R evaluates ~3
+// rows plus the gap row, against ~17-19 FP64 iterations for the plain form.
+// Compiled with -fmad=true: the tests bound its error against the FP64
+// oracle.
+#include <cub/cub.cuh>
+
 #include "capi_util.h"
 #include "gjk_impl.h"
 #include "gjk_mixed.cuh"
@@ -45,25 +58,16 @@ using namespace d3d;
 
 
 // Per-call counters (one 256-byte block): cursors of A, B and C, then the
-// lengths of the fallback and finished lists.
-enum { kCurA = 0, kCurB, kCurC, kNumFallback, kNumEnd, kCounters };
-
-// B's state of a pair whose loop has ended, for the end pass (the simplex's
-// Y rows and row count go to the outputs directly).
-struct alignas(16) EndRecord {
-    double pq[4][6];  // P and Q rows below n
-    double dir[3];
-    double vl;
-    int it;  // A's and B's iterations
-    int state;
-    int status;
-    int n;
-};
+// lengths of the fallback, finished and run lists.
+enum { kCurA = 0, kCurB, kCurC, kNumFallback, kNumEnd, kNumRun, kCounters };
 
 struct Lists {
     int32_t* fallback;
     int32_t* ends;         // pairs whose FP64 loop ended in B, for the end pass
-    EndRecord* records;    // their state, by pair
+    EndRecord* records;    // by pair: R's FP64 rows for B, B's end state for E
+    int8_t* run_flag;      // by slot of the order: R left the pair to B
+    int32_t* run_pid;      // by slot of the order: the pair
+    int32_t* run;          // the flagged pairs in the order (B's work list)
     unsigned long long* ctr;
 };
 
@@ -121,14 +125,163 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
     }
 }
 
+// R, one lane per slot of the order (see the top of this file).  The grid
+// covers the capacity; slots at and beyond the pair count are flagged 0.
 template <int BLOCK, bool MESH>
-__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_t* __restrict__ i1,
+__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_r(d3d_store s, const int32_t* __restrict__ i1,
                                                         const int32_t* __restrict__ i2,
-                                                        const int32_t* __restrict__ order, int64_t n,
+                                                        const int32_t* __restrict__ order, int64_t cap,
                                                         const int64_t* __restrict__ n_dev, d3d_gjk_options opt,
                                                         const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
+    // p and q of up to five rows per lane: element e of row j at [(6 j + e) BLOCK]
+    __shared__ double rows[30 * BLOCK];
+    const int64_t n = n_dev ? *n_dev : cap;
+    const int64_t slot = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+    if (slot >= cap) return;
+    int32_t pid = 0;
+    int outcome = PA_FAILED, nr = 0, it_a = 0;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (slot < n) {
+        pid = order ? order[slot] : (int32_t)slot;
+        v = hand[pid].v;
+        outcome = __float_as_int(v.w) & 0xff;
+        nr = (__float_as_int(v.w) >> 8) & 0xff;
+        it_a = handoff_iters(v);
+    }
+    const bool mine = outcome == PA_SEPARATED || outcome == PA_TOUCHING;  // R or B finishes it
+    const bool rows_ok = mine && nr >= 1 && nr <= 4;
+    const bool sep = rows_ok && outcome == PA_SEPARATED && nr <= 3;
+    const bool touch = rows_ok && outcome == PA_TOUCHING && nr == 4;
+    int a = 0, b = 0;
+    if (rows_ok) {
+        a = i1[pid];
+        b = i2[pid];
+    }
+    // the rows in FP64, then the gap row of a separated pair along -v
+    const int count = rows_ok ? nr + (sep ? 1 : 0) : 0;
+    double* my = rows + threadIdx.x;
+#pragma unroll 1
+    for (int j = 0; j < 5; ++j) {
+        if (j < count) {
+            d3 d;
+            if (j < nr) {
+                const float4 f = hand[pid].d[j];
+                d = mk((double)f.x, (double)f.y, (double)f.z);
+            } else {
+                d = mk(-(double)v.x, -(double)v.y, -(double)v.z);
+            }
+            d3 p, q;
+            pair_supports<double, RefineSupportT<MESH>>(s, a, b, d, p, q);
+            my[(6 * j + 0) * BLOCK] = p.x;
+            my[(6 * j + 1) * BLOCK] = p.y;
+            my[(6 * j + 2) * BLOCK] = p.z;
+            my[(6 * j + 3) * BLOCK] = q.x;
+            my[(6 * j + 4) * BLOCK] = q.y;
+            my[(6 * j + 5) * BLOCK] = q.z;
+        }
+    }
+    auto row_p = [&](int j) { return mk(my[(6 * j) * BLOCK], my[(6 * j + 1) * BLOCK], my[(6 * j + 2) * BLOCK]); };
+    auto row_q = [&](int j) {
+        return mk(my[(6 * j + 3) * BLOCK], my[(6 * j + 4) * BLOCK], my[(6 * j + 5) * BLOCK]);
+    };
+    bool done = false;
+    d3 cp1 = mk(0.0, 0.0, 0.0), cp2 = cp1;
+    double dist = 0.0;
+    d3 w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) w[j] = (j < nr && rows_ok) ? row_p(j) - row_q(j) : mk(0.0, 0.0, 0.0);
+    if (sep) {
+        d3 vv;
+        double lam[3];
+        const bool inside = feature_point(w, nr, vv, lam);
+        const double vl = dot(vv, vv);
+        const d3 wg = row_p(nr) - row_q(nr);
+        const d3 u = mk((double)v.x, (double)v.y, (double)v.z);
+        // distance in [u.wg / |u|, |vv|] (wg is the support of the Minkowski difference along -u)
+        const double upper = sqrt(vl);
+        const double lower = dot(u, wg) / sqrt(dot(u, u));
+        const double gap = upper - lower;
+        double ymax = dot(w[0], w[0]);
+#pragma unroll
+        for (int j = 1; j < 3; ++j)
+            if (j < nr) ymax = maxf2(ymax, dot(w[j], w[j]));
+        const double tol_sq = opt.tolerance * opt.tolerance;
+        // touching in FP64 (pb_round's test) is B's to decide
+        const bool apart = vl > tol_sq && vl > DBL_EPSILON * ymax;
+        const bool closed = gap <= kMixedRelGap * upper || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(wg, wg));
+        if (inside && apart && closed) {
+            cp1 = row_p(0) * lam[0];
+            cp2 = row_q(0) * lam[0];
+#pragma unroll
+            for (int j = 1; j < 3; ++j) {
+                if (j < nr) {
+                    cp1 = cp1 + row_p(j) * lam[j];
+                    cp2 = cp2 + row_q(j) * lam[j];
+                }
+            }
+            dist = upper;
+            const d3 ab = cp1 - cp2;
+            // pb_end's consistency check
+            done = abs_t(sqrt(dot(ab, ab)) - dist) <= 1e-10 * maxf2(dist, 1.0);
+        }
+    } else if (touch) {
+        if (outside_planes(w[0], w[1], w[2], w[3], reference_eps<double>()) == 0) {
+            // the origin inside the FP64 tetrahedron: closest points as gjk_end takes them
+            // (bary_tetra, then merged at distance 0)
+            double o4[4];
+            bary_tetra(w[0], w[1], w[2], w[3], o4);
+            const d3 pa = ((row_p(0) * o4[0] + row_p(1) * o4[1]) + row_p(2) * o4[2]) + row_p(3) * o4[3];
+            const d3 pb = ((row_q(0) * o4[0] + row_q(1) * o4[1]) + row_q(2) * o4[2]) + row_q(3) * o4[3];
+            cp1 = cp2 = (pa + pb) * 0.5;
+            done = true;
+        }
+    }
+    if (done) {
+        o.dist[pid] = dist;
+        o.cp1[3 * (int64_t)pid] = cp1.x;
+        o.cp1[3 * (int64_t)pid + 1] = cp1.y;
+        o.cp1[3 * (int64_t)pid + 2] = cp1.z;
+        o.cp2[3 * (int64_t)pid] = cp2.x;
+        o.cp2[3 * (int64_t)pid + 1] = cp2.y;
+        o.cp2[3 * (int64_t)pid + 2] = cp2.z;
+        double* sp = o.simplex + 12 * (int64_t)pid;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            sp[3 * j] = w[j].x;
+            sp[3 * j + 1] = w[j].y;
+            sp[3 * j + 2] = w[j].z;
+        }
+        o.n_simplex[pid] = (int8_t)nr;
+        o.status[pid] = (int8_t)D3D_STATUS_OK;
+        // the gap row counts as the FP64 iteration that closed the bracket
+        if (o.iterations) o.iterations[pid] = it_a + (sep ? 1 : 0);
+    } else if (mine) {
+        EndRecord& e = lists.records[pid];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j < nr && rows_ok) {
+                const d3 p = row_p(j), q = row_q(j);
+                e.pq[j][0] = p.x;
+                e.pq[j][1] = p.y;
+                e.pq[j][2] = p.z;
+                e.pq[j][3] = q.x;
+                e.pq[j][4] = q.y;
+                e.pq[j][5] = q.z;
+            }
+        }
+        e.n = rows_ok ? nr : 0;
+    }
+    lists.run_flag[slot] = (int8_t)(mine && !done);
+    lists.run_pid[slot] = pid;
+}
+
+// B over R's run list, in the type-sorted order.
+template <int BLOCK, bool MESH>
+__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_t* __restrict__ i1,
+                                                        const int32_t* __restrict__ i2, d3d_gjk_options opt,
+                                                        const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
     __shared__ double rows[24 * BLOCK];
-    if (n_dev) n = *n_dev;
+    const int64_t n = (int64_t)lists.ctr[kNumRun];
     const JoltEps<double> E = reference_eps<double>();
     const double tol_sq = opt.tolerance * opt.tolerance;
     PhaseB<SmemRows<double, BLOCK>> B;
@@ -149,18 +302,14 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
         live = __ballot_sync(live, !quit);
         if (quit) break;
         if (need) {
-            // the pairs in the collider-type order, A's separated and touching ones
-            pid = order ? order[slot] : (int32_t)slot;
-            const float4 v = hand[pid].v;
-            const int outcome = __float_as_int(v.w) & 0xff;
-            if (outcome != PA_SEPARATED && outcome != PA_TOUCHING) continue;
+            pid = lists.run[slot];
             a = i1[pid];
             b = i2[pid];
-            it_a = handoff_iters(v);
-            pb_begin(B, v);
+            it_a = handoff_iters(hand[pid].v);
+            pb_begin(B, lists.records[pid]);
             need = false;
         }
-        if (B.mode == PB_FALLBACK || pb_round<MESH>(B, s, a, b, hand[pid].d, tol_sq, opt, E)) {
+        if (B.mode == PB_FALLBACK || pb_round<MESH>(B, s, a, b, tol_sq, opt, E)) {
             if (B.mode != PB_FALLBACK) {
                 // The closest points and checks of the pair (pb_end) run in
                 // the end pass, where a warp's lanes all hold finished pairs;
@@ -251,16 +400,28 @@ inline size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 
 namespace d3d {
 
-size_t gjk_mixed_scratch_bytes(int64_t capacity) {
-    return 256 + up(sizeof(int32_t) * (size_t)capacity) + pair_order_temp_bytes(capacity) +
-           up(sizeof(Handoff) * (size_t)capacity) + 2 * up(sizeof(int32_t) * (size_t)capacity) +
-           up(sizeof(EndRecord) * (size_t)capacity);
+// temporary storage of the run list's stable compaction (CUB) over n slots
+size_t select_temp_bytes(int64_t n) {
+    size_t b = 0;
+    cub::DeviceSelect::Flagged(nullptr, b, static_cast<const int32_t*>(nullptr), static_cast<const int8_t*>(nullptr),
+                               static_cast<int32_t*>(nullptr), static_cast<unsigned long long*>(nullptr), (int)n);
+    return up(b);
 }
+
+size_t gjk_mixed_scratch_bytes(int64_t capacity) {
+    const size_t c = (size_t)capacity;
+    return 256 + up(sizeof(int32_t) * c) + pair_order_temp_bytes(capacity) + up(sizeof(Handoff) * c) +
+           2 * up(sizeof(int32_t) * c) + up(sizeof(EndRecord) * c) + up(c) + 2 * up(sizeof(int32_t) * c) +
+           select_temp_bytes(capacity);
+}
+
+// R's block: 30 doubles of shared memory per lane
+constexpr int kRefineBlock = 128;
 
 template <int BLOCK, bool MESH>
 int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
                  const int64_t* n_dev, const d3d_gjk_options& opt, Handoff* hand, const DistanceOut& o,
-                 const Lists& lists, int per_sm, cudaStream_t stream) {
+                 const Lists& lists, void* select_temp, size_t select_bytes, int per_sm, cudaStream_t stream) {
     const float tol_sq = (float)(opt.tolerance * opt.tolerance);
     const void* ka = (const void*)k_gjk_mixed_a<BLOCK, MESH>;
     k_gjk_mixed_a<BLOCK, MESH><<<persistent_blocks(ka, BLOCK, n, per_sm), BLOCK, 0, stream>>>(
@@ -268,10 +429,21 @@ int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, c
         lists);
     int rc = check_launch("d3d_gjk_distance (mixed, FP32 phase)");
     if (rc) return rc;
-    const void* kb = (const void*)k_gjk_mixed_b<BLOCK, MESH>;
-    k_gjk_mixed_b<BLOCK, MESH><<<persistent_blocks(kb, BLOCK, n, per_sm), BLOCK, 0, stream>>>(
+    k_gjk_mixed_r<kRefineBlock, MESH><<<grid_for(n, kRefineBlock), kRefineBlock, 0, stream>>>(
         store, i1, i2, order, n, n_dev, opt, hand, o, lists);
-    rc = check_launch("d3d_gjk_distance (mixed, FP64 phase)");
+    rc = check_launch("d3d_gjk_distance (mixed, refinement pass)");
+    if (rc) return rc;
+    // the flagged pairs, in the order of the slots
+    cudaError_t e = cub::DeviceSelect::Flagged(select_temp, select_bytes, lists.run_pid, lists.run_flag, lists.run,
+                                               lists.ctr + kNumRun, (int)n, stream);
+    if (e != cudaSuccess) {
+        set_error("d3d_gjk_distance (mixed, run list): %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    const void* kb = (const void*)k_gjk_mixed_b<BLOCK, MESH>;
+    k_gjk_mixed_b<BLOCK, MESH><<<persistent_blocks(kb, BLOCK, n, per_sm), BLOCK, 0, stream>>>(store, i1, i2, opt,
+                                                                                             hand, o, lists);
+    rc = check_launch("d3d_gjk_distance (mixed, FP64 loop)");
     if (rc) return rc;
     k_gjk_mixed_end<<<persistent_blocks((const void*)k_gjk_mixed_end, 128, n), 128, 0, stream>>>(opt, o, lists);
     return check_launch("d3d_gjk_distance (mixed, end pass)");
@@ -281,17 +453,20 @@ int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, c
 template <int BLOCK>
 int launch_mixed(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* order, int64_t n,
                  const int64_t* n_dev, const d3d_gjk_options& opt, Handoff* hand, const DistanceOut& o,
-                 const Lists& lists, int per_sm, cudaStream_t stream) {
+                 const Lists& lists, void* select_temp, size_t select_bytes, int per_sm, cudaStream_t stream) {
     if (store.n_links > 0)
-        return launch_mixed<BLOCK, true>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, per_sm, stream);
-    return launch_mixed<BLOCK, false>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, per_sm, stream);
+        return launch_mixed<BLOCK, true>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, select_temp,
+                                         select_bytes, per_sm, stream);
+    return launch_mixed<BLOCK, false>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, select_temp, select_bytes,
+                                      per_sm, stream);
 }
 
 int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, int64_t n, const int64_t* n_dev,
                   const d3d_gjk_options& opt, const DistanceOut& o, void* scratch, cudaStream_t stream) {
     const d3d_tuning t = tuning();
     const bool sched = n >= t.sort_min;
-    const size_t order_bytes = up(sizeof(int32_t) * (size_t)n);
+    const size_t c = (size_t)n;
+    const size_t order_bytes = up(sizeof(int32_t) * c);
     const size_t temp_bytes = pair_order_temp_bytes(n);
     char* p = static_cast<char*>(scratch);
     Lists lists;
@@ -302,12 +477,21 @@ int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, 
     void* temp = p;
     p += temp_bytes;
     Handoff* hand = reinterpret_cast<Handoff*>(p);
-    p += up(sizeof(Handoff) * (size_t)n);
+    p += up(sizeof(Handoff) * c);
     lists.fallback = reinterpret_cast<int32_t*>(p);
-    p += up(sizeof(int32_t) * (size_t)n);
+    p += up(sizeof(int32_t) * c);
     lists.ends = reinterpret_cast<int32_t*>(p);
-    p += up(sizeof(int32_t) * (size_t)n);
+    p += up(sizeof(int32_t) * c);
     lists.records = reinterpret_cast<EndRecord*>(p);
+    p += up(sizeof(EndRecord) * c);
+    lists.run_flag = reinterpret_cast<int8_t*>(p);
+    p += up(c);
+    lists.run_pid = reinterpret_cast<int32_t*>(p);
+    p += up(sizeof(int32_t) * c);
+    lists.run = reinterpret_cast<int32_t*>(p);
+    p += up(sizeof(int32_t) * c);
+    void* select_temp = p;
+    const size_t select_bytes = select_temp_bytes(n);
     cudaError_t e = cudaMemsetAsync(lists.ctr, 0, kCounters * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) {
         set_error("d3d_gjk_distance (mixed): %s", cudaGetErrorString(e));
@@ -316,13 +500,14 @@ int gjk_mixed_run(const d3d_store& store, const int32_t* i1, const int32_t* i2, 
     int rc = sched ? pair_order(store, i1, i2, n, order, temp, temp_bytes, stream, n_dev) : D3D_SUCCESS;
     if (!rc) {
         if (t.gjk_block == 64)
-            rc = launch_mixed<64>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, blocks_per_sm(t, 64), stream);
+            rc = launch_mixed<64>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, select_temp, select_bytes,
+                                  blocks_per_sm(t, 64), stream);
         else if (t.gjk_block == 256)
-            rc = launch_mixed<256>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, blocks_per_sm(t, 256),
-                                   stream);
+            rc = launch_mixed<256>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, select_temp, select_bytes,
+                                   blocks_per_sm(t, 256), stream);
         else
-            rc = launch_mixed<128>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, blocks_per_sm(t, 128),
-                                   stream);
+            rc = launch_mixed<128>(store, i1, i2, order, n, n_dev, opt, hand, o, lists, select_temp, select_bytes,
+                                   blocks_per_sm(t, 128), stream);
     }
     if (!rc)
         rc = launch_gjk_f64(store, i1, i2, lists.fallback, n, lists.ctr + kNumFallback, lists.ctr + kCurC, opt, o,

@@ -266,41 +266,60 @@ __device__ __forceinline__ Handoff pa_handoff(const PhaseALoop& L, int outcome) 
 // ---------------------------------------------------------------- phase B
 enum PhaseBMode { PB_RUN = 0, PB_DONE = 1, PB_FALLBACK = 2, PB_REPLAY = 3 };
 
-// FP64 refinement of one pair, a per-lane state machine.  REPLAY: A's final
-// simplex rows are re-evaluated in FP64 along the FP32 directions that
-// produced them, all in one round, and the simplex is solved as the loop's
-// first iteration would (nothing to beat yet).  If it encloses
-// or touches the origin the pair is done; otherwise RUN continues the
-// reference's loop from there, stopped by the duality gap.
+// The FP64 rows of one pair that the refinement pass hands to B: the support
+// points p and q of each row of A's final simplex, evaluated in FP64 along
+// the FP32 direction that produced the row, and their count.  B writes the
+// state of a pair whose loop it ends into the same record for the end pass.
+struct alignas(16) EndRecord {
+    double pq[4][6];  // P and Q rows below n
+    double dir[3];
+    double vl;
+    int it;  // A's and B's iterations
+    int state;
+    int status;
+    int n;
+};
+
+// FP64 continuation of the reference's loop for one pair, a per-lane state
+// machine.  REPLAY: the simplex holds the FP64 rows handed over by the
+// refinement pass, and the first round solves it as the loop's first
+// iteration would (nothing to beat yet).  If it encloses or touches the
+// origin the pair is done; otherwise RUN continues the reference's loop from
+// there, stopped by the duality gap.
 template <typename Rows>
 struct PhaseB {
     GjkLoop<double, Rows> g;
     int mode;
-    int rows;
 };
 
 template <typename Rows>
-__device__ __forceinline__ void pb_begin(PhaseB<Rows>& B, float4 v) {
+__device__ __forceinline__ void pb_begin(PhaseB<Rows>& B, const EndRecord& rec) {
     simplex_clear(B.g.S);
     B.g.it = 0;
     B.g.state = GJK_RUNNING;
     B.g.status = D3D_STATUS_OK;
-    const int outcome = __float_as_int(v.w) & 0xff;
-    B.rows = (__float_as_int(v.w) >> 8) & 0xff;
-    B.mode = (outcome == PA_SEPARATED || outcome == PA_TOUCHING) && B.rows > 0 ? PB_REPLAY : PB_FALLBACK;
+    const int n = rec.n;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (j < n) {
+            const d3 p = mk(rec.pq[j][0], rec.pq[j][1], rec.pq[j][2]);
+            const d3 q = mk(rec.pq[j][3], rec.pq[j][4], rec.pq[j][5]);
+            simplex_push(B.g.S, p - q, p, q);
+        }
+    }
+    B.mode = n > 0 && n <= 4 ? PB_REPLAY : PB_FALLBACK;
 }
 
-// One round for one lane: FP64 supports along every replayed row direction
-// (REPLAY, from `dirs`: all of A's rows in one round) or one pair along the
-// loop's direction (RUN), then the simplex update (_gjk_jolt.py:224-288).
-// Every round ends in the simplex solve, so a warp's lanes reach it together
-// whatever mode each is in.  Returns true once the loop has ended: g.state
-// is GJK_INTERSECTION or GJK_NO_INTERSECTION (pb_end finishes the pair), or
+// One round for one lane: nothing to evaluate in the REPLAY round (the rows
+// are in the simplex), one FP64 support pair along the loop's direction in a
+// RUN round, then the simplex update (_gjk_jolt.py:224-288).  Every round ends
+// in the simplex solve, so a warp's lanes reach it together whatever mode
+// each is in.  Returns true once the loop has ended: g.state is
+// GJK_INTERSECTION or GJK_NO_INTERSECTION (pb_end finishes the pair), or
 // B.mode is PB_FALLBACK (clipped, iteration bound, failed replay).
 template <bool MESH = true, typename Rows>
-__device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, int a, int b,
-                                         const float4* __restrict__ dirs, double tol_sq, const d3d_gjk_options& opt,
-                                         const JoltEps<double>& E) {
+__device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, int a, int b, double tol_sq,
+                                         const d3d_gjk_options& opt, const JoltEps<double>& E) {
     GjkLoop<double, Rows>& g = B.g;
     const bool replay = B.mode == PB_REPLAY;
     if (!replay) {
@@ -309,31 +328,21 @@ __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, in
             return true;
         }
         ++g.it;
-    }
-    const int count = replay ? B.rows : 1;
-    for (int r = 0; r < count; ++r) {
-        d3 d = g.dir;
-        if (replay) {
-            const float4 f = dirs[r];
-            d = mk((double)f.x, (double)f.y, (double)f.z);
-        }
         d3 p, q;
-        pair_supports<double, RefineSupportT<MESH>>(s, a, b, d, p, q);
+        pair_supports<double, RefineSupportT<MESH>>(s, a, b, g.dir, p, q);
         const d3 w = p - q;
-        if (!replay) {
-            const double dd = dot(g.dir, w);
-            if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
-                B.mode = PB_FALLBACK;  // clipped: the FP64 kernel reports it
+        const double dd = dot(g.dir, w);
+        if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
+            B.mode = PB_FALLBACK;  // clipped: the FP64 kernel reports it
+            return true;
+        }
+        if (g.S.n > 0) {
+            // duality gap: |v| - (|v|^2 - v.w) / |v| <= distance <= |v|
+            const double gap = g.vl + dd;
+            if (gap <= kMixedRelGap * g.vl || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl) {
+                g.dir = -g.dir;
+                g.state = GJK_NO_INTERSECTION;
                 return true;
-            }
-            if (g.S.n > 0) {
-                // duality gap: |v| - (|v|^2 - v.w) / |v| <= distance <= |v|
-                const double gap = g.vl + dd;
-                if (gap <= kMixedRelGap * g.vl || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl) {
-                    g.dir = -g.dir;
-                    g.state = GJK_NO_INTERSECTION;
-                    return true;
-                }
             }
         }
         simplex_push(g.S, w, p, q);
@@ -374,6 +383,44 @@ __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, in
     }
     g.prev = g.vl;
     return false;
+}
+
+// ---------------------------------------------------------------- refinement pass
+// Closest point to the origin of the affine hull of the rows w[0..n), n <= 3,
+// and its barycentric coordinates (a Gram-system solve for a triangle, one
+// division).  True only if the point lies strictly inside the feature and the
+// feature is not degenerate (|det| above 1e-10 of d00 d11, i.e. the edges are
+// more than ~1e-5 rad from parallel); otherwise the reference's solve in B
+// decides.  Whether the point is the closest point of the Minkowski
+// difference is certified separately by the duality gap.
+__device__ __forceinline__ bool feature_point(const d3* w, int n, d3& v, double* lam) {
+    lam[1] = lam[2] = 0.0;
+    if (n == 1) {
+        v = w[0];
+        lam[0] = 1.0;
+        return true;
+    }
+    const d3 e0 = w[1] - w[0];
+    if (n == 2) {
+        const double den = dot(e0, e0);
+        const double t = -dot(w[0], e0) / den;
+        v = w[0] + e0 * t;
+        lam[0] = 1.0 - t;
+        lam[1] = t;
+        return den > 0.0 && t > 0.0 && t < 1.0;
+    }
+    const d3 e1 = w[2] - w[0];
+    const double d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1);
+    const double b0 = -dot(w[0], e0), b1 = -dot(w[0], e1);
+    const double det = d00 * d11 - d01 * d01;
+    const double inv = 1.0 / det;
+    const double s = (d11 * b0 - d01 * b1) * inv;
+    const double t = (d00 * b1 - d01 * b0) * inv;
+    v = (w[0] + e0 * s) + e1 * t;
+    lam[0] = 1.0 - s - t;
+    lam[1] = s;
+    lam[2] = t;
+    return det > 1e-10 * (d00 * d11) && s > 0.0 && t > 0.0 && lam[0] > 0.0;
 }
 
 // Finish a pair after its loop.  The closest points use the scale-invariant

@@ -126,6 +126,13 @@ typedef struct d3d_epa_options {
 int d3d_abi_version(void);
 const char* d3d_last_error(void);
 
+/* Diagnostics (no counterpart in the reference): the kernel nodes of a CUDA
+ * graph (a cudaGraph_t passed as void*, child graphs included) that launch
+ * this library's own kernels (*own) and the CUDA toolkit's CUB kernels the
+ * library instantiates (*toolkit), e.g. for a graph captured around
+ * d3d_collide: the kernels one replay launches. */
+int d3d_graph_kernel_nodes(const void* graph, int64_t* own, int64_t* toolkit);
+
 /* Pack a store.  Input arrays are the packed host format already copied to
  * the device: types[n] (D3D_* or-ed with D3D_MARGIN for a Margin wrapper),
  * poses[n][12], params[n][4] (params[3]: the margin), hull_offset[n] (int64;

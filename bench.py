@@ -10,12 +10,17 @@ the intersecting pairs.  Inputs are seeded synthetic data (2.1 M colliders,
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-``value`` is the mixed-precision form, inputs resident in HBM; ``fp64`` the
-plain FP64 drop-in on the same data; ``e2e`` the mixed form through the C ABI
-from pinned host buffers with every host<->device copy inside the timed
-region.  ``--impl reference`` times the CPU reference restatement (oracle,
-all host cores) on the same workload.  Under torchrun each rank processes its
-own shard of pairs (no data exchange) and rank 0 prints one JSON line.
+``value`` is the mixed-precision form, inputs resident in HBM; ``e2e`` the
+mixed form through the C ABI from pinned host buffers with every host<->device
+copy inside the timed region; the plain FP64 drop-in runs on the same data.
+Beside them: the serving loop, the broad+narrow scene, the robot batch, MPR,
+the plain 1,000-pair Sphere/Capsule/Box workload (GPU FP64, the oracle, and
+the reference itself with its JIT disabled), the literal [-1,1]^3 workload,
+and the reference on a sample of the main workload.  The headline figures
+are repeated at the end of the line (``summary``).  ``--impl reference``
+times the CPU reference restatement (oracle, all host cores) on the same
+workload.  Under torchrun each rank processes its own shard of pairs (no
+data exchange) and rank 0 prints one JSON line.
 """
 import argparse
 import json
@@ -41,12 +46,13 @@ EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 # grows in proportion to the pairs
 NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78464256 + 3834112 + 140287744 + 23856896 + 45120768 + 1776384) / 131072,
                            "epa_mixed": (33026304 + 36096 + 37686784 + 27904) / 38814}
-# this library's kernels per timed mixed step (one graph replay): k_pair_keys,
-# k_gjk_mixed_a, k_gjk_mixed_b, k_gjk_mixed_end, k_gjk_distance_f64
-# (fallback list), k_epa_select, k_epa_warp<float>, k_epa_refine,
-# k_epa_warp<double> (fallback list), k_epa_exact_warp (second fallback
-# list); the CUB sort kernels are the toolkit's
-MIXED_STEP_LAUNCHES = 10
+# this library's kernels per timed mixed step (one graph replay), used only
+# when the graph cannot be read back (d3d_graph_kernel_nodes): k_pair_keys,
+# k_gjk_mixed_a, k_gjk_mixed_r, k_gjk_mixed_b, k_gjk_mixed_end,
+# k_gjk_distance_f64 (fallback list), k_epa_select, k_epa_warp<float>,
+# k_epa_refine, k_epa_warp<double> (fallback list), k_epa_exact_warp (second
+# fallback list); the CUB sort and compaction kernels are the toolkit's
+MIXED_STEP_LAUNCHES = 11
 
 # Algorithmic bytes per pair (counted once): two collider records, the hull
 # vertices of hull colliders, and the outputs.  FP64 record 120 B (pose 96 +
@@ -63,6 +69,18 @@ REC64, REC32, OUT_GJK, OUT_EPA = 124, 64, 154, 29
 SUPPORT_FLOPS = [12, 50, 48, 50, 50]
 HULL_FLOPS_PER_VERTEX = 6
 SOLVE_FLOPS = 150
+
+# Flop model of one EPA iteration (FMA = 2), fixed before any EPA flop rate
+# was measured and not tuned since: the two supports (SUPPORT_FLOPS), the
+# visibility test of every live face (EPA_FACE_FLOPS each: w - v0, a dot
+# product, a compare) and the new faces on the horizon (EPA_NEW_FACES of
+# EPA_NEW_FACE_FLOPS each: two edges, a cross product, its norm and the
+# plane offset).  A polytope that gains one vertex per iteration has 4 + 2k
+# faces at iteration k and has run (n_faces - 4) / 2 iterations when it stops
+# (the iteration bound when it does not converge).
+EPA_FACE_FLOPS = 8
+EPA_NEW_FACES = 4
+EPA_NEW_FACE_FLOPS = 40
 
 
 def parse():
@@ -123,16 +141,45 @@ def measure_pipe_peaks(dev):
     return fp64, fp32
 
 
-def gjk_model_flops(cs, i1, i2, iterations):
-    """Model FLOPs of the plain GJK over all pairs, from the per-pair
-    iteration counts (exact: the FP64 kernel reports them)."""
+def bench_config(n, world):
+    """The workload both arms measure (the same dict on both)."""
+    return {"workload": f"{n:,} six-type pairs (Sphere, Capsule, Box, Cylinder, Ellipsoid, ConvexHullVertices), "
+                        "GJK distance + EPA (256 faces, 128 loose edges, 64 iterations) on intersecting pairs",
+            "pairs_per_gpu": n, "center_half_width": workload_half_width(), "seed": SEED,
+            "l2": f"inputs ~{1.6 * n / N_PAIRS:.2g} GB resident (L2 129 MB), no flush between steps",
+            "parallelism": f"replicas x{world}"}
+
+
+def workload_half_width():
+    from distance3d_gb300 import workloads
+    return workloads.INTERSECT30_HALF_WIDTH
+
+
+def support_costs(cs):
+    """Model FLOPs of one support evaluation per collider (SUPPORT_FLOPS)."""
     cost = np.zeros(len(cs))
     for t, f in enumerate(SUPPORT_FLOPS):
         cost[cs.types == t] = f
     hull = cs.types == 5
     cost[hull] = HULL_FLOPS_PER_VERTEX * cs.hull_count[hull]
+    return cost
+
+
+def gjk_model_flops(cs, i1, i2, iterations):
+    """Model FLOPs of a GJK over all pairs, from the per-pair iteration counts
+    (the kernels report them)."""
+    cost = support_costs(cs)
     per_iter = cost[i1] + cost[i2] + SOLVE_FLOPS
     return float(np.sum(per_iter * iterations))
+
+
+def epa_model_flops(cs, i1, i2, n_faces, status, max_iter):
+    """Model FLOPs of EPA on pairs (i1, i2) from their final face counts and
+    statuses (EPA_* table above)."""
+    cost = support_costs(cs)
+    it = np.where(status == 4, max_iter, np.clip((n_faces.astype(np.int64) - 4) // 2, 0, max_iter))
+    per = it * (cost[i1] + cost[i2] + EPA_NEW_FACES * EPA_NEW_FACE_FLOPS) + EPA_FACE_FLOPS * (4 * it + it * (it - 1))
+    return float(np.sum(per))
 
 
 class ClockSampler:
@@ -151,7 +198,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
@@ -193,14 +240,16 @@ class ClockSampler:
 def accuracy_report(store, i1, i2, out_mixed, out_fp64, dev):
     """Errors of the mixed form against the FP64 form (= the reference).
 
-    Distances: relative error where the reference is self-consistent; where
-    its distance disagrees with its own closest points (rare), the mixed
-    result's own duality bracket (exact FP64 supports) is reported instead.
-    EPA depths: both forms return h(n) = n . (s1(n) - s2(-n)), an upper bound
-    on the true depth; pairs where the reference's depth exceeds h(n_mixed)
-    by more than 1e-5 are counted as reference errors, the rest give the
-    error statistics, and any pair where the mixed depth is the larger one
-    beyond 1e-5 is counted as a mixed error."""
+    Every statistic first over all pairs, nothing excluded (the *_all_pairs
+    keys, the EPA status agreement), then the certified split.  Distances:
+    where the reference's distance disagrees with its own closest points
+    (rare), the mixed result's own duality bracket (exact FP64 supports) is
+    reported beside.  EPA depths: both forms return h(n) = n . (s1(n) -
+    s2(-n)), an upper bound on the true depth; pairs where the reference's
+    depth exceeds h(n_mixed) by more than 1e-5 are counted as reference errors
+    (their largest difference is reported), the rest give the certified error
+    statistics, and any pair where the mixed depth is the larger one beyond
+    1e-5 is counted as a mixed error."""
     import torch
     gm, hm, em = out_mixed
     gf, hf, ef = out_fp64
@@ -208,10 +257,15 @@ def accuracy_report(store, i1, i2, out_mixed, out_fp64, dev):
     sep_f = (gf["cp1"] - gf["cp2"]).norm(dim=1)
     incons = ((sep_f - df).abs() > 1e-9 * df.clamp(min=1.0)) & (df > 0)
     ok = ~incons
-    rel = ((dm - df).abs() / df.abs().clamp(min=1.0))[ok].cpu().numpy()
+    rel_all_t = (dm - df).abs() / df.abs().clamp(min=1.0)
+    rel_all = rel_all_t.cpu().numpy()
+    rel = rel_all_t[ok].cpu().numpy()
     sep = df > 1e-6
-    out = {"max_rel_dist_err": float(rel.max()), "p99_rel_dist_err": float(np.percentile(rel, 99)),
+    out = {"max_rel_dist_err_all_pairs": float(rel_all.max()),
+           "p99_rel_dist_err_all_pairs": float(np.percentile(rel_all, 99)),
+           "max_rel_dist_err": float(rel.max()), "p99_rel_dist_err": float(np.percentile(rel, 99)),
            "flags_identical_beyond_1e-6": bool(torch.equal(dm[sep] > 0, df[sep] > 0)),
+           "flag_agreement_all_pairs": float(((dm > 0) == (df > 0)).float().mean().item()),
            "reference_self_inconsistent_pairs": int(incons.sum().item())}
     k = torch.nonzero(incons & (dm > 0)).flatten()
     if k.numel():
@@ -234,8 +288,17 @@ def accuracy_report(store, i1, i2, out_mixed, out_fp64, dev):
     h = (n * (store.support(i1[pairs], n) - store.support(i2[pairs], -n))).sum(dim=1)
     ref_wrong = (db > da + tol) & (h < db - tol)
     good = ~ref_wrong
-    derr = ((da - db).abs() / db.clamp(min=1.0))[good].cpu().numpy()
-    out.update({"epa_pairs_both_converged": int(both.sum().item()),
+    derr_t = (da - db).abs() / db.clamp(min=1.0)
+    derr_all = derr_t.cpu().numpy()
+    derr = derr_t[good].cpu().numpy()
+    sm, sf = em["status"][ia], ef["status"][ib]
+    out.update({"epa_depth_max_rel_err_all_pairs": float(derr_all.max()) if derr_all.size else None,
+                "epa_depth_p99_rel_err_all_pairs": float(np.percentile(derr_all, 99)) if derr_all.size else None,
+                "epa_status_agreement": float((sm == sf).float().mean().item()) if sm.numel() else None,
+                "epa_status_mixed_converged_fp64_not": int(((sm == 0) & (sf != 0)).sum().item()),
+                "epa_status_fp64_converged_mixed_not": int(((sf == 0) & (sm != 0)).sum().item()),
+                "epa_excluded_pairs_max_rel_err": float(derr_t[ref_wrong].max().item()) if ref_wrong.any() else 0.0,
+                "epa_pairs_both_converged": int(both.sum().item()),
                 "epa_converged_mixed": int((em["status"] == 0).sum().item()),
                 "epa_converged_fp64": int((ef["status"] == 0).sum().item()),
                 "epa_depth_max_rel_err": float(derr.max()) if derr.size else None,
@@ -287,8 +350,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": f"{len(i1):,} six-type pairs, GJK distance + EPA (256 faces) on intersecting pairs",
-                   "pairs": len(i1)},
+        "config": bench_config(len(i1), world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
                          "sample": f"{args.steps} full passes over {len(i1)} pairs"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -507,6 +569,226 @@ def mpr_report(store, cs, i1_np, i2_np, dev, reps=3, check_pairs=20000, cpu_pair
     return out
 
 
+def capture_step(store, i1, i2, precision, dev):
+    """One step of the batched form as a CUDA graph: d3d_collide (GJK,
+    device-side selection of the EPA pairs, EPA) over all pairs, inputs
+    resident.  Returns (CollisionBatch, graph)."""
+    import torch
+    from distance3d_gb300.serve import CollisionBatch
+    n = len(i1)
+    b = CollisionBatch(store, n, precision=precision, epa_kw=EPA_KW, graphs=False, classes=[n])
+    b.i1.copy_(torch.as_tensor(i1, device=dev))
+    b.i2.copy_(torch.as_tensor(i2, device=dev))
+    b.n_dev.fill_(n)
+    torch.cuda.synchronize(dev)
+    with torch.cuda.stream(b.stream):
+        b._launch(n)  # first use, outside the capture
+    b.stream.synchronize()
+    try:
+        g = torch.cuda.CUDAGraph(keep_graph=True)  # keeps the graph readable (count_graph_kernels)
+    except TypeError:
+        g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=b.stream):
+        b._launch(n)
+    return b, g
+
+
+def count_graph_kernels(g):
+    """This library's kernel launches per replay of graph g, read from the
+    graph (d3d_graph_kernel_nodes), and the toolkit's CUB kernels it adds;
+    the fixed count MIXED_STEP_LAUNCHES where the graph cannot be read."""
+    import ctypes
+    from distance3d_gb300 import _lib
+    try:
+        raw = g.raw_cuda_graph()
+        own, cub = ctypes.c_int64(0), ctypes.c_int64(0)
+        _lib.check(_lib.load().d3d_graph_kernel_nodes(ctypes.c_void_p(raw), ctypes.byref(own), ctypes.byref(cub)))
+        return {"own": own.value, "toolkit_cub": cub.value, "source": "kernel nodes of the step's CUDA graph"}
+    except Exception as e:  # noqa: BLE001 - older torch without raw_cuda_graph / keep_graph
+        return {"own": MIXED_STEP_LAUNCHES, "toolkit_cub": None, "source": f"fixed count ({type(e).__name__})"}
+
+
+def time_graph(b, g, steps, warmup, stream, barrier):
+    """Seconds for `steps` replays after `warmup`, CUDA events on `stream`."""
+    import torch
+    for _ in range(warmup):
+        g.replay()
+    barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        g.replay()
+    end.record(stream)
+    barrier()
+    return start.elapsed_time(end) / 1e3
+
+
+def phase_times(store, i1, i2, precision, steps, dev):
+    """Device seconds per call of the GJK distance and of EPA (on GJK's
+    intersecting pairs) through the separate entry points, each timed over
+    back-to-back calls so that host-side launch work overlaps the device
+    work.  Returns (gjk_s, epa_s, gjk outputs, EPA pair indices, EPA outputs)."""
+    import torch
+    from distance3d_gb300.epa import epa_batch, epa_scratch_bytes
+    from distance3d_gb300.gjk import gjk_distance_batch
+    stream = torch.cuda.current_stream(dev)
+    n = len(i1)
+    g = gjk_distance_batch(store, i1, i2, precision=precision)
+    hit = torch.nonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4)).flatten()
+    a, b, s = i1[hit], i2[hit], g["simplex"][hit].contiguous()
+    scratch = torch.empty(max(1, epa_scratch_bytes(len(hit), precision=precision, **EPA_KW)), dtype=torch.uint8,
+                          device=dev)
+    e = epa_batch(store, a, b, s, scratch=scratch, precision=precision, **EPA_KW)
+    out = {k: torch.empty_like(v) for k, v in g.items()}
+    torch.cuda.synchronize(dev)
+    t = []
+    for fn in (lambda: gjk_distance_batch(store, i1, i2, precision=precision, out=out),
+               lambda: epa_batch(store, a, b, s, scratch=scratch, precision=precision, **EPA_KW)):
+        fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        t.append(e0.elapsed_time(e1) / 1e3 / steps)
+    return t[0], t[1], g, hit, e, n
+
+
+REF_DIR = os.path.join(ROOT, "baseline", "_ref")
+
+
+def import_reference():
+    """The reference (distance3d 0.9.0, pure Python) from its pip install in
+    baseline/_ref, JIT disabled (the numba and pytransform3d stand-ins of
+    tests/golden/_standins).  Returns (make_golden module, gjk, epa,
+    colliders) or raises ImportError."""
+    if not os.path.isdir(os.path.join(REF_DIR, "distance3d")):
+        raise ImportError("baseline/_ref holds no install of the reference")
+    golden = os.path.join(ROOT, "tests", "golden")
+    if golden not in sys.path:
+        sys.path.insert(0, golden)
+    import make_golden
+    gjk, epa, colliders, _, _ = make_golden.import_reference(REF_DIR)
+    return make_golden, gjk, epa, colliders
+
+
+class _Colliders:
+    """Colliders idx of a ColliderSet, as make_golden.make_ref_colliders reads them."""
+
+    def __init__(self, cs, idx):
+        self.types, self.poses, self.params = cs.types[idx], cs.poses[idx], cs.params[idx]
+        self.hull_offset, self.hull_count, self.vertices = cs.hull_offset[idx], cs.hull_count[idx], cs.vertices
+
+    def __len__(self):
+        return len(self.types)
+
+
+def reference_cpu(cs, i1, i2, with_epa, budget_s=8.0):
+    """The reference itself on the host, one core, JIT disabled: for each
+    pair gjk_distance_jolt and, where it returns distance 0 and with_epa, epa
+    with the bench's limits, looping over the pairs as the reference's own
+    benchmark does (benchmarks/benchmark_gjk.py); stops after budget_s.
+    Returns a dict (value in pairs/s), or an `unavailable` reason."""
+    try:
+        mg, gjk, epa, colliders = import_reference()
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference not importable here: {e}"}
+    import distance3d
+    idx = np.stack([i1, i2], axis=1).reshape(-1)
+    cols = mg.make_ref_colliders(colliders, _Colliders(cs, idx))
+    done, t0 = 0, time.perf_counter()
+    for k in range(len(i1)):
+        c1, c2 = cols[2 * k], cols[2 * k + 1]
+        dist, _, _, simplex = gjk.gjk_distance_jolt(c1, c2)
+        if with_epa and dist == 0.0:
+            try:
+                epa.epa(simplex.copy(), c1, c2, **EPA_KW)
+            except Exception:  # noqa: BLE001 - the reference asserts on face overflow
+                pass
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": UNIT, "cores": 1, "kind": "reference (JIT disabled: numba is absent)",
+            "version": getattr(distance3d, "__version__", "?"),
+            "sample": f"{done} pairs ({el:.1f} s), GJK distance" + (" + EPA on intersecting pairs" if with_epa else "")}
+
+
+def config1_report(dev, n_pairs=1000, seed=0, reps=20):
+    """The plain GJK distance workload: 1,000 Sphere/Capsule/Box pairs
+    (workloads.pairs_sphere_capsule_box: centers U[-1,1]^3), FP64 distance and
+    closest points.  The GPU's plain FP64 form through the public API, device
+    time per call over back-to-back calls with resident inputs, and wall time
+    per call from host index arrays to distances and points in host memory;
+    the oracle's C restatement on the host (all threads, one thread); the
+    reference itself, JIT disabled."""
+    import torch
+    from distance3d_gb300 import workloads
+    from distance3d_gb300.gjk import gjk_distance_batch
+    from distance3d_gb300.store import ColliderStore
+    from oracle import oracle
+    cs, i1, i2 = workloads.pairs_sphere_capsule_box(n_pairs, seed=seed)
+    st = ColliderStore(cs, device=dev)
+    a, b = torch.as_tensor(i1, device=dev), torch.as_tensor(i2, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    gjk_distance_batch(st, a, b)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        gjk_distance_batch(st, a, b)
+    e1.record(stream)
+    e1.synchronize()
+    dev_s = e0.elapsed_time(e1) / 1e3 / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        r = gjk_distance_batch(st, i1, i2)
+        host = {k: r[k].cpu().numpy() for k in ("dist", "cp1", "cp2")}
+    e2e_s = (time.perf_counter() - t0) / reps
+    ref = oracle.gjk_distance(cs, i1, i2)
+    exact = all(np.array_equal(host[k], ref[k]) for k in ("dist", "cp1", "cp2"))
+    cpu = {}
+    full = oracle.max_threads()
+    # one thread last, then the thread count restored (it persists in the OpenMP runtime)
+    for threads in (full, 1, full):
+        oracle.gjk_distance(cs, i1, i2, nthreads=threads)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            oracle.gjk_distance(cs, i1, i2, nthreads=threads)
+        cpu.setdefault(threads, n_pairs * reps / (time.perf_counter() - t0))
+    return {"pairs": n_pairs, "seed": seed, "workload": "Sphere/Capsule/Box, centers U[-1,1]^3, FP64",
+            "intersecting_fraction": float(np.mean(ref["dist"] == 0.0)),
+            "gpu_fp64": {"pairs_per_s": n_pairs / dev_s, "ms_per_call": 1e3 * dev_s,
+                         "e2e_pairs_per_s": n_pairs / e2e_s, "e2e_ms_per_call": 1e3 * e2e_s,
+                         "bit_exact_vs_oracle": bool(exact)},
+            "cpu_port": {"pairs_per_s": cpu[full], "cores": full, "one_core_pairs_per_s": cpu[1],
+                         "kind": "port"},
+            "reference_cpu": reference_cpu(cs, i1, i2, with_epa=False, budget_s=5.0)}
+
+
+def config2a_report(dev, steps, warmup, barrier, n_pairs=N_PAIRS, seed=SEED):
+    """The batched workload as literally specified: centers in [-1,1]^3
+    (about 3% of pairs intersect, not the ~30% the specification states;
+    the headline uses half-width 0.38 for ~30%).  The same graph step, both
+    forms."""
+    import torch
+    from distance3d_gb300 import workloads
+    from distance3d_gb300.store import ColliderStore
+    cs, i1, i2 = workloads.pairs_mixed_six(n_pairs, seed=seed, center_half_width=1.0)
+    st = ColliderStore(cs, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {"pairs": n_pairs, "center_half_width": 1.0, "seed": seed}
+    for precision in ("mixed", "fp64"):
+        b, g = capture_step(st, i1, i2, precision, dev)
+        t = time_graph(b, g, steps, warmup, stream, barrier)
+        out[precision] = {"pairs_per_s": n_pairs * steps / t, "ms_per_step": 1e3 * t / steps,
+                          "intersecting_fraction": float((b.out["epa_status"] >= 0).float().mean().item())}
+        del b, g
+    out["mixed_over_fp64"] = out["mixed"]["pairs_per_s"] / out["fp64"]["pairs_per_s"]
+    return out
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -517,8 +799,6 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=dev)
     from distance3d_gb300 import _lib
     from distance3d_gb300.store import ColliderStore, PinnedColliderSet
-    from distance3d_gb300.gjk import gjk_distance_batch
-    from distance3d_gb300.epa import epa_batch, epa_scratch_bytes
 
     _lib.load()
     cs, i1_np, i2_np = make_workload(args.pairs, rank)
@@ -532,105 +812,45 @@ def run_ours(args):
     i1 = torch.as_tensor(i1_np, device=dev)
     i2 = torch.as_tensor(i2_np, device=dev)
     stream = torch.cuda.current_stream(dev)
-    scratch = torch.empty(max(epa_scratch_bytes(n, precision=p, **EPA_KW) for p in ("fp64", "mixed")),
-                          dtype=torch.uint8, device=dev)
-
-    def step(precision, ev=None):
-        if ev is not None:
-            ev[0].record(stream)
-        g = gjk_distance_batch(store, i1, i2, precision=precision)
-        if ev is not None:
-            ev[1].record(stream)
-        hit = torch.nonzero((g["dist"] == 0.0) & (g["n_simplex"] == 4)).flatten()
-        if ev is not None:
-            ev[2].record(stream)
-        e = epa_batch(store, i1[hit], i2[hit], g["simplex"][hit], scratch=scratch, precision=precision, **EPA_KW)
-        if ev is not None:
-            ev[3].record(stream)
-        return g, hit, e
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
 
-    def timed(precision):
-        for _ in range(args.warmup):
-            step(precision)
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-        barrier()
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        out = None
-        for k in range(args.steps):
-            out = step(precision, evs[k])
-        end.record(stream)
-        barrier()
-        total = start.elapsed_time(end) / 1e3
-        gjk = float(np.mean([e[0].elapsed_time(e[1]) for e in evs])) / 1e3
-        epa = float(np.mean([e[2].elapsed_time(e[3]) for e in evs])) / 1e3
-        if world > 1:
-            t = torch.tensor([total], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total = float(t.item())
-        return total, gjk, epa, out
-
     # the batched form: the autotuner picks the launch parameters on a sample,
     # then one CUDA graph of d3d_collide (GJK, device-side EPA pair selection,
     # EPA) per precision is replayed per step, inputs resident
-    from distance3d_gb300.serve import CollisionBatch
     from distance3d_gb300.tune import autotune
     from distance3d_gb300.tune import get_tuning
     # on the workload itself, outside the timed region
     tuned = get_tuning() if args.no_tune else autotune(store, i1, i2, epa_kw=EPA_KW)
-    batches = {}
-    for precision in ("mixed", "fp64"):
-        b = CollisionBatch(store, n, precision=precision, epa_kw=EPA_KW, graphs=False, classes=[n])
-        b.i1.copy_(i1)
-        b.i2.copy_(i2)
-        b.n_dev.fill_(n)
-        torch.cuda.synchronize(dev)
-        with torch.cuda.stream(b.stream):
-            b._launch(n)  # first use, outside the capture
-        b.stream.synchronize()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=b.stream):
-            b._launch(n)
-        batches[precision] = (b, g)
+    batches = {precision: capture_step(store, i1, i2, precision, dev) for precision in ("mixed", "fp64")}
+    launches_per_step = count_graph_kernels(batches["mixed"][1])
 
     def graph_timed(precision):
         b, g = batches[precision]
-        for _ in range(args.warmup):
-            g.replay()
-        barrier()
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        for _ in range(args.steps):
-            g.replay()
-        end.record(stream)
-        barrier()
-        total = start.elapsed_time(end) / 1e3
+        total = time_graph(b, g, args.steps, args.warmup, stream, barrier)
         if world > 1:
             t = torch.tensor([total], device=dev)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             total = float(t.item())
         o = b.out
         hit = torch.nonzero(o["epa_status"] >= 0).flatten()
-        return total, (o, hit, {"mtv": o["mtv"][hit], "status": o["epa_status"][hit]})
+        return total, (o, hit, {"mtv": o["mtv"][hit], "status": o["epa_status"][hit],
+                                "n_faces": o["n_faces"][hit]})
 
     with ClockSampler(local) as clocks:
         t_mixed, out_mixed = graph_timed("mixed")
     t_fp64, out_fp64 = graph_timed("fp64")
-    # per-phase split (GJK / EPA) of each form from the separate-call path, one
-    # extra timed pass each (not the headline)
-    _, gjk_mixed, epa_mixed, _ = timed("mixed")
-    _, gjk_fp64, epa_fp64, _ = timed("fp64")
+    # per-phase split (GJK / EPA) of each form through the separate entry
+    # points (not the headline)
+    gjk_mixed, epa_mixed, *_ = phase_times(store, i1, i2, "mixed", max(2, args.steps), dev)
+    gjk_fp64, epa_fp64, *_ = phase_times(store, i1, i2, "fp64", max(2, min(args.steps, 5)), dev)
 
     # accuracy of the mixed form against the FP64 form (which equals the
     # reference bit for bit); see accuracy_report
     acc = accuracy_report(store, i1, i2, out_mixed, out_fp64, dev)
-    gm, hm, em = out_mixed
-    n_epa = int(hm.numel())
 
     # end to end through the public API from pinned host buffers: every step
     # copies its colliders to the device and packs them into a resident store
@@ -673,28 +893,33 @@ def run_ours(args):
     fp64_value = world * n * args.steps / t_fp64
     e2e_value = world * n * args.steps / t_e2e
 
-    # compute roofline of the plain FP64 GJK kernel (one kernel per call):
-    # model FLOPs from its exact iteration counts / event-timed duration,
-    # against the measured FP64 FMA peak
+    # pipe rooflines: model FLOPs (fixed tables above) over event-timed
+    # duration, against the FP32 and FP64 FMA peaks measured in this run
     peak64, peak32 = measure_pipe_peaks(dev)
-    gf = out_fp64[0]
-    flops64 = gjk_model_flops(cs, i1_np, i2_np, gf["iterations"].cpu().numpy())
-    compute_roofline = {"kernel": "k_gjk_distance_f64", "bound": "fp64 pipe",
-                        "model_flops_per_launch": flops64, "achieved_tflops": flops64 / gjk_fp64 / 1e12,
-                        "peak_tflops": peak64 / 1e12, "frac": flops64 / gjk_fp64 / peak64,
-                        "peak_source": "measured in this run (FMA chains, libd3d_peak)",
-                        "fp32_peak_tflops": peak32 / 1e12}
+    gm, hm, em = out_mixed
+    gf, hf, ef = out_fp64
+    n_epa = int(hm.numel())
+    hm_np, hf_np = hm.cpu().numpy(), hf.cpu().numpy()
+    flops = {
+        "gjk_mixed": gjk_model_flops(cs, i1_np, i2_np, gm["iterations"].cpu().numpy()),
+        "gjk_fp64": gjk_model_flops(cs, i1_np, i2_np, gf["iterations"].cpu().numpy()),
+        "epa_mixed": epa_model_flops(cs, i1_np[hm_np], i2_np[hm_np], em["n_faces"].cpu().numpy(),
+                                     em["status"].cpu().numpy(), EPA_KW["max_iter"]),
+        "epa_fp64": epa_model_flops(cs, i1_np[hf_np], i2_np[hf_np], ef["n_faces"].cpu().numpy(),
+                                    ef["status"].cpu().numpy(), EPA_KW["max_iter"])}
+    times = {"gjk_mixed": gjk_mixed, "epa_mixed": epa_mixed, "gjk_fp64": gjk_fp64, "epa_fp64": epa_fp64}
+    peak_src = "FMA chains measured in this run (libd3d_peak)"
+    compute_roofline = {}
+    for key, kernel, peak in (("gjk_fp64", "k_gjk_distance_f64", peak64), ("epa_fp64", "k_epa_exact_warp", peak64),
+                              ("gjk_mixed", "k_gjk_mixed_a/_r/_b/_end", peak32),
+                              ("epa_mixed", "k_epa_warp<float> + k_epa_refine", peak32)):
+        compute_roofline[key] = {"kernel": kernel, "bound": "fp64 pipe" if peak is peak64 else "fp32 pipe",
+                                 "model_flops_per_launch": flops[key], "ms": 1e3 * times[key],
+                                 "achieved_tflops": flops[key] / times[key] / 1e12, "peak_tflops": peak / 1e12,
+                                 "frac": flops[key] / times[key] / peak}
 
-    # roofline: the dominant kernel of the mixed step
-    gjk_bytes = algorithmic_bytes(cs, i1_np, 0, "mixed") - OUT_EPA * 0
-    epa_bytes = n_epa * (2 * REC64 + OUT_EPA + 96)
-    if gjk_mixed >= epa_mixed:
-        dom, t_dom, bytes_dom = ("d3d_gjk_distance mixed (k_gjk_mixed_a, k_gjk_mixed_b, k_gjk_mixed_end)", gjk_mixed,
-                                 gjk_bytes)
-        traffic = NCU_DRAM_BYTES_PER_PAIR["gjk_mixed"] * n
-    else:
-        dom, t_dom, bytes_dom = "d3d_epa mixed (k_epa_warp, k_epa_refine)", epa_mixed, epa_bytes
-        traffic = NCU_DRAM_BYTES_PER_PAIR["epa_mixed"] * n_epa
+    # roofline: the dominant kernel set of the mixed step, against both its
+    # pipe (FP32 FMA) and HBM; `bound` names the larger fraction
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -702,7 +927,27 @@ def run_ours(args):
     except OSError:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = bytes_dom / t_dom / 1e9
+    gjk_bytes = algorithmic_bytes(cs, i1_np, 0, "mixed")
+    epa_bytes = n_epa * (2 * REC64 + OUT_EPA + 96)
+    if gjk_mixed >= epa_mixed:
+        dom, key, bytes_dom = "d3d_gjk_distance mixed (k_gjk_mixed_a, _r, _b, _end)", "gjk_mixed", gjk_bytes
+        traffic = NCU_DRAM_BYTES_PER_PAIR["gjk_mixed"] * n
+    else:
+        dom, key, bytes_dom = "d3d_epa mixed (k_epa_warp<float>, k_epa_refine)", "epa_mixed", epa_bytes
+        traffic = NCU_DRAM_BYTES_PER_PAIR["epa_mixed"] * n_epa
+    t_dom = times[key]
+    hbm = {"achieved": bytes_dom / t_dom / 1e9, "peak": hbm_peak, "unit": "GB/s",
+           "frac": bytes_dom / t_dom / 1e9 / hbm_peak, "algorithmic_bytes_per_launch": bytes_dom,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
+    pipe = compute_roofline[key]
+    if pipe["frac"] >= hbm["frac"]:
+        roofline = {"bound": "fp32 pipe", "kernel": dom, "achieved": pipe["achieved_tflops"],
+                    "peak": pipe["peak_tflops"], "unit": "TFLOP/s", "frac": pipe["frac"], "traffic": traffic,
+                    "model_flops_per_launch": pipe["model_flops_per_launch"], "peak_source": peak_src, "hbm": hbm}
+    else:
+        roofline = dict(hbm, bound="hbm", kernel=dom, traffic=traffic, pipe=pipe)
+    roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum at 131,072 pairs, "
+                                  "scaled by the pair count")
 
     line = None
     if rank == 0:
@@ -710,40 +955,65 @@ def run_ours(args):
         broad = None if args.no_extras else broad_narrow_report(dev)
         robot = None if args.no_extras else robot_report(dev)
         mpr = None if args.no_extras else mpr_report(store, cs, i1_np, i2_np, dev)
+        cfg1 = None if args.no_extras else config1_report(dev)
+        cfg2a = None if args.no_extras else config2a_report(dev, max(2, min(args.steps, 5)), args.warmup, barrier)
         cpu_value, cores, cpu_pairs, cpu_s = time_cpu(cs, i1_np, i2_np, args.cpu_seconds)
+        sample = np.random.default_rng(1).choice(n, 1000, replace=False)
+        ref_cpu = None if args.no_extras else reference_cpu(cs, i1_np[sample], i2_np[sample], with_epa=True)
+        fp64 = {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * t_fp64 / args.steps,
+                "gjk_ms": 1e3 * gjk_fp64, "epa_ms": 1e3 * epa_fp64}
+
+        def serve_summary(s):
+            if not s:
+                return None
+            return {p: {"peak_pairs_per_s": s[p]["peak_pairs_per_s"],
+                        **{f"p50_p99_ms_at_{lvl}": [s[p][f"load_{lvl}"]["p50_ms"], s[p][f"load_{lvl}"]["p99_ms"]]
+                           for lvl in (50, 80, 100)},
+                        "p99_ms_runs_at_80": s[p]["load_80"]["p99_ms_per_run"]} for p in ("mixed", "fp64")}
+
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_mixed / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"{n:,} six-type pairs, GJK distance + EPA (256 faces) on "
-                                   "intersecting pairs, centers in [-0.38,0.38]^3",
-                       "pairs_per_gpu": n, "intersecting_fraction": n_epa / n, "epa_pairs": n_epa,
-                       "l2": "inputs 1.6 GB > L2, no flush", "parallelism": f"replicas x{world}"},
-            "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * t_fp64 / args.steps,
-                     "gjk_ms": 1e3 * gjk_fp64, "epa_ms": 1e3 * epa_fp64},
-            "mixed_over_fp64": value / fp64_value,
-            "kernels_ms": {"gjk_mixed": 1e3 * gjk_mixed, "epa": 1e3 * epa_mixed,
-                           "gjk_fp64": 1e3 * gjk_fp64},
-            "accuracy": acc,
+            "config": bench_config(n, world),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": traffic,
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum at 131,072 pairs, "
-                                           "scaled by the pair count",
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"},
-            "compute_roofline": compute_roofline,
+            "roofline": roofline,
             "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{cpu_pairs} pairs ({cpu_s:.1f} s) of the same workload, "
                                        "GJK + EPA, C restatement with OpenMP"},
+            "gpu_launches": launches_per_step["own"] * args.steps,
+            "gpu_launches_per_step": launches_per_step,
+            "clocks": clocks.summary(),
+            "step": "one CUDA-graph replay of d3d_collide (GJK, EPA pair selection, EPA) over all pairs",
+            "tuning": tuned,
+            "workload_stats": {"intersecting_fraction": n_epa / n, "epa_pairs": n_epa},
+            # the sections in full
+            "accuracy": acc,
             "serve": serve,
             "broad_narrow": broad,
             "robot_self_collision": robot,
             "mpr": mpr,
-            "tuning": tuned,
-            "step": "one CUDA-graph replay of d3d_collide (GJK, EPA pair selection, EPA) over all pairs",
-            "gpu_launches": MIXED_STEP_LAUNCHES * args.steps,
-            "clocks": clocks.summary(),
+            "config1_plain_gjk_1000_pairs": cfg1,
+            "config2a_literal_unit_box": cfg2a,
+            "reference_cpu": ref_cpu,
+            # the headline figures again, last, where a truncated tail of the
+            # line still shows them
+            "summary": {
+                "mixed_pairs_per_s": value, "e2e_pairs_per_s": e2e_value, "fp64": fp64,
+                "mixed_over_fp64": value / fp64_value,
+                "phase_ms": {k: 1e3 * v for k, v in times.items()},
+                "pipe_frac": {k: v["frac"] for k, v in compute_roofline.items()},
+                "accuracy": {k: acc.get(k) for k in ("max_rel_dist_err_all_pairs", "p99_rel_dist_err_all_pairs",
+                                                     "flags_identical_beyond_1e-6",
+                                                     "epa_depth_max_rel_err_all_pairs",
+                                                     "epa_depth_p99_rel_err_all_pairs", "epa_status_agreement")},
+                "serve": serve_summary(serve),
+                "config1_gpu_fp64_pairs_per_s": cfg1["gpu_fp64"]["pairs_per_s"] if cfg1 else None,
+                "config2a_mixed_pairs_per_s": cfg2a["mixed"]["pairs_per_s"] if cfg2a else None,
+                "cpu_port_pairs_per_s": cpu_value,
+                "reference_cpu_pairs_per_s": (ref_cpu or {}).get("value"),
+                "compute_roofline": compute_roofline},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -202,6 +202,79 @@ __device__ __forceinline__ int hull_argmax(const T* verts, int off, int nv, V3<T
     return best;
 }
 
+// The same first maximum over the FP64 vertices (v64), found with the FP32
+// mirror (v32, each coordinate the FP64 one rounded to nearest) so that the
+// FP64 pipe evaluates only the vertices that can win.  For vertex k the FP32
+// product s_k = v32_k . d32 (dot102 order) and the FP64 product the
+// reference computes differ by at most
+//     E_k = 2^-20 S_k + 2^-126 (|v32_k|_1 + |d32|_1 + 1),   S_k = sum_i |v32_ki d32_i|
+// (16 unit roundoffs of the FP32 operands and products, 2^-24 each, plus an
+// absolute term that covers denormal operands).  A first FP32 pass finds
+// L = max_k (s_k - E_k), a lower bound on the FP64 maximum; the second pass
+// computes the FP64 product only where s_k + E_k >= L, in index order with
+// the strict comparison of hull_argmax.  Every vertex it skips has an FP64
+// product below L, so the index is hull_argmax's, bit for bit.  With a
+// non-finite FP32 value (NaN or infinite coordinates, or magnitudes beyond
+// FP32) the plain FP64 scan runs instead.
+struct Filter32 {
+    float dx, dy, dz, dabs;
+};
+__device__ __forceinline__ Filter32 filter32(V3<double> d) {
+    Filter32 f;
+    f.dx = __double2float_rn(d.x);
+    f.dy = __double2float_rn(d.y);
+    f.dz = __double2float_rn(d.z);
+    f.dabs = fabsf(f.dx) + fabsf(f.dy) + fabsf(f.dz);
+    return f;
+}
+// (s_k, E_k) of vertex row `row` of the FP32 mirror
+__device__ __forceinline__ float2 filter_product(const float* v32, int row, const Filter32& f) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(v32) + row);
+    const float s = fmaf(v.z, f.dz, fmaf(v.x, f.dx, v.y * f.dy));
+    const float sa = fmaf(fabsf(v.z), fabsf(f.dz), fmaf(fabsf(v.x), fabsf(f.dx), fabsf(v.y) * fabsf(f.dy)));
+    const float e = fmaf(sa, 0x1p-20f, 0x1p-126f * (fabsf(v.x) + fabsf(v.y) + fabsf(v.z) + f.dabs + 1.f));
+    return make_float2(s, e);
+}
+
+__device__ __forceinline__ int hull_argmax_filtered(const double* v64, const float* v32, int off, int nv, V3<double> d) {
+    if (nv <= 1) return 0;
+    const Filter32 f = filter32(d);
+    float lo = -INFINITY;
+    bool finite = isfinite(f.dabs);
+#pragma unroll 1
+    for (int k = 0; k < nv; ++k) {
+        const float2 se = filter_product(v32, off + k, f);
+        finite &= isfinite(se.x) && isfinite(se.y);
+        lo = fmaxf(lo, se.x - se.y);
+    }
+    // not finite: every vertex is a candidate, which is hull_argmax's scan
+    const bool all = !finite;
+    int best = -1;
+    double bd = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < nv; ++k) {
+        const float2 se = filter_product(v32, off + k, f);
+        if (all || se.x + se.y >= lo) {
+            const V3<double> w = load_vertex(v64, off + k);
+            const double x = dot102(w.x, w.y, w.z, d.x, d.y, d.z);
+            if (best < 0 || x > bd) {
+                bd = x;
+                best = k;
+            }
+        }
+    }
+    return best;
+}
+
+// The first-maximum vertex of a box or hull in the store: FP64 through the
+// FP32 filter, FP32 directly.
+__device__ __forceinline__ int polytope_argmax(const d3d_store& st, int off, int nv, V3<double> d) {
+    return hull_argmax_filtered(st.verts64, st.verts32, off, nv, d);
+}
+__device__ __forceinline__ int polytope_argmax(const d3d_store& st, int off, int nv, V3<float> d) {
+    return hull_argmax(st.verts32, off, nv, d);
+}
+
 // utils.py:78-122 plane_basis_from_normal: x, y of the plane with normal n
 // (unfused Python scalar arithmetic); the record of a disk stores them as R
 // columns 0 and 1.
@@ -392,7 +465,7 @@ __device__ __forceinline__ V3<T> base_support(const Col<T>& c, const d3d_store& 
     }
     default:
         if (c.nv < 1) return mk(T(NAN), T(NAN), T(NAN));  // rejected by d3d_store_pack
-        return load_vertex(verts, c.off + hull_argmax(verts, c.off, c.nv, d));
+        return load_vertex(verts, c.off + polytope_argmax(st, c.off, c.nv, d));
     }
 }
 

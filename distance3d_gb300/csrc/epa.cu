@@ -357,7 +357,9 @@ __device__ d3 minkowski_exact_warp(const d3d_store& st, int a, int b, d3 d) {
         if (c.nv < 1) {
             s = mk(double(NAN), double(NAN), double(NAN));
         } else {
-            // first maximum of V . d (dot102); a NaN at vertex 0 wins, later NaNs never do
+            // first maximum of V . d (dot102); a NaN at vertex 0 wins, later NaNs never do.  (The
+            // FP32 filter of hull_argmax_filtered does not pay here: with 16 lanes a typical hull
+            // takes a few FP64 rounds, about what its FP32 passes and reductions cost.)
             const int h = ln & 15;
             double bv = 0.0;
             int bi = -1;

@@ -21,8 +21,13 @@ constexpr int kChunk = 32;
 // pair at a time (one iteration per round) and fetches the next pair, in the
 // type-sorted `order`, when its pair ends.  `n_dev` (if not null) holds the
 // pair count on the device (fallback lists of the mixed form).
+// The register budget of 12 resident warps per SM (at most 168 registers a
+// thread), which ptxas would otherwise trade for a few more registers.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_gjk_distance_f64(d3d_store s, const int32_t* __restrict__ i1,
+constexpr int f64_min_blocks() { return BLOCK >= 384 ? 1 : 384 / BLOCK; }
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, f64_min_blocks<BLOCK>()) k_gjk_distance_f64(d3d_store s, const int32_t* __restrict__ i1,
                                                             const int32_t* __restrict__ i2,
                                                             const int32_t* __restrict__ order, int64_t n,
                                                             const unsigned long long* __restrict__ n_dev,
@@ -36,7 +41,7 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_distance_f64(d3d_store s, const i
     g.S.R.base = rows + threadIdx.x;
     int64_t pid = 0;
     int a = 0, b = 0;
-    bool need = true;
+    bool need = true, bad = false;
     unsigned live = __activemask();  // the warp's lanes still in the loop
     WarpChunk chunk;
     // whole chunks to the end of the order: with long pairs, the lanes' coherence outweighs the slots
@@ -52,16 +57,16 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_distance_f64(d3d_store s, const i
             pid = order ? order[slot] : slot;
             a = i1[pid];
             b = i2[pid];
-            if (!pair_ok(s, a, b)) {
-                store_bad_index(o, pid);
-                continue;  // the lane fetches again
-            }
+            bad = !pair_ok(s, a, b);
             simplex_clear(g.S);
             const d3 dir = mk(1.0, 0.0, 0.0);
             gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
             need = false;
         }
-        if (gjk_step<double>(g, s, a, b, tol_sq, opt.max_distance_squared, opt.max_iterations, E)) {
+        if (bad) {  // out-of-range index: reported at once, no record read
+            store_bad_index(o, pid);
+            need = true;
+        } else if (gjk_step<double>(g, s, a, b, tol_sq, opt.max_distance_squared, opt.max_iterations, E)) {
             GjkResult<double> r;
             gjk_end(g, opt.sanity_check, E, r);
             store_result(o, pid, r, g.S);
@@ -148,7 +153,18 @@ int launch_gjk_f64(const d3d_store& store, const int32_t* i1, const int32_t* i2,
                    const unsigned long long* n_dev, unsigned long long* cursor, const d3d_gjk_options& opt,
                    const DistanceOut& o, cudaStream_t stream) {
     const d3d_tuning t = tuning();
-    if (t.gjk_block == 64) {
+    int sms = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 32LL * sms) {
+        // A small batch: one warp per block, so that the pairs spread over
+        // as many SMs as they fill warps.  An FP64 instruction costs an SM's
+        // FP64 pipe the same however few lanes are active, so fewer warps
+        // per SM finish each round sooner (1,000 pairs: 32 SMs instead of 8).
+        const int blocks = (int)((n + 31) / 32);
+        k_gjk_distance_f64<32><<<blocks > 0 ? blocks : 1, 32, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor,
+                                                                           opt, o);
+    } else if (t.gjk_block == 64) {
         const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<64>, 64, n, blocks_per_sm(t, 64));
         k_gjk_distance_f64<64><<<blocks, 64, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
     } else if (t.gjk_block == 256) {

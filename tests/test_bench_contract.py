@@ -19,6 +19,9 @@ def test_reference_arm_prints_one_contract_line():
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert key in d, key
     assert d["impl"] == "reference" and d["unit"] == "pairs/s" and d["value"] > 0
-    assert d["config"]["pairs"] == 4096
+    # the same config dict as the GPU arm's (bench.bench_config)
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.bench_config(4096, 1)
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0

@@ -398,17 +398,21 @@ def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=8192, slots=8, r
                 rate = load * peak / mean_size
                 count = max(20, int(rate * seconds))
                 runs = []
+                srv.stats(reset=True)
                 for _ in range(repeats):
                     sz, a, b = trace(count)
                     offsets = np.cumsum(rng.exponential(1.0 / rate, count))
                     lat, span = srv.replay(sz, a, b, offsets)
                     runs.append((float(np.percentile(lat, 50) * 1e3), float(np.percentile(lat, 99) * 1e3),
-                                 float(lat.max() * 1e3), float(sz.sum()) / span))
+                                 float(lat.max() * 1e3), float(sz.sum()) / span, srv.stats(reset=True)))
                 med = sorted(runs, key=lambda r: r[1])[len(runs) // 2]  # the run with the median p99
                 res[f"load_{int(load * 100)}"] = {
                     "offered_pairs_per_s": load * peak, "p50_ms": med[0], "p99_ms": med[1], "max_ms": med[2],
                     "served_pairs_per_s": med[3], "requests": count,
-                    "p99_ms_per_run": [r[1] for r in runs]}
+                    "p99_ms_per_run": [r[1] for r in runs],
+                    # per run: the longest batch on the device and the longest host-side pass of the
+                    # server's worker, which tell a slow batch from a stalled host thread
+                    "worker_stats_per_run": [r[4] for r in runs]}
         finally:
             srv.close()
         out[precision] = res

@@ -52,6 +52,11 @@ class PairResults(ctypes.Structure):
                                                "iterations", "mtv", "epa_status", "n_faces")]
 
 
+class ServerStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_int64), ("max_batch_s", ctypes.c_double), ("max_enqueue_s", ctypes.c_double),
+                ("max_loop_gap_s", ctypes.c_double)]
+
+
 class Tuning(ctypes.Structure):
     _fields_ = [("gjk_block", ctypes.c_int32), ("gjk_warps_per_sm", ctypes.c_int32), ("epa_warps", ctypes.c_int32),
                 ("sort_min", ctypes.c_int32)]
@@ -106,6 +111,7 @@ SIGNATURES = [
     ("d3d_server_submit", c_int, [c_void_p, c_void_p, c_void_p, c_int64, ctypes.POINTER(c_int64)]),
     ("d3d_server_wait", c_int, [c_void_p, c_int64, c_double]),
     ("d3d_server_result", c_int, [c_void_p, c_int64, ctypes.POINTER(PairResults), ctypes.POINTER(c_double)]),
+    ("d3d_server_stats_read", c_int, [c_void_p, ctypes.POINTER(ServerStats), c_int]),
     ("d3d_server_replay", c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                   ctypes.POINTER(c_double)]),
     ("d3d_bvh_bytes", c_size_t, [c_int64]),

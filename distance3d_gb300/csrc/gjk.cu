@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(BLOCK, f64_min_blocks<BLOCK>()) k_gjk_distance
             gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
             need = false;
         }
+        __syncwarp(live);  // the round starts converged (gjk_step keeps it so through the solve)
         if (bad) {  // out-of-range index: reported at once, no record read
             store_bad_index(o, pid);
             need = true;

@@ -111,7 +111,8 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
             pa_begin(L);
             need = false;
         }
-        // a pair with an out-of-range index ends at once; B skips it (its outcome is neither
+        __syncwarp(live);  // the round starts converged (pa_step keeps it so through the solve)
+        // a pair with an out-of-range index ends at once; R skips it (its outcome is neither
         // separated nor touching) and it joins no list
         const int o = bad ? PA_BAD_INDEX : pa_step<MESH>(L, s, a, b, tol_sq, max_d2, max_iter);
         const bool done = o >= 0;
@@ -309,6 +310,7 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_b(d3d_store s, const int32_
             pb_begin(B, lists.records[pid]);
             need = false;
         }
+        __syncwarp(live);  // the round starts converged (pb_round keeps it so through the solve)
         if (B.mode == PB_FALLBACK || pb_round<MESH>(B, s, a, b, tol_sq, opt, E)) {
             if (B.mode != PB_FALLBACK) {
                 // The closest points and checks of the pair (pb_end) run in

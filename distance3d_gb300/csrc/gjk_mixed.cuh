@@ -227,8 +227,12 @@ __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a,
     const JoltEps<float> E = fp32_eps();
     if (L.it >= max_iter) return PA_FAILED;
     ++L.it;
+    const unsigned together = __activemask();
     f3 p, q;
     pair_supports<float, FastSupportT<MESH>>(s, a, b, L.dir, p, q);
+    // reconverge after the type- and size-dependent supports, so that the
+    // lanes solve their simplices together (see gjk_step)
+    __syncwarp(together);
     f3 w = p - q;
     float dd = dot(L.dir, w);
     if (dd < 0.f && dd * dd > L.vl * max_d2) return PA_CLIPPED;
@@ -322,30 +326,38 @@ __device__ __forceinline__ bool pb_round(PhaseB<Rows>& B, const d3d_store& s, in
                                          const d3d_gjk_options& opt, const JoltEps<double>& E) {
     GjkLoop<double, Rows>& g = B.g;
     const bool replay = B.mode == PB_REPLAY;
+    // The lanes that call together solve together: the support and its
+    // checks only set `ended`, and all lanes reconverge before the solve (see
+    // gjk_step).
+    const unsigned together = __activemask();
+    int ended = 0;  // 1: to the fallback (iteration bound, clipped); 2: the duality gap closed
     if (!replay) {
         if (g.it >= opt.max_iterations) {
-            B.mode = PB_FALLBACK;
-            return true;
-        }
-        ++g.it;
-        d3 p, q;
-        pair_supports<double, RefineSupportT<MESH>>(s, a, b, g.dir, p, q);
-        const d3 w = p - q;
-        const double dd = dot(g.dir, w);
-        if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
-            B.mode = PB_FALLBACK;  // clipped: the FP64 kernel reports it
-            return true;
-        }
-        if (g.S.n > 0) {
+            ended = 1;
+        } else {
+            ++g.it;
+            d3 p, q;
+            pair_supports<double, RefineSupportT<MESH>>(s, a, b, g.dir, p, q);
+            const d3 w = p - q;
+            const double dd = dot(g.dir, w);
             // duality gap: |v| - (|v|^2 - v.w) / |v| <= distance <= |v|
             const double gap = g.vl + dd;
-            if (gap <= kMixedRelGap * g.vl || gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl) {
+            if (dd < 0.0 && dd * dd > g.vl * opt.max_distance_squared) {
+                ended = 1;  // clipped: the FP64 kernel reports it
+            } else if (g.S.n > 0 && (gap <= kMixedRelGap * g.vl ||
+                                     gap * gap <= kMixedAbsGap2 * maxf2(1.0, dot(w, w)) * g.vl)) {
                 g.dir = -g.dir;
                 g.state = GJK_NO_INTERSECTION;
-                return true;
+                ended = 2;
+            } else {
+                simplex_push(g.S, w, p, q);
             }
         }
-        simplex_push(g.S, w, p, q);
+    }
+    __syncwarp(together);
+    if (ended) {
+        if (ended == 1) B.mode = PB_FALLBACK;
+        return true;
     }
     d3 nv;
     double nl;

@@ -75,6 +75,7 @@ struct Slot {
     std::vector<Piece> pieces;
     int64_t n = 0;
     bool busy = false;
+    Clock::time_point launched_at;
 };
 
 }  // namespace
@@ -92,6 +93,8 @@ struct d3d_server {
     std::unordered_map<int64_t, std::shared_ptr<Request>> requests;
     int64_t next_id = 1;
     int64_t inflight_pairs = 0;
+    int64_t events = 0;  // arrivals and finished batches, counted to wake the worker
+    d3d_server_stats stats = {};
     bool stop = false;
     int error = D3D_SUCCESS;
     char error_msg[256] = {};
@@ -193,6 +196,8 @@ void collect(d3d_server* s, Slot& sl, Clock::time_point now) {
                         static_cast<unsigned char*>(sl.h_out[k]) + p.off * kOutBytes[k], len * kOutBytes[k]);
     }
     std::lock_guard<std::mutex> lock(s->mu);
+    const double batch_s = std::chrono::duration<double>(now - sl.launched_at).count();
+    if (batch_s > s->stats.max_batch_s) s->stats.max_batch_s = batch_s;
     for (const Piece& p : sl.pieces) {
         Request& r = *p.req;
         if (--r.pieces_out == 0) {
@@ -204,6 +209,18 @@ void collect(d3d_server* s, Slot& sl, Clock::time_point now) {
     sl.pieces.clear();
     sl.busy = false;
     s->cv_done.notify_all();
+}
+
+// Host function queued after a batch's copies: wakes the worker, which then
+// finds the slot's event complete.  It runs on a thread of the CUDA runtime
+// and calls no CUDA function.
+void CUDART_CB batch_done(void* arg) {
+    d3d_server* s = static_cast<d3d_server*>(arg);
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        ++s->events;
+    }
+    s->cv_work.notify_one();
 }
 
 // Form and launch a batch on a free slot; false if nothing was pending.
@@ -242,6 +259,7 @@ bool launch(d3d_server* s, Slot& sl) {
     *sl.h_n = n;
     sl.n = n;
     sl.busy = true;
+    sl.launched_at = Clock::now();
     cudaError_t e = cudaMemcpyAsync(sl.i1, sl.h_i1, sizeof(int32_t) * n, cudaMemcpyHostToDevice, sl.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sl.i2, sl.h_i2, sizeof(int32_t) * n, cudaMemcpyHostToDevice, sl.stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sl.n_dev, sl.h_n, sizeof(int64_t), cudaMemcpyHostToDevice, sl.stream);
@@ -262,6 +280,13 @@ bool launch(d3d_server* s, Slot& sl) {
     for (int k = 0; k < kOutputs && e == cudaSuccess && !rc; ++k)
         e = cudaMemcpyAsync(sl.h_out[k], sl.out[k], kOutBytes[k] * n, cudaMemcpyDeviceToHost, sl.stream);
     if (e == cudaSuccess && !rc) e = cudaEventRecord(sl.done, sl.stream);
+    if (e == cudaSuccess && !rc) e = cudaLaunchHostFunc(sl.stream, batch_done, s);
+    {
+        const double enqueue_s = std::chrono::duration<double>(Clock::now() - sl.launched_at).count();
+        std::lock_guard<std::mutex> lock(s->mu);
+        ++s->stats.batches;
+        if (enqueue_s > s->stats.max_enqueue_s) s->stats.max_enqueue_s = enqueue_s;
+    }
     if (e != cudaSuccess || rc) {
         std::lock_guard<std::mutex> lock(s->mu);
         if (rc) {
@@ -275,12 +300,20 @@ bool launch(d3d_server* s, Slot& sl) {
     return true;
 }
 
+// The worker sleeps until a request arrives or a batch finishes (the host
+// function above), rather than polling the slots' events: a polling thread
+// holds a host core for itself, and on a host whose cores are shared or
+// rationed that can cost whole milliseconds of latency when the scheduler
+// takes the core away.
 void worker_main(d3d_server* s) {
     cudaSetDevice(s->device);
+    int64_t seen = 0;
     while (true) {
+        const Clock::time_point pass = Clock::now();
         {
             std::lock_guard<std::mutex> lock(s->mu);
             if (s->stop || s->error) break;
+            seen = s->events;
         }
         bool did = false;
         for (Slot& sl : s->slots) {
@@ -297,13 +330,17 @@ void worker_main(d3d_server* s) {
         }
         for (Slot& sl : s->slots)
             if (!sl.busy && launch(s, sl)) did = true;
+        {
+            const double pass_s = std::chrono::duration<double>(Clock::now() - pass).count();
+            std::lock_guard<std::mutex> lock(s->mu);
+            if (pass_s > s->stats.max_loop_gap_s) s->stats.max_loop_gap_s = pass_s;
+        }
         if (!did) {
-            bool any_busy = false;
-            for (Slot& sl : s->slots) any_busy |= sl.busy;
+            // nothing to collect or launch: wait for the next arrival or finished batch (a bounded
+            // wait, so that a lost wake-up costs at most that long)
             std::unique_lock<std::mutex> lock(s->mu);
-            if (!any_busy && s->pending.empty() && !s->stop)
-                s->cv_work.wait_for(lock, std::chrono::milliseconds(5));
-            // with batches in flight the loop polls their events
+            s->cv_work.wait_for(lock, std::chrono::milliseconds(2),
+                                [&] { return s->stop || s->error || s->events != seen; });
         }
     }
 }
@@ -356,8 +393,9 @@ extern "C" void d3d_server_destroy(d3d_server* s) {
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
+    // the streams' last host functions (batch_done) refer to the server: wait for them too
     for (Slot& sl : s->slots) {
-        if (sl.busy) cudaEventSynchronize(sl.done);
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
         free_slot(sl);
     }
     delete s;
@@ -391,6 +429,7 @@ int submit(d3d_server* s, const int32_t* i1, const int32_t* i2, int64_t n, int64
     }
     s->requests[r->id] = r;
     *id = r->id;
+    ++s->events;
     s->cv_work.notify_one();
     return D3D_SUCCESS;
 }
@@ -448,6 +487,14 @@ extern "C" int d3d_server_result(d3d_server* s, int64_t id, const d3d_pair_resul
     return D3D_SUCCESS;
 }
 
+extern "C" int d3d_server_stats_read(d3d_server* s, d3d_server_stats* out, int reset) {
+    D3D_REQUIRE(s && out, "d3d_server_stats_read: null argument");
+    std::lock_guard<std::mutex> lock(s->mu);
+    *out = s->stats;
+    if (reset) s->stats = d3d_server_stats{};
+    return D3D_SUCCESS;
+}
+
 extern "C" int d3d_server_replay(d3d_server* s, int64_t n_requests, const double* offsets_s, const int64_t* sizes,
                                  const int32_t* i1, const int32_t* i2, double* latency_s, double* wait_s,
                                  double* span_s) {
@@ -458,6 +505,9 @@ extern "C" int d3d_server_replay(d3d_server* s, int64_t n_requests, const double
     int64_t base = 0;
     for (int64_t k = 0; k < n_requests; ++k) {
         const auto at = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(offsets_s[k]));
+        // sleep to just before the arrival, then spin the last stretch for timing accuracy
+        const auto wake = at - std::chrono::microseconds(200);
+        if (Clock::now() < wake) std::this_thread::sleep_until(wake);
         while (Clock::now() < at) {
         }
         int rc = submit(s, i1 + base, i2 + base, sizes[k], &ids[k], false);

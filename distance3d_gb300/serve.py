@@ -353,3 +353,13 @@ class NativeCollisionServer:
                                                ctypes.byref(span)))
         self.last_wait = wait
         return lat, span.value
+
+    def stats(self, reset=True):
+        """The worker's counters since the last reset (d3d_server_stats_read):
+        batches, and the longest batch (launch to results in host memory), the
+        longest enqueue of one batch and the longest pass of the worker loop,
+        in milliseconds."""
+        st = _lib.ServerStats()
+        _lib.check(self._lib.d3d_server_stats_read(self._h, ctypes.byref(st), 1 if reset else 0))
+        return {"batches": st.batches, "max_batch_ms": 1e3 * st.max_batch_s,
+                "max_enqueue_ms": 1e3 * st.max_enqueue_s, "max_loop_pass_ms": 1e3 * st.max_loop_gap_s}

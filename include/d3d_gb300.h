@@ -337,6 +337,19 @@ int d3d_server_result(d3d_server* server, int64_t request_id, const d3d_pair_res
  * last finish; the results are not kept. */
 int d3d_server_replay(d3d_server* server, int64_t n_requests, const double* offsets_s, const int64_t* sizes,
                       const int32_t* i1, const int32_t* i2, double* latency_s, double* wait_s, double* span_s);
+/* Counters of the worker since the last reset (reset != 0 clears them after
+ * reading): batches launched, the longest batch from launch to results in
+ * host memory, the longest time the worker took to enqueue one batch
+ * (copies, graph launch), and the longest pass of the worker loop (a stall
+ * of the host thread).  For telling a slow batch on the device from a
+ * stalled host when a latency outlier appears. */
+typedef struct {
+    int64_t batches;
+    double max_batch_s;
+    double max_enqueue_s;
+    double max_loop_gap_s;
+} d3d_server_stats;
+int d3d_server_stats_read(d3d_server* server, d3d_server_stats* out, int reset);
 
 /* ------------------------------------------------------------------ broad phase
  * A linear BVH over FP64 boxes aabbs[n][3][2] ([axis][min,max]).  The tree

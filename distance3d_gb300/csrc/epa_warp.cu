@@ -404,7 +404,7 @@ __device__ Search search_pair(const Poly<T>& P, const d3d_store& st, int a, int 
         const V3<T> sd = mk(cn.x, cn.y, cn.z);
         const V3<T> w = minkowski_of<MESH>(st, a, b, sd);
         scale = maxf2(scale, sqrt_t(dot(w, w)));
-        const T eps = maxf2((T)o.epsilon, T(8) * eps_of<T>() * scale);
+        const T eps = maxf2((T)o.epsilon, T(kSearchUlps) * eps_of<T>() * scale);
         if (dot(w, sd) - cn.w < eps) {
             R.status = D3D_STATUS_OK;
             return R;

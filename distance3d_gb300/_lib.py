@@ -88,6 +88,9 @@ SIGNATURES = [
     ("d3d_gjk_distance", c_int, [_SP, c_void_p, c_void_p, c_int64, ctypes.POINTER(GjkOptions),
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p]),
+    ("d3d_gjk_distance_cached", c_int, [_SP, c_void_p, c_void_p, c_int64, ctypes.POINTER(GjkOptions),
+                                        c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]),
     ("d3d_gjk_intersection", c_int, [_SP, c_void_p, c_void_p, c_int64, c_double, c_int32, c_void_p,
                                      c_void_p, c_void_p]),
     ("d3d_epa_scratch_bytes", c_size_t, [c_int64, ctypes.POINTER(EpaOptions)]),

@@ -304,16 +304,20 @@ class Cone(ConvexCollider):
 class MeshGraph(ConvexCollider):
     """Convex mesh with hill-climbing support (colliders.py:187-240):
     ``vertices`` (n,3) in the mesh frame, ``triangles`` (m,3) vertex
-    indices.  Every support call climbs from the mesh's start vertex
-    (the smallest index in ``triangles``); the reference starts from its
-    previous answer, which gives the same vertex unless the climb can stop
-    within 10 EPSILON of the maximum."""
+    indices.  ``first_idx`` is the reference's vertex cache
+    (mesh.py:30, 85): the hill climbs of ``gjk.gjk_distance`` on this
+    collider start from it and leave their last answer in it, as the
+    reference's support object does.  ``support_function`` climbs from the
+    mesh's start vertex (the smallest index in ``triangles``) and leaves the
+    cache alone; that gives the same vertex unless the climb can stop within
+    10 EPSILON of the maximum."""
 
     def __init__(self, mesh2origin, vertices, triangles, artist=None):
         super().__init__(artist)
         self.mesh2origin = mesh2origin
         self.vertices = vertices
         self.triangles = triangles
+        self.first_idx = int(np.min(triangles))
 
     def first_vertex(self):
         return self.mesh2origin[:3, 3] + np.dot(self.mesh2origin[:3, :3], self.vertices[0])

@@ -361,12 +361,15 @@ __device__ __noinline__ int mesh_climb_call(const T* __restrict__ verts, const i
 
 // The climb for collider c, inlined (CALL = false) or called.  The links
 // offset and the start vertex are read from the FP64 record (exact integers
-// there; the FP32 record cannot hold large offsets).
+// there; the FP32 record cannot hold large offsets).  `from` >= 0 starts the
+// climb at that vertex instead (the reference's cached answer of its
+// previous call, mesh.py:84-85); out-of-range values start at vertex 0, as
+// mesh_climb_body clamps them.
 template <bool CALL = false, typename T>
-__device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, V3<T> l) {
+__device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, V3<T> l, int from = -1) {
     const double* rec = st.rec64 + (size_t)c.idx * 16;
     const int32_t* blk = st.links + (int64_t)__ldg(rec + 12);
-    const int start = (int)__ldg(rec + 13);
+    const int start = from >= 0 ? from : (int)__ldg(rec + 13);
     if (CALL) return mesh_climb_call(store_verts(st, T(0)), blk, c.off, c.nv, start, l.x, l.y, l.z);
     return mesh_climb_body(store_verts(st, T(0)), blk, c.off, c.nv, start, l.x, l.y, l.z);
 }
@@ -375,10 +378,12 @@ __device__ __forceinline__ int mesh_climb(const Col<T>& c, const d3d_store& st, 
 // geometry.py:314-346, capsule :209-256, cylinder :160-206, ellipsoid
 // :259-284 (norm_vector utils.py:12-30), disk :353-387, ellipse :390-418,
 // cone :421-455; box and hull: first-maximum vertex (colliders.py:131-132);
-// mesh: hill climb from the mesh's start vertex (mesh.py:77-85; each call
-// starts there, where the reference starts from its previous answer).
+// mesh: hill climb (mesh.py:77-85).  Without `cache` each mesh call starts
+// from the mesh's start vertex; with it, the climb starts from *cache (a
+// negative value: the start vertex) and leaves its answer there, the vertex
+// caching of the reference's support object.
 template <typename T>
-__device__ __forceinline__ V3<T> base_support(const Col<T>& c, const d3d_store& st, V3<T> d) {
+__device__ __forceinline__ V3<T> base_support(const Col<T>& c, const d3d_store& st, V3<T> d, int* cache = nullptr) {
     const T* verts = store_verts(st, T(0));
     switch (c.type) {
     case D3D_SPHERE: {
@@ -460,7 +465,8 @@ __device__ __forceinline__ V3<T> base_support(const Col<T>& c, const d3d_store& 
     }
     case D3D_MESH: {
         if (c.nv < 1) return mk(T(NAN), T(NAN), T(NAN));  // rejected by d3d_store_pack
-        const int k = mesh_climb(c, st, rt_mul(c.R, d));
+        const int k = mesh_climb(c, st, rt_mul(c.R, d), cache ? *cache : -1);
+        if (cache) *cache = k;
         return xform(c.R, c.t, load_vertex(verts, c.off + k));
     }
     default:
@@ -480,8 +486,8 @@ __device__ __forceinline__ V3<T> add_margin(const Col<T>& c, V3<T> s, V3<T> d) {
 }
 
 template <typename T>
-__device__ __forceinline__ V3<T> support(const Col<T>& c, const d3d_store& st, V3<T> d) {
-    return add_margin(c, base_support(c, st, d), d);
+__device__ __forceinline__ V3<T> support(const Col<T>& c, const d3d_store& st, V3<T> d, int* cache = nullptr) {
+    return add_margin(c, base_support(c, st, d, cache), d);
 }
 
 }  // namespace d3d

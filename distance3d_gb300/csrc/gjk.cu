@@ -76,6 +76,41 @@ __global__ void __launch_bounds__(BLOCK, f64_min_blocks<BLOCK>()) k_gjk_distance
     }
 }
 
+// The same loop with the reference's MeshGraph vertex caching: the mesh
+// supports of pair k start from mesh_cache[2k] (collider i1[k]) and
+// mesh_cache[2k+1] (collider i2[k]), -1 meaning the mesh's start vertex, and
+// leave there the vertex their last call returned, as the reference's support
+// object keeps it (mesh.py:84-85).  One thread per pair, in input order;
+// entries of non-mesh colliders pass through unchanged.
+__global__ void __launch_bounds__(128) k_gjk_distance_f64_cached(d3d_store s, const int32_t* __restrict__ i1,
+                                                                 const int32_t* __restrict__ i2, int64_t n,
+                                                                 d3d_gjk_options opt, DistanceOut o,
+                                                                 int32_t* __restrict__ mesh_cache) {
+    __shared__ double rows[24 * 128];
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int a = i1[k], b = i2[k];
+    if (!pair_ok(s, a, b)) {
+        store_bad_index(o, k);
+        return;
+    }
+    const JoltEps<double> E = reference_eps<double>();
+    GjkLoop<double, SmemRows<double, 128>> g;
+    g.S.R.base = rows + threadIdx.x;
+    simplex_clear(g.S);
+    const d3 dir = mk(1.0, 0.0, 0.0);
+    gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
+    int cache[2] = {mesh_cache[2 * k], mesh_cache[2 * k + 1]};
+    const double tol_sq = opt.tolerance * opt.tolerance;
+    while (!gjk_step<double>(g, s, a, b, tol_sq, opt.max_distance_squared, opt.max_iterations, E, 0.0, 0.0, cache)) {
+    }
+    GjkResult<double> r;
+    gjk_end(g, opt.sanity_check, E, r);
+    store_result(o, k, r, g.S);
+    mesh_cache[2 * k] = cache[0];
+    mesh_cache[2 * k + 1] = cache[1];
+}
+
 __global__ void __launch_bounds__(128) k_gjk_intersection_f64(d3d_store s, const int32_t* __restrict__ i1,
                                                               const int32_t* __restrict__ i2, int64_t n,
                                                               double tol_sq, int max_iter, int8_t* __restrict__ hit,
@@ -179,6 +214,26 @@ int launch_gjk_f64(const d3d_store& store, const int32_t* i1, const int32_t* i2,
 }
 
 }  // namespace d3d
+
+extern "C" int d3d_gjk_distance_cached(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                                       const d3d_gjk_options* options, int32_t* mesh_cache, double* dist,
+                                       double* cp1, double* cp2, double* simplex, int8_t* n_simplex, int8_t* status,
+                                       int32_t* iterations, void* stream) {
+    int rc = d3d::check_store(store, "d3d_gjk_distance_cached");
+    if (rc) return rc;
+    D3D_REQUIRE(options, "d3d_gjk_distance_cached: null options");
+    D3D_REQUIRE(n >= 0, "d3d_gjk_distance_cached: n < 0");
+    D3D_REQUIRE(options->max_iterations >= 1, "d3d_gjk_distance_cached: max_iterations < 1");
+    D3D_REQUIRE(options->precision == D3D_PRECISION_FP64,
+                "d3d_gjk_distance_cached: the vertex cache is the reference's; only the FP64 form takes it");
+    if (n == 0) return D3D_SUCCESS;
+    D3D_REQUIRE(i1 && i2 && mesh_cache && dist && cp1 && cp2 && simplex && n_simplex && status,
+                "d3d_gjk_distance_cached: null pointer");
+    DistanceOut o{dist, cp1, cp2, simplex, n_simplex, status, iterations};
+    k_gjk_distance_f64_cached<<<d3d::grid_for(n, 128), 128, 0, d3d::as_stream(stream)>>>(*store, i1, i2, n,
+                                                                                          *options, o, mesh_cache);
+    return d3d::check_launch("d3d_gjk_distance_cached");
+}
 
 extern "C" int d3d_gjk_intersection(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
                                     double tolerance, int32_t max_iterations, int8_t* hit, int8_t* status,

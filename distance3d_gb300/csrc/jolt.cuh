@@ -456,6 +456,23 @@ __device__ __forceinline__ void pair_supports(const d3d_store& st, int a, int b,
     }
 }
 
+// The same with the reference's supports and a MeshGraph vertex cache per
+// collider (cache[0] for a, cache[1] for b; see base_support).
+template <typename T>
+__device__ __forceinline__ void pair_supports_cached(const d3d_store& st, int a, int b, V3<T> d, V3<T>& p, V3<T>& q,
+                                                     int* cache) {
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        Col<T> c;
+        load_col(st, k ? b : a, c);
+        const V3<T> x = support(c, st, k ? -d : d, cache + k);
+        if (k)
+            q = x;
+        else
+            p = x;
+    }
+}
+
 template <typename T>
 struct GjkResult {
     T dist;
@@ -497,10 +514,13 @@ __device__ __forceinline__ void gjk_begin(GjkLoop<T, Rows>& g, V3<T> dir, T vl, 
 // support point along -v, |v| - (|v|^2 - v.w) / |v| <= distance <= |v|.  The
 // loop stops once that bracket is within rel_gap |v| (relative) or within
 // sqrt(abs_gap2) max(1, |w|) (absolute, on the scene's scale).  The FP64
-// drop-in is compiled without it.
+// drop-in is compiled without it.  A non-null `mesh_cache` (two ints) takes
+// the reference's supports with MeshGraph vertex caching
+// (pair_supports_cached) instead of Sup.
 template <typename T, typename Sup = ExactSupport, bool GAP = false, typename Rows>
 __device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
-                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0), T abs_gap2 = T(0)) {
+                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0), T abs_gap2 = T(0),
+                                         int* mesh_cache = nullptr) {
     if (g.it >= max_iter) {
         g.status = D3D_STATUS_MAX_ITER;
         g.state = GJK_NO_INTERSECTION;
@@ -509,7 +529,10 @@ __device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& s
     ++g.it;
     const unsigned together = __activemask();
     V3<T> p, q;
-    pair_supports<T, Sup>(st, a, b, g.dir, p, q);
+    if (mesh_cache)
+        pair_supports_cached<T>(st, a, b, g.dir, p, q, mesh_cache);
+    else
+        pair_supports<T, Sup>(st, a, b, g.dir, p, q);
     // The supports branch by collider type and polytope size; without this
     // the lanes would reach the simplex solve in the groups those branches
     // left and run it once per group.

@@ -28,7 +28,7 @@ _PRECISIONS = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}
 
 
 def gjk_distance_batch(store, i1, i2, *, tolerance=1e-10, max_distance_squared=100000.0, sanity_check=1e-8,
-                       max_iterations=DEFAULT_MAX_ITERATIONS, precision="fp64", out=None):
+                       max_iterations=DEFAULT_MAX_ITERATIONS, precision="fp64", out=None, mesh_cache=None):
     """Jolt GJK distance for pairs (i1[k], i2[k]) of ``store``.
 
     Returns a dict of device tensors: ``dist`` (n,) float64, ``cp1``/``cp2``
@@ -37,9 +37,16 @@ def gjk_distance_batch(store, i1, i2, *, tolerance=1e-10, max_distance_squared=1
     ``precision="fp64"`` reproduces the reference bit for bit;
     ``precision="mixed"`` runs the iterations in FP32 and refines in FP64.
     ``out`` may pass preallocated tensors with those keys.
+
+    ``mesh_cache`` (an (n,2) int32 device tensor, updated in place) gives the
+    MeshGraph supports of each pair the reference's vertex caching: the
+    climbs of pair k start from mesh_cache[k] (-1: the mesh's start vertex)
+    and leave their last answers there (d3d_gjk_distance_cached; FP64 only).
     """
     if precision not in _PRECISIONS:
         raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
+    if mesh_cache is not None and precision != "fp64":
+        raise ValueError("mesh_cache is the reference's vertex caching: precision must be 'fp64'")
     dev = store.device
     with torch.cuda.device(dev):
         a = as_index(i1, dev, store.n_colliders)
@@ -57,6 +64,16 @@ def gjk_distance_batch(store, i1, i2, *, tolerance=1e-10, max_distance_squared=1
                        iterations=torch.empty(n, dtype=torch.int32, device=dev))
         opt = _lib.GjkOptions(tolerance, max_distance_squared, sanity_check, int(max_iterations),
                               _PRECISIONS[precision])
+        if mesh_cache is not None:
+            if (not isinstance(mesh_cache, torch.Tensor) or mesh_cache.device != torch.device(dev)
+                    or mesh_cache.dtype != torch.int32 or tuple(mesh_cache.shape) != (n, 2)
+                    or not mesh_cache.is_contiguous()):
+                raise ValueError("mesh_cache must be a contiguous (n, 2) int32 tensor on the store's device")
+            _lib.check(_lib.load().d3d_gjk_distance_cached(
+                store.view, _ptr(a), _ptr(b), n, ctypes.byref(opt), _ptr(mesh_cache), _ptr(out["dist"]),
+                _ptr(out["cp1"]), _ptr(out["cp2"]), _ptr(out["simplex"]), _ptr(out["n_simplex"]),
+                _ptr(out["status"]), _ptr(out.get("iterations")), store.stream()))
+            return out
         _lib.check(_lib.load().d3d_gjk_distance(
             store.view, _ptr(a), _ptr(b), n, ctypes.byref(opt), _ptr(out["dist"]), _ptr(out["cp1"]),
             _ptr(out["cp2"]), _ptr(out["simplex"]), _ptr(out["n_simplex"]), _ptr(out["status"]),
@@ -83,6 +100,18 @@ def _pair_store(collider1, collider2):
     return ColliderStore(ColliderSet.from_colliders([collider1, collider2]))
 
 
+def _mesh_cache_holder(c):
+    """The object that holds a MeshGraph collider's vertex cache (``first_idx``):
+    this package's MeshGraph, or the support object of distance3d's own
+    (mesh.py:30, 85), also inside a Margin; None for other colliders."""
+    if type(c).__name__ == "Margin":
+        c = getattr(c, "collider", None)
+    if c is None or type(c).__name__ != "MeshGraph":
+        return None
+    sf = getattr(c, "_support_function", None)
+    return sf if sf is not None and hasattr(sf, "first_idx") else c
+
+
 def gjk_distance_jolt(collider1, collider2, tolerance=1e-10, max_distance_squared=100000.0, sanity_check=1e-8):
     """Drop-in for distance3d.gjk.gjk_distance_jolt (_gjk_jolt.py:138-221).
 
@@ -93,9 +122,18 @@ def gjk_distance_jolt(collider1, collider2, tolerance=1e-10, max_distance_square
     rows, and rows GJK never wrote are zero.
     """
     store = _pair_store(collider1, collider2)
+    holders = [_mesh_cache_holder(collider1), _mesh_cache_holder(collider2)]
+    cache = None
+    if any(x is not None for x in holders):
+        cache = torch.tensor([[int(x.first_idx) if x is not None else -1 for x in holders]], dtype=torch.int32,
+                             device=store.device)
     r = gjk_distance_batch(store, [0], [1], tolerance=tolerance, max_distance_squared=max_distance_squared,
-                           sanity_check=sanity_check)
+                           sanity_check=sanity_check, mesh_cache=cache)
     h = {k: v.cpu().numpy() for k, v in r.items()}
+    if cache is not None:
+        for x, v in zip(holders, cache.cpu().numpy()[0]):
+            if x is not None:
+                x.first_idx = int(v)
     status = int(h["status"][0])
     if status == _lib.STATUS_CLIPPED:
         return MAX_FLOAT, None, None, None

@@ -175,6 +175,28 @@ int d3d_gjk_distance(const d3d_store* store, const int32_t* i1, const int32_t* i
                      double* simplex, int8_t* n_simplex, int8_t* status, int32_t* iterations,
                      void* stream);
 
+/* The plain FP64 GJK distance with the reference's MeshGraph vertex caching.
+ * The reference's MeshGraph support object starts each hill climb from the
+ * vertex its previous call returned and keeps the new answer
+ * (MeshHillClimbingSupportFunction.__call__, mesh.py:64-87; the cache starts
+ * at the smallest vertex index of the triangles, mesh.py:30), so its results
+ * depend on the calls made on that object before.  Here pair k's mesh
+ * supports start from mesh_cache[k][0] (collider i1[k]) and mesh_cache[k][1]
+ * (collider i2[k]), -1 meaning the mesh's start vertex, chain through the
+ * pair's support calls in the reference's order, and leave the last answer
+ * in mesh_cache (device int32[n][2], in/out; entries of other colliders
+ * pass through).  Passing the cache states the reference's objects hold
+ * before a call reproduces that call bit for bit; pairs of one batch run
+ * independently, so a collider used by several pairs carries its state from
+ * one to the next only across calls.  One thread per pair, input order
+ * (no scheduling).  options->precision must be D3D_PRECISION_FP64.  Outputs
+ * as d3d_gjk_distance.  Replaces gjk_distance_jolt on MeshGraph colliders
+ * (gjk/_gjk_jolt.py:138-221 with colliders.py:187-240). */
+int d3d_gjk_distance_cached(const d3d_store* store, const int32_t* i1, const int32_t* i2, int64_t n,
+                            const d3d_gjk_options* options, int32_t* mesh_cache, double* dist, double* cp1,
+                            double* cp2, double* simplex, int8_t* n_simplex, int8_t* status, int32_t* iterations,
+                            void* stream);
+
 /* Batched Jolt GJK intersection test: hit[k] = 1 if the pair intersects.
  * Replaces gjk.gjk_intersection / gjk_intersection_jolt, _gjk_jolt.py:29-135
  * (alias gjk/__init__.py:28). */

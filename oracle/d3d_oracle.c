@@ -97,6 +97,8 @@ typedef struct {
     int nverts;
     const int32_t* links; /* mesh: links block (shortcuts, offsets, neighbour lists) */
     int start;            /* mesh: start vertex of the hill climb */
+    int* cache;           /* mesh: the support object's vertex cache (mesh.py:30, 85), or NULL
+                             to start every climb at `start` */
     double box[8 * 4];   /* box vertices, geometry.py:138-157 */
 } collider;
 
@@ -154,6 +156,7 @@ static void load_collider(collider* c, int idx, const int32_t* types, const doub
     }
     c->links = NULL;
     c->start = 0;
+    c->cache = NULL;
     if (c->type == T_MESH) {
         c->links = links + (int64_t)c->p[0];
         c->start = (int)c->p[1];
@@ -254,11 +257,12 @@ static v3 base_support(const collider* c, v3 d) {
     }
     case T_MESH: {
         /* mesh.py:77-85, 88-127: direction into the mesh frame, hill climb
-         * from the start vertex (each call starts there), posed vertex */
+         * from the cached vertex (mesh.py:82-85; without a cache each call
+         * starts at the start vertex), posed vertex */
         v3 l = rt_mul(c->R, d);
         const int32_t* blk = c->links;
         const double eps = 10.0 * EPS;  /* PROJECTION_LENGTH_EPSILON */
-        int best = c->start;
+        int best = (c->cache && *c->cache >= 0 && *c->cache < c->nverts) ? *c->cache : c->start;
         for (int k = 0; k < 6; ++k) {
             int cand = blk[k];
             const double* a = c->verts + (int64_t)cand * 4;
@@ -276,6 +280,7 @@ static v3 base_support(const collider* c, v3 d) {
                 if (dot(l, mk(a[0] - b[0], a[1] - b[1], a[2] - b[2])) > eps) { best = cand; converged = 0; }
             }
         }
+        if (c->cache) *c->cache = best;  /* vertex caching, mesh.py:85 */
         const double* v = c->verts + (int64_t)best * 4;
         return xform(c->R, c->t, mk(v[0], v[1], v[2]));
     }
@@ -1114,6 +1119,39 @@ void orc_gjk_distance(SET_ARGS, const int32_t* i1, const int32_t* i2, int64_t n,
         collider a, b;
         load_collider(&a, i1[k], SET_PASS);
         load_collider(&b, i2[k], SET_PASS);
+        gjk_result r;
+        gjk_distance(&a, &b, tol, max_d2, sanity, max_iter, &r);
+        dist[k] = r.dist;
+        cp1[3 * k] = r.cp1.x; cp1[3 * k + 1] = r.cp1.y; cp1[3 * k + 2] = r.cp1.z;
+        cp2[3 * k] = r.cp2.x; cp2[3 * k + 1] = r.cp2.y; cp2[3 * k + 2] = r.cp2.z;
+        for (int j = 0; j < 4; ++j) {
+            simplex[12 * k + 3 * j] = r.Y[j].x;
+            simplex[12 * k + 3 * j + 1] = r.Y[j].y;
+            simplex[12 * k + 3 * j + 2] = r.Y[j].z;
+        }
+        n_simplex[k] = (int8_t)r.n;
+        status[k] = (int8_t)r.status;
+        if (iters) iters[k] = r.iters;
+    }
+}
+
+/* orc_gjk_distance with the MeshGraph vertex cache: pair k's mesh supports
+ * start their climbs at cache[2k] (collider i1[k]) and cache[2k+1] (i2[k]),
+ * -1 meaning the mesh's start vertex, and leave their last answer there --
+ * one support object per pair side, as a reference MeshGraph object carries
+ * its first_idx from call to call (mesh.py:30, 82-85). */
+void orc_gjk_distance_cached(SET_ARGS, const int32_t* i1, const int32_t* i2, int64_t n,
+                             double tol, double max_d2, double sanity, int max_iter, int32_t* cache,
+                             double* dist, double* cp1, double* cp2, double* simplex,
+                             int8_t* n_simplex, int8_t* status, int32_t* iters, int nthreads) {
+    set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t k = 0; k < n; ++k) {
+        collider a, b;
+        load_collider(&a, i1[k], SET_PASS);
+        load_collider(&b, i2[k], SET_PASS);
+        a.cache = cache + 2 * k;
+        b.cache = cache + 2 * k + 1;
         gjk_result r;
         gjk_distance(&a, &b, tol, max_d2, sanity, max_iter, &r);
         dist[k] = r.dist;

@@ -28,6 +28,9 @@ def lib():
         _lib.orc_gjk_distance.argtypes = _set_args + [
             I32P, I32P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
             ctypes.c_int, DP, DP, DP, DP, I8P, I8P, I32P, ctypes.c_int]
+        _lib.orc_gjk_distance_cached.argtypes = _set_args + [
+            I32P, I32P, ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+            ctypes.c_int, I32P, DP, DP, DP, DP, I8P, I8P, I32P, ctypes.c_int]
         _lib.orc_gjk_intersection.argtypes = _set_args + [
             I32P, I32P, ctypes.c_int64, ctypes.c_double, ctypes.c_int, I8P, I8P, I32P, ctypes.c_int]
         _lib.orc_epa.argtypes = _set_args + [
@@ -80,6 +83,26 @@ def gjk_distance(cs, i1, i2, tolerance=1e-10, max_distance_squared=100000.0,
                            _p(out["dist"], DP), _p(out["cp1"], DP), _p(out["cp2"], DP),
                            _p(out["simplex"], DP), _p(out["n_simplex"], I8P),
                            _p(out["status"], I8P), _p(out["iterations"], I32P), nthreads)
+    return out
+
+
+def gjk_distance_cached(cs, i1, i2, mesh_cache, tolerance=1e-10, max_distance_squared=100000.0,
+                        sanity_check=1e-8, max_iter=1024, nthreads=0):
+    """gjk_distance with the MeshGraph vertex cache (mesh.py:30, 82-85):
+    ``mesh_cache`` (n,2) int32, -1 for the start vertex, is updated in place."""
+    i1, i2 = _idx(i1), _idx(i2)
+    n = len(i1)
+    if (not isinstance(mesh_cache, np.ndarray) or mesh_cache.dtype != np.int32
+            or mesh_cache.shape != (n, 2) or not mesh_cache.flags.c_contiguous):
+        raise ValueError("mesh_cache must be a C-contiguous (n, 2) int32 array")
+    out = dict(dist=np.empty(n), cp1=np.empty((n, 3)), cp2=np.empty((n, 3)),
+               simplex=np.empty((n, 4, 3)), n_simplex=np.empty(n, np.int8),
+               status=np.empty(n, np.int8), iterations=np.empty(n, np.int32))
+    lib().orc_gjk_distance_cached(*_set(cs), _p(i1, I32P), _p(i2, I32P), n, tolerance,
+                                  max_distance_squared, sanity_check, max_iter, _p(mesh_cache, I32P),
+                                  _p(out["dist"], DP), _p(out["cp1"], DP), _p(out["cp2"], DP),
+                                  _p(out["simplex"], DP), _p(out["n_simplex"], I8P),
+                                  _p(out["status"], I8P), _p(out["iterations"], I32P), nthreads)
     return out
 
 

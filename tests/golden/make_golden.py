@@ -3,7 +3,7 @@
 Run from the repository root, in a container where the reference source tree
 is available (it is NOT needed at test time):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/distance3d [mixed6 scb all9 tree]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/distance3d [mixed6 scb all9 mesh10 edge tree mesh_cached]
 
 (no names: every fixture).
 The reference is imported with its JIT disabled -- the mode its own CI uses --
@@ -46,6 +46,14 @@ Inputs come from ``distance3d_gb300.workloads`` (seeded).  Outputs:
   GJK, EPA and MPR on every pair of the colliders whose supports are finite.
   Calls on which the reference raises its sanity assertion are recorded as
   such (status 2).
+* ``gjk_mesh_cached.npz`` -- the stock reference MeshGraph with its vertex
+  caching: 600 pairs over 21 shared colliders (axis-aligned and rotated
+  cube MeshGraphs, whose tied vertices make the answer depend on the start
+  vertex, random hull MeshGraphs, a MeshGraph in a Margin, spheres, boxes)
+  run through the stock ``gjk_distance_jolt`` in a fixed order; per pair
+  the two sides' caches (``first_idx``, -1 for no MeshGraph) before and
+  after the call, and the outputs.  Also the triangles, for rebuilding the
+  colliders.
 * ``aabb_tree.npz``   -- a 400-collider scene: reference AabbTree self overlap
   (both orders, i == j dropped, reduced to i < j), brute force
   ``all_aabbs_overlap``, BoundingVolumeHierarchy.aabb_overlapping_with_self on
@@ -540,6 +548,117 @@ def make_edge(mods, workloads):
     np.savez_compressed(os.path.join(HERE, "edge.npz"), **gf)
 
 
+def mesh_cached_colliders(colliders, seed=77):
+    """Stock reference colliders for the vertex-cache fixture: axis-aligned
+    cube MeshGraphs (GJK's first search direction, +x, and many later ones
+    tie four cube vertices within 10 EPSILON, so the vertex a climb returns
+    depends on where it starts), rotated cubes, random hull MeshGraphs, a
+    MeshGraph in a Margin, and spheres and boxes as partners.  Returns the
+    objects and each one's triangles (None for other types)."""
+    from scipy.spatial import ConvexHull
+    C = colliders
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cube_v = np.array([[x, y, z] for x in (-0.5, 0.5) for y in (-0.5, 0.5) for z in (-0.5, 0.5)])
+    cube_t = ConvexHull(cube_v).simplices
+
+    def pose(rotate=False):
+        m = np.eye(4)
+        if rotate:
+            q = rng.standard_normal(4)
+            q /= np.linalg.norm(q)
+            w, x, y, z = q
+            m[:3, :3] = [[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                         [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                         [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]]
+        m[:3, 3] = np.round(rng.uniform(-0.6, 0.6, 3), 2)
+        return m
+    cols, tris = [], []
+    for k in range(8):
+        s = np.round(rng.uniform(0.3, 0.7), 2)
+        cols.append(C.MeshGraph(pose(rotate=k >= 6), cube_v * s, cube_t))
+        tris.append(cube_t)
+    for k in range(6):
+        u = rng.standard_normal((int(rng.integers(8, 40)), 3))
+        v = u / np.linalg.norm(u, axis=1, keepdims=True) * rng.uniform(0.15, 0.4)
+        t = ConvexHull(v).simplices
+        cols.append(C.MeshGraph(pose(rotate=True), v, t))
+        tris.append(t)
+    cols.append(C.Margin(C.MeshGraph(pose(), cube_v * 0.4, cube_t), 0.05))
+    tris.append(cube_t)
+    for k in range(3):
+        cols.append(C.Sphere(np.round(rng.uniform(-0.6, 0.6, 3), 2), float(np.round(rng.uniform(0.1, 0.4), 2))))
+        tris.append(None)
+        cols.append(C.Box(pose(), np.round(rng.uniform(0.2, 0.8, 3), 2)))
+        tris.append(None)
+    return cols, tris
+
+
+def make_mesh_cached(mods, workloads, n=600, seed=78):
+    """The stock reference MeshGraph's vertex caching (mesh.py:30, 82-85):
+    every collider object is shared by all the pairs that name it, and the
+    pairs run through the stock gjk_distance_jolt one after another in this
+    fixed order, so each climb starts where the object's previous climb
+    stopped.  Records per pair the caches of both sides before and after the
+    call (-1 for colliders without one) and the outputs."""
+    from distance3d_gb300.collider_set import ColliderSet
+    gjk, _, colliders, _, _ = mods
+    print("MeshGraph vertex cache (stock objects, fixed call order)")
+    cols, tris = mesh_cached_colliders(colliders)
+    cs = ColliderSet.from_colliders(cols)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    i1 = rng.integers(0, len(cols), n).astype(np.int32)
+    i2 = ((i1 + rng.integers(1, len(cols), n)) % len(cols)).astype(np.int32)
+
+    def holder(c):
+        inner = c.collider if type(c).__name__ == "Margin" else c
+        return inner._support_function if type(inner).__name__ == "MeshGraph" else None
+
+    def caches(c1, c2):
+        return [int(h.first_idx) if h is not None else -1 for h in (holder(c1), holder(c2))]
+    before = np.empty((n, 2), np.int32)
+    after = np.empty((n, 2), np.int32)
+    dist = np.empty(n)
+    cp1 = np.full((n, 3), np.nan)
+    cp2 = np.full((n, 3), np.nan)
+    simplex = np.full((n, 4, 3), np.nan)
+    n_simplex = np.empty(n, np.int8)
+    iters = np.empty(n, np.int32)
+    sanity = np.zeros(n, bool)
+    for k in range(n):
+        c1, c2 = cols[i1[k]], cols[i2[k]]
+        before[k] = caches(c1, c2)
+        d, a, b, Y, m, it = ref_distance(gjk, c1, c2)
+        after[k] = caches(c1, c2)
+        # the stock call from the same caches: same outputs, same caches after
+        for h, v in zip((holder(c1), holder(c2)), before[k]):
+            if h is not None:
+                h.first_idx = int(v)
+        try:
+            d0, a0, b0, Y0 = gjk.gjk_distance_jolt(c1, c2)
+            assert d == d0
+            if a is not None:
+                assert np.array_equal(a, a0) and np.array_equal(b, b0) and np.array_equal(Y[:m], Y0[:m])
+        except AssertionError:
+            sanity[k] = True  # the reference's sanity check (_gjk_jolt.py:215-216) or a mismatch
+        assert caches(c1, c2) == list(after[k])
+        dist[k], simplex[k], n_simplex[k], iters[k] = d, Y, m, it
+        if a is not None:
+            cp1[k], cp2[k] = a, b
+    moved = np.sum(np.any(before != after, axis=1))
+    print(f"  {n} pairs over {len(cols)} colliders: {moved} calls moved a cache, {sanity.sum()} sanity assertions, "
+          f"{np.sum(dist == 0.0)} intersecting")
+    assert not sanity.any()
+    tri_ptr = np.zeros(len(cols) + 1, np.int64)
+    for j, t in enumerate(tris):
+        tri_ptr[j + 1] = tri_ptr[j] + (0 if t is None else len(t))
+    tri_all = np.concatenate([t for t in tris if t is not None]).astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, "gjk_mesh_cached.npz"), types=cs.types, poses=cs.poses, params=cs.params,
+                        hull_offset=cs.hull_offset, hull_count=cs.hull_count, vertices=cs.vertices[:, :3].copy(),
+                        links=cs.links, triangles=tri_all, triangle_ptr=tri_ptr, i1=i1, i2=i2,
+                        cache_before=before, cache_after=after, dist=dist, cp1=cp1, cp2=cp2, simplex=simplex,
+                        n_simplex=n_simplex, iterations=iters)
+
+
 def make_tree(mods, workloads):
     print("aabb tree scene")
     scene = workloads.scene_mixed_six(400, seed=4321, half_width=3.0)
@@ -547,7 +666,7 @@ def make_tree(mods, workloads):
 
 
 FIXTURES = {"mixed6": make_mixed6, "scb": make_scb, "all9": make_all9, "mesh10": make_mesh, "edge": make_edge,
-            "tree": make_tree}
+            "tree": make_tree, "mesh_cached": make_mesh_cached}
 
 
 def main(ref_root, names):

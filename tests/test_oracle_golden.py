@@ -171,3 +171,53 @@ def test_edge_colliders_bit_exact(golden):
         st = g[f"epa_status_{tag}"]
         assert np.array_equal(e["status"], st)
         assert np.array_equal(e["mtv"][st == 0], g[f"epa_mtv_{tag}"][st == 0])
+
+
+def test_mesh_cache_bit_exact(golden):
+    """The stock reference MeshGraph's vertex caching (mesh.py:30, 82-85):
+    each pair's climbs start from the caches the previous calls left, and
+    the oracle, given those caches, reproduces the outputs and the caches
+    after the call."""
+    g, cs = golden("gjk_mesh_cached")
+    cache = g["cache_before"].copy()
+    r = oracle.gjk_distance_cached(cs, g["i1"], g["i2"], cache)
+    assert np.array_equal(cache, g["cache_after"])
+    assert np.array_equal(r["dist"], g["dist"])
+    assert np.array_equal(r["n_simplex"], g["n_simplex"])
+    assert np.array_equal(r["iterations"], g["iterations"])
+    assert np.array_equal(r["cp1"], g["cp1"], equal_nan=True)
+    assert np.array_equal(r["cp2"], g["cp2"], equal_nan=True)
+    written = ~np.isnan(g["simplex"])
+    assert np.array_equal(r["simplex"][written], g["simplex"][written])
+
+
+def test_mesh_cache_chained(golden):
+    """One cache per collider object carried from call to call in the
+    fixture's order, one pair per call: the caches each call sees and leaves
+    are the recorded ones."""
+    g, cs = golden("gjk_mesh_cached")
+    state = {}
+    for k in range(len(g["i1"])):
+        for side, idx in enumerate((g["i1"][k], g["i2"][k])):
+            state.setdefault(int(idx), int(g["cache_before"][k, side]))
+    for k in range(len(g["i1"])):
+        a, b = int(g["i1"][k]), int(g["i2"][k])
+        cache = np.array([[state[a], state[b]]], np.int32)
+        assert np.array_equal(cache[0], g["cache_before"][k])
+        r = oracle.gjk_distance_cached(cs, g["i1"][k:k + 1], g["i2"][k:k + 1], cache)
+        assert r["dist"][0] == g["dist"][k]
+        assert np.array_equal(cache[0], g["cache_after"][k])
+        state[a], state[b] = int(cache[0, 0]), int(cache[0, 1])
+
+
+def test_mesh_cache_changes_answers(golden):
+    """The fixture exercises the cache: climbs from the start vertex stop at
+    other tied vertices on many pairs (same distance to rounding, other
+    closest points)."""
+    g, cs = golden("gjk_mesh_cached")
+    r = oracle.gjk_distance(cs, g["i1"], g["i2"])
+    written = ~np.isnan(g["cp1"][:, 0])
+    differ = written & np.any(r["cp1"] != g["cp1"], axis=1)
+    assert differ.sum() > 50
+    np.testing.assert_allclose(r["dist"], g["dist"], rtol=0, atol=1e-12)
+    assert np.any(g["cache_before"] != g["cache_after"])

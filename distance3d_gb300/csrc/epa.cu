@@ -287,7 +287,7 @@ __device__ __forceinline__ int lane_of() { return threadIdx.x & 31; }
 __host__ __device__ inline int pm_words(int nvc) { return (nvc + 31) / 32; }
 __host__ __device__ inline int exact_warp_bytes(int cap_f, int cap_e, int nvc) {
     const int e = cap_e > 0 ? cap_e : 1;
-    return (104 * cap_f + 48 * e + 24 * nvc + 4 * nvc * pm_words(nvc) + 4 * cap_f + 2 * e + cap_f + 15) & ~15;
+    return (32 * cap_f + 24 * nvc + 4 * nvc * pm_words(nvc) + 4 * cap_f + 2 * e + cap_f + 15) & ~15;
 }
 __host__ __device__ inline int exact_warp_bytes(const d3d_epa_options& o) {
     return exact_warp_bytes(o.max_faces, o.max_loose_edges, o.max_iterations + 4);
@@ -295,29 +295,31 @@ __host__ __device__ inline int exact_warp_bytes(const d3d_epa_options& o) {
 
 // One warp's polytope in shared memory.  Every point of the polytope is one
 // of its vertices: the simplex's four points and one support point per
-// iteration (at most nvc = max_iterations + 4), and faces and loose edges
-// hold bit-exact copies of them.  Vertex ids ride along with the copies, and
-// pm holds the reference's closeness test between two points
-// (norm(x - y) < epsilon, epa.py:189-191) for every pair of vertices, so
-// that matching loose edges needs no arithmetic.
+// iteration (at most nvc = max_iterations + 4).  A face is the ids of its
+// three corners in V and its unit normal; a loose edge the ids of its ends.
+// The reference's faces and loose edges hold copies of the corner points
+// (epa.py:86, 131-133, 169, 196); the ids name exactly those points, so every
+// product below reads the same doubles.  pm holds the reference's closeness
+// test between two points (norm(x - y) < epsilon, epa.py:189-191) for every
+// pair of vertices, so that matching loose edges needs no arithmetic.  (Ids
+// instead of copies: about a third of the shared memory per polytope, so
+// about three times the warps per SM on the FP64 pipe.)
 struct WarpPoly {
-    double* F;              // faces: v0, v1, v2, n (12 doubles)
+    double* N;              // faces' unit normals (3 doubles)
     unsigned long long* K;  // ordering key of each face's distance
-    double* E;              // loose edges: a, b (6 doubles)
     double* V;              // vertices (3 doubles)
     unsigned* pm;           // bit y of row x (words x * W ...): vertices x and y are close
-    unsigned* fid;          // vertex ids of each face's corners, 8 bits each
-    unsigned short* eid;    // vertex ids of each loose edge's ends, 8 bits each
+    unsigned* fid;          // vertex ids of each face's corners v0, v1, v2, 8 bits each
+    unsigned short* eid;    // vertex ids of each loose edge's ends (a | b << 8)
     unsigned char* vis;     // visibility flags of the faces
     int W;                  // words per row of pm
 
     __device__ static WarpPoly at(unsigned char* base, int cap_f, int cap_e, int nvc) {
         const int e = cap_e > 0 ? cap_e : 1;
         WarpPoly P;
-        P.F = reinterpret_cast<double*>(base);
-        P.K = reinterpret_cast<unsigned long long*>(P.F + 12 * (int64_t)cap_f);
-        P.E = reinterpret_cast<double*>(P.K + cap_f);
-        P.V = P.E + 6 * (int64_t)e;
+        P.N = reinterpret_cast<double*>(base);
+        P.K = reinterpret_cast<unsigned long long*>(P.N + 3 * (int64_t)cap_f);
+        P.V = reinterpret_cast<double*>(P.K + cap_f);
         P.W = pm_words(nvc);
         P.pm = reinterpret_cast<unsigned*>(P.V + 3 * nvc);
         P.fid = P.pm + nvc * P.W;
@@ -326,6 +328,14 @@ struct WarpPoly {
         return P;
     }
     __device__ bool close(int x, int y) const { return (pm[x * W + (y >> 5)] >> (y & 31)) & 1u; }
+    __device__ d3 vert(int v) const { return ld(V + 3 * v); }
+    __device__ d3 corner(int f, int j) const { return vert((fid[f] >> (8 * j)) & 0xff); }
+    __device__ d3 normal(int f) const { return ld(N + 3 * f); }
+    // epa.py:104-106, np.sum(v0 * n) over the face's row
+    __device__ double dist(int f) const {
+        const d3 v = corner(f, 0), n = normal(f);
+        return (v.x * n.x + v.y * n.y) + v.z * n.z;
+    }
 };
 
 // Ordering key of a face distance: unsigned order equals the order of the
@@ -336,9 +346,6 @@ __device__ __forceinline__ unsigned long long dist_key(double d) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(d);
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
-
-// the face distance of epa.py:104-106, np.sum(v0 * n) over the row
-__device__ __forceinline__ double face_dist(const double* f) { return (f[0] * f[9] + f[1] * f[10]) + f[2] * f[11]; }
 
 // w = s_a(d) - s_b(-d) with the reference's supports: lanes 0-15 evaluate
 // collider a, lanes 16-31 collider b; a box or hull's first-maximum vertex is
@@ -393,16 +400,12 @@ __device__ d3 minkowski_exact_warp(const d3d_store& st, int a, int b, d3 d) {
     return up ? o - s : s - o;
 }
 
-// One pair's EPA by one warp (epa.py:9-78).  F, E, vis: the warp's faces,
-// loose edges and visibility flags in shared memory.  Returns the status;
-// mtv and nf (faces left) as k_epa sets them.
-// The polytope of max_faces faces and max_loose_edges loose edges lives in
-// the warp's shared memory (WarpPoly).
+// One pair's EPA by one warp (epa.py:9-78).  Returns the status; mtv and nf
+// (faces left) as k_epa sets them.  The polytope of max_faces faces and
+// max_loose_edges loose edges lives in the warp's shared memory (WarpPoly).
 __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double* simplex,
                              const d3d_epa_options& o, LengthBounds lb, const WarpPoly& P, d3& mtv, int& nf_out) {
-    double* const F = P.F;
     unsigned long long* const K = P.K;
-    double* const E = P.E;
     unsigned char* const vis = P.vis;
     const int ln = lane_of();
     const double eps = o.epsilon;
@@ -417,10 +420,10 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
     // epa.py:56-57, 89-97: faces ABC, ACD, ADB, BDC
     if (ln < 4) {
         const int init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
-        double* f = F + 12 * ln;
-        for (int j = 0; j < 3; ++j) st(f + 3 * j, ld(P.V + 3 * init[ln][j]));
-        face_normal(f);
-        K[ln] = dist_key(face_dist(f));
+        const d3 v0 = P.vert(init[ln][0]), v1 = P.vert(init[ln][1]), v2 = P.vert(init[ln][2]);
+        const d3 n = norm_vec(cross(v1 - v0, v2 - v0));  // epa.py:99-102
+        st(P.N + 3 * ln, n);
+        K[ln] = dist_key((v0.x * n.x + v0.y * n.y) + v0.z * n.z);
         P.fid[ln] = (unsigned)init[ln][0] | ((unsigned)init[ln][1] << 8) | ((unsigned)init[ln][2] << 16);
     }
     __syncwarp();
@@ -428,9 +431,8 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
     for (int it = 0;; ++it) {
         if (it >= o.max_iterations) {
             // epa.py:77: closest_face is a view, read after the last iteration's edits
-            const double* f = F + 12 * closest;
-            const d3 n = ld(f + 9);
-            mtv = n * dot(ld(f), n);
+            const d3 n = P.normal(closest);
+            mtv = n * dot(P.corner(closest, 0), n);
             nf_out = nf;
             return D3D_STATUS_EPA_NOT_CONVERGED;
         }
@@ -460,9 +462,8 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             }
         }
         closest = (K[0] == ~0ull || bk == ~0ull) ? 0 : bi;
-        const double* cf = F + 12 * closest;
-        const double md = face_dist(cf);
-        const d3 sd = ld(cf + 9);
+        const double md = P.dist(closest);
+        const d3 sd = P.normal(closest);
         const d3 w = minkowski_exact_warp(store, a, b, sd);
         const double pd = dot(w, sd);
         if (pd - md < eps) {  // epa.py:67-70
@@ -490,10 +491,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             }
         }
         // epa.py:157-165: visibility of every face (epa.py:122-124)
-        for (int i = ln; i < nf; i += 32) {
-            const double* f = F + 12 * i;
-            vis[i] = dot(ld(f + 9), w - ld(f)) > eps ? 1 : 0;
-        }
+        for (int i = ln; i < nf; i += 32) vis[i] = dot(P.normal(i), w - P.corner(i, 0)) > eps ? 1 : 0;
         __syncwarp();
         // remove visible faces in the reference's order, collecting edges
         int ne = 0, i = 0;
@@ -508,7 +506,6 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 }
             }
             if (p < 0) break;
-            const double* f = F + 12 * p;
             const unsigned fv = P.fid[p];
             // epa.py:167-187: edge j = (v_j, v_j+1) of the face matches loose
             // edge (a, b) when b is close to v_j and a to v_j+1
@@ -531,22 +528,17 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                     }
                 }
                 if (found >= 0) {
-                    if (ln < 6) E[6 * found + ln] = E[6 * (ne - 1) + ln];
                     if (ln == 0) P.eid[found] = P.eid[ne - 1];
                     --ne;
                 } else {
                     if (ne >= o.max_loose_edges) break;  // epa.py:193-198
-                    if (ln < 3) {
-                        E[6 * ne + ln] = f[3 * j + ln];
-                        E[6 * ne + 3 + ln] = f[3 * ((j + 1) % 3) + ln];
-                    }
                     if (ln == 0) P.eid[ne] = (unsigned short)(x0 | (x1 << 8));
                     ++ne;
                 }
                 __syncwarp();
             }
             // epa.py:118-120: the last face moves into slot p, which is tested again
-            if (ln < 12) F[12 * p + ln] = F[12 * (nf - 1) + ln];
+            if (ln < 3) P.N[3 * p + ln] = P.N[3 * (nf - 1) + ln];
             if (ln == 0) {
                 vis[p] = vis[nf - 1];
                 K[p] = K[nf - 1];
@@ -560,25 +552,22 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
         int kept = 0;
         for (int kb = 0; kb < ne; kb += 32) {
             const int k = kb + ln;
-            double nfa[12];
+            d3 v0 = mk(0.0, 0.0, 0.0), nrm = v0;
             bool keep = false;
             unsigned ids = 0;
             if (k < ne) {
-                const double* e = E + 6 * k;
-                for (int q = 0; q < 6; ++q) nfa[q] = e[q];
-                nfa[6] = w.x;
-                nfa[7] = w.y;
-                nfa[8] = w.z;
+                // the face (a, b, w) of loose edge k (epa.py:131-133)
                 const unsigned ev = P.eid[k];
                 ids = (ev & 0xffu) | (ev & 0xff00u) | ((unsigned)wv << 16);
-                face_normal(nfa);
-                const d3 n = ld(nfa + 9);
-                keep = !(dot(n, n) < lb.keep);
+                const d3 e0 = P.vert(ev & 0xffu), e1 = P.vert((ev >> 8) & 0xffu);
+                v0 = e0;
+                nrm = norm_vec(cross(e1 - e0, w - e0));
+                keep = !(dot(nrm, nrm) < lb.keep);
                 // epa.py:139-146: the reference swaps through a NumPy view of
                 // row 0, so the net effect is v0 := v1 (v1 unchanged), n := -n
-                if (keep && dot(ld(nfa), n) + 1e-6 < 0.0) {
-                    st(nfa, ld(nfa + 3));
-                    st(nfa + 9, -n);
+                if (keep && dot(v0, nrm) + 1e-6 < 0.0) {
+                    v0 = e1;
+                    nrm = -nrm;
                     ids = (ids & ~0xffu) | ((ids >> 8) & 0xffu);
                 }
             }
@@ -590,9 +579,8 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             const int limit = om ? __ffs(om) - 1 : 32;  // edges of this chunk written before the overflow
             if (keep && ln < limit) {
                 const int idx = nf + kept + before;
-                double* dst = F + 12 * idx;
-                for (int q = 0; q < 12; ++q) dst[q] = nfa[q];
-                K[idx] = dist_key(face_dist(nfa));
+                st(P.N + 3 * idx, nrm);
+                K[idx] = dist_key((v0.x * nrm.x + v0.y * nrm.y) + v0.z * nrm.z);
                 P.fid[idx] = ids;
             }
             if (om) {
@@ -607,8 +595,9 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
             // loop the slot holds the last loose edge's face if that one was not kept.  An unconverged
             // pair's MTV can read it (closest_face is a view into the faces, epa.py:77).
             if (k == ne - 1 && !keep) {
-                double* dst = F + 12 * (nf + kept + before);
-                for (int q = 0; q < 12; ++q) dst[q] = nfa[q];
+                const int idx = nf + kept + before;
+                st(P.N + 3 * idx, nrm);
+                P.fid[idx] = ids;
             }
             kept += __popc(km);
         }
@@ -653,8 +642,13 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
             n_faces[pid] = stt == D3D_STATUS_EPA_DEGENERATE ? 0 : nf;
         }
         if (faces && stt != D3D_STATUS_EPA_DEGENERATE) {
+            // the reference's rows: v0, v1, v2, n
             double* out = faces + pid * 12 * (int64_t)o.max_faces;
-            for (int j = ln; j < 12 * nf; j += 32) out[j] = P.F[j];
+            for (int f = ln; f < nf; f += 32) {
+#pragma unroll
+                for (int j = 0; j < 3; ++j) st(out + 12 * f + 3 * j, P.corner(f, j));
+                st(out + 12 * f + 9, P.normal(f));
+            }
         }
         __syncwarp();
     }

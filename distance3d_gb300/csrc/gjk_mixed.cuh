@@ -89,11 +89,22 @@ __device__ __forceinline__ V3<T> margin_fast(const d3d_store& st, const Col<T>& 
     return n2 == T(0) ? s : s + d * (record_margin(st, c) * rsqrt_t(n2));
 }
 
+// Corner of a box (the store's 8 vertices in itertools.product order) that
+// maximises V . d: bit 2, 1, 0 of the index set where R^T d is positive along
+// box axis 0, 1, 2.  Where a component is zero the two faces tie and the
+// lower index is the first maximum, as in hull_argmax; near such ties the
+// rounded FP32 products may pick the other corner, a support all the same.
+__device__ __forceinline__ int box_corner(const float* R, f3 d) {
+    const f3 l = rt_mul(R, d);
+    return (l.x > 0.f ? 4 : 0) | (l.y > 0.f ? 2 : 0) | (l.z > 0.f ? 1 : 0);
+}
+
 // FP32 support of the mixed form's search phases.  MESH = false leaves out
 // the MeshGraph branch, for kernels launched on stores without meshes.
 template <bool MESH>
 struct FastSupportT {
     static __device__ __forceinline__ f3 base(const Col<float>& c, const d3d_store& s, f3 d) {
+        if (c.type == D3D_BOX && c.nv == 8) return load_vertex(s.verts32, c.off + box_corner(c.R, d));
         if (c.type == D3D_BOX || c.type == D3D_HULL) {
             if (c.nv < 1) return mk(NAN, NAN, NAN);
             return load_vertex(s.verts32, c.off + hull_argmax(s.verts32, c.off, c.nv, d));
@@ -125,6 +136,13 @@ struct RefineSupportT {
 
     static __device__ __forceinline__ d3 base(const Col<double>& c, const d3d_store& s, d3 d) {
         const f3 df = mk(__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z));
+        if (c.type == D3D_BOX && c.nv == 8) {
+            // the FP32 record's rotation, as FastSupport sees it
+            float Rf[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) Rf[k] = __double2float_rn(c.R[k]);
+            return load_vertex(s.verts64, c.off + box_corner(Rf, df));
+        }
         if (c.type == D3D_BOX || c.type == D3D_HULL) {
             if (c.nv < 1) return mk(double(NAN), double(NAN), double(NAN));
             return load_vertex(s.verts64, c.off + hull_argmax(s.verts32, c.off, c.nv, df));

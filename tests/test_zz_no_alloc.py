@@ -88,7 +88,9 @@ def test_noalloc_matches_epa_and_oracle_on_two_calls_in_a_row(kw):
 
 def test_noalloc_rejects_oversized_polytopes():
     _, st, i1, i2, simplex = intersecting(43, 200)
-    big = _lib.EpaOptions(64, 4096, 4096, 0, 1e-8)
+    # 16,384 faces: beyond a block's shared memory (32 B per face) and, at
+    # 12 * 16384 + 6 * 4096 doubles per pair, room for 9 pairs in the array
+    big = _lib.EpaOptions(64, 4096, 16384, 0, 1e-8)
     a = torch.as_tensor(i1, dtype=torch.int32, device=st.device)
     rc = _lib.load().d3d_epa_noalloc(st.view, _ptr(a), _ptr(a), len(i1), None, ctypes.byref(big), None, None,
                                      None, None, st.stream())

@@ -44,7 +44,7 @@ class MprOptions(ctypes.Structure):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("capacity", ctypes.c_int64), ("slots", ctypes.c_int32), ("use_graphs", ctypes.c_int32),
-                ("hbm_budget", ctypes.c_int64)]
+                ("hbm_budget", ctypes.c_int64), ("worker_priority", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class PairResults(ctypes.Structure):
@@ -54,7 +54,8 @@ class PairResults(ctypes.Structure):
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("batches", ctypes.c_int64), ("max_batch_s", ctypes.c_double), ("max_enqueue_s", ctypes.c_double),
-                ("max_loop_gap_s", ctypes.c_double)]
+                ("max_loop_gap_s", ctypes.c_double), ("worker_realtime", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class Tuning(ctypes.Structure):

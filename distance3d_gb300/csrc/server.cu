@@ -22,6 +22,9 @@
 // as soon as a slot and memory are free, and the batches of different slots
 // overlap on the device.  Latency is measured from a request's arrival
 // (submission) to its last piece being back in host memory.
+#include <pthread.h>
+#include <sched.h>
+
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
@@ -181,6 +184,13 @@ int init_slot(d3d_server* s, Slot& sl) {
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return cuda_fail(s, e, "graph instantiation");
         sl.graphs.emplace_back(c, x);
+        // upload the executable graph and launch it once on an empty batch (the device count is
+        // still 0): the first launch of a graph pays for its upload, which had stalled the first
+        // batches of a new size class by tens of milliseconds
+        e = cudaGraphUpload(x, sl.stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(x, sl.stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sl.stream);
+        if (e != cudaSuccess) return cuda_fail(s, e, "graph upload");
     }
     return D3D_SUCCESS;
 }
@@ -307,6 +317,13 @@ bool launch(d3d_server* s, Slot& sl) {
 // takes the core away.
 void worker_main(d3d_server* s) {
     cudaSetDevice(s->device);
+    if (s->opt.worker_priority > 0) {
+        sched_param sp = {};
+        sp.sched_priority = s->opt.worker_priority;
+        const bool rt = pthread_setschedparam(pthread_self(), SCHED_FIFO, &sp) == 0;
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->stats.worker_realtime = rt ? 1 : 0;
+    }
     int64_t seen = 0;
     while (true) {
         const Clock::time_point pass = Clock::now();
@@ -358,8 +375,10 @@ extern "C" int d3d_server_create(const d3d_store* store, const d3d_gjk_options* 
     if (rc) return rc;
     D3D_REQUIRE(gjk && epa && options && out, "d3d_server_create: null argument");
     D3D_REQUIRE(options->capacity > 0 && options->capacity <= INT32_MAX && options->slots >= 1 &&
-                    options->slots <= 64 && options->hbm_budget >= 0,
-                "d3d_server_create: invalid options (capacity 1..2^31-1, slots 1..64, budget >= 0)");
+                    options->slots <= 64 && options->hbm_budget >= 0 && options->worker_priority >= 0 &&
+                    options->worker_priority <= 99,
+                "d3d_server_create: invalid options (capacity 1..2^31-1, slots 1..64, budget >= 0, "
+                "worker_priority 0..99)");
     D3D_REQUIRE(d3d_collide_scratch_bytes(options->capacity, gjk, epa) > 0, "d3d_server_create: invalid options");
     auto* s = new d3d_server();
     s->store = *store;
@@ -491,7 +510,11 @@ extern "C" int d3d_server_stats_read(d3d_server* s, d3d_server_stats* out, int r
     D3D_REQUIRE(s && out, "d3d_server_stats_read: null argument");
     std::lock_guard<std::mutex> lock(s->mu);
     *out = s->stats;
-    if (reset) s->stats = d3d_server_stats{};
+    if (reset) {
+        const int32_t rt = s->stats.worker_realtime;
+        s->stats = d3d_server_stats{};
+        s->stats.worker_realtime = rt;
+    }
     return D3D_SUCCESS;
 }
 

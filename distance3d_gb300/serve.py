@@ -285,10 +285,13 @@ class NativeCollisionServer:
     copies a request's host pairs and returns its id; ``result`` waits for it
     and returns host arrays plus its latency; ``replay`` submits a whole
     arrival trace from the library (so the arrival times are kept to the
-    microsecond) and returns the per-request latencies."""
+    microsecond) and returns the per-request latencies.  ``worker_priority``
+    > 0 asks for the worker thread under SCHED_FIFO at that priority (kept at
+    the default policy where the process may not raise it; ``stats()`` says
+    which)."""
 
     def __init__(self, store, *, capacity=65536, slots=2, precision="mixed", epa_kw=None, gjk_kw=None, graphs=True,
-                 hbm_budget=0):
+                 hbm_budget=0, worker_priority=0):
         if precision not in _PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(_PRECISIONS)}")
         ek = dict(max_iter=64, max_loose_edges=32, max_faces=64, epsilon=1e-8)
@@ -301,7 +304,8 @@ class NativeCollisionServer:
                                     _PRECISIONS[precision], float(ek["epsilon"]))
         self.store = store  # the server reads the store's device buffers
         self._lib = _lib.load()
-        opt = _lib.ServerOptions(int(capacity), int(slots), 1 if graphs else 0, int(hbm_budget))
+        opt = _lib.ServerOptions(int(capacity), int(slots), 1 if graphs else 0, int(hbm_budget),
+                                 int(worker_priority), 0)
         handle = ctypes.c_void_p()
         with torch.cuda.device(store.device):
             torch.cuda.synchronize(store.device)
@@ -362,4 +366,5 @@ class NativeCollisionServer:
         st = _lib.ServerStats()
         _lib.check(self._lib.d3d_server_stats_read(self._h, ctypes.byref(st), 1 if reset else 0))
         return {"batches": st.batches, "max_batch_ms": 1e3 * st.max_batch_s,
-                "max_enqueue_ms": 1e3 * st.max_enqueue_s, "max_loop_pass_ms": 1e3 * st.max_loop_gap_s}
+                "max_enqueue_ms": 1e3 * st.max_enqueue_s, "max_loop_pass_ms": 1e3 * st.max_loop_gap_s,
+                "worker_realtime": bool(st.worker_realtime)}

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define D3D_ABI_VERSION 2
+#define D3D_ABI_VERSION 3
 
 /* return codes */
 #define D3D_SUCCESS 0
@@ -325,13 +325,20 @@ int d3d_autotune(const d3d_store* store, const int32_t* i1, const int32_t* i2, i
  * requests are split over batches.  `use_graphs` replays one CUDA graph per
  * capacity class.  Results per pair are d3d_collide's; latency runs from
  * submission to the request's results being in host memory.  The store must
- * outlive the server. */
+ * outlive the server.  `worker_priority` > 0 asks for the worker thread to
+ * run under SCHED_FIFO at that priority (1-99), so that other threads on a
+ * busy host do not delay its launches and completions; the worker sleeps
+ * between passes and never spins.  Where the process may not raise a
+ * thread's priority the worker keeps the default policy
+ * (d3d_server_stats.worker_realtime says which); 0 leaves it unchanged. */
 typedef struct d3d_server d3d_server;
 typedef struct {
     int64_t capacity;
     int32_t slots;
     int32_t use_graphs;
     int64_t hbm_budget;
+    int32_t worker_priority;
+    int32_t reserved; /* 0 */
 } d3d_server_options;
 /* host output arrays of one request (n pairs), any may be NULL */
 typedef struct {
@@ -370,6 +377,8 @@ typedef struct {
     double max_batch_s;
     double max_enqueue_s;
     double max_loop_gap_s;
+    int32_t worker_realtime; /* 1 if the worker runs under SCHED_FIFO (not reset) */
+    int32_t reserved;
 } d3d_server_stats;
 int d3d_server_stats_read(d3d_server* server, d3d_server_stats* out, int reset);
 

@@ -46,7 +46,7 @@ def test_binding_covers_header():
 
 
 def test_abi_version(lib):
-    assert lib.d3d_abi_version() == 2
+    assert lib.d3d_abi_version() == 3
 
 
 def test_epa_scratch_sizing(lib):

@@ -109,6 +109,29 @@ def test_native_server_same_alone_and_in_the_mix(scene):
         srv.close()
 
 
+def test_native_server_worker_priority(scene):
+    """A worker asking for SCHED_FIFO answers as the default one; whether the
+    process was allowed to raise it is reported, and out-of-range priorities
+    are rejected."""
+    from distance3d_gb300 import _lib
+    from distance3d_gb300.serve import NativeCollisionServer
+    _, st, i1, i2 = scene
+    ref = CollisionBatch(st, 4096, precision="mixed", epa_kw=EPA_KW, graphs=False)
+    srv = NativeCollisionServer(st, capacity=4096, slots=2, precision="mixed", epa_kw=EPA_KW, worker_priority=1)
+    try:
+        out, _ = srv.result(srv.submit(i1[:500], i2[:500]))
+        alone = ref.run(i1[:500], i2[:500])
+        for k in alone:
+            assert np.array_equal(out[k], alone[k], equal_nan=True), k
+        stats = srv.stats(reset=True)
+        assert isinstance(stats["worker_realtime"], bool)
+        assert srv.stats(reset=False)["worker_realtime"] == stats["worker_realtime"]  # survives a reset
+    finally:
+        srv.close()
+    with pytest.raises(_lib.D3DError):
+        NativeCollisionServer(st, capacity=4096, slots=1, precision="mixed", epa_kw=EPA_KW, worker_priority=100)
+
+
 def test_native_server_rejects_bad_pairs(scene):
     from distance3d_gb300 import _lib
     from distance3d_gb300.serve import NativeCollisionServer

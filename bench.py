@@ -41,11 +41,12 @@ METRIC = "GJK+EPA pairs/s (mixed precision form; plain FP64 form alongside)"
 UNIT = "pairs/s"
 EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 # DRAM bytes per pair of the mixed kernels from one ncu capture of the
-# 131,072-pair workload (k_gjk_mixed_a + k_gjk_mixed_b + k_gjk_mixed_end per
-# pair; k_epa_warp + k_epa_refine per EPA pair, 38,814 of them); traffic
-# grows in proportion to the pairs
-NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78464256 + 3834112 + 140287744 + 23856896 + 45120768 + 1776384) / 131072,
-                           "epa_mixed": (33026304 + 36096 + 37686784 + 27904) / 38814}
+# 131,072-pair workload (k_gjk_mixed_a + _r + _b + _end per pair; k_epa_warp
+# + k_epa_refine per EPA pair, 38,814 of them); traffic grows in proportion
+# to the pairs
+NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78461440 + 3803648 + 127036160 + 10536704 + 15979776 + 0 + 7286784
+                                         + 182528) / 131072,
+                           "epa_mixed": (33027584 + 34560 + 34507776 + 18944) / 38814}
 # this library's kernels per timed mixed step (one graph replay), used only
 # when the graph cannot be read back (d3d_graph_kernel_nodes): k_pair_keys,
 # k_gjk_mixed_a, k_gjk_mixed_r, k_gjk_mixed_b, k_gjk_mixed_end,

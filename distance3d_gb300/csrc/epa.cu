@@ -266,8 +266,9 @@ __global__ void __launch_bounds__(kBlock) k_epa(d3d_store s, const int32_t* __re
 }
 
 // ---------------------------------------------------------------------------
-// The same EPA with one warp per pair.  The polytope (faces of 12 doubles)
-// and the loose edges live in the warp's shared memory; the steps whose
+// The same EPA with one warp per pair.  The polytope (faces as corner ids
+// and normals, see WarpPoly) and the loose edges live in the warp's shared
+// memory; the steps whose
 // order does not matter run across the lanes -- the closest-face scan (on
 // integer keys of the face distances), the visibility of every face, the
 // normals of the new faces, the closeness of a new vertex to the others --

@@ -165,14 +165,25 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_r(d3d_store s, const int32_
     for (int j = 0; j < 5; ++j) {
         if (j < count) {
             d3 d;
+            float4 f = make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));  // the gap row: no vertices known
             if (j < nr) {
-                const float4 f = hand[pid].d[j];
+                f = hand[pid].d[j];
                 d = mk((double)f.x, (double)f.y, (double)f.z);
             } else {
                 d = mk(-(double)v.x, -(double)v.y, -(double)v.z);
             }
+            // the polytope vertices phase A took along this row's direction are read, not searched again
             d3 p, q;
-            pair_supports<double, RefineSupportT<MESH>>(s, a, b, d, p, q);
+#pragma unroll 1
+            for (int k = 0; k < 2; ++k) {
+                Col<double> c;
+                load_col(s, k ? b : a, c);
+                const d3 x = RefineSupportT<MESH>::eval_at(c, s, k ? -d : d, handoff_vertex(f, k));
+                if (k)
+                    q = x;
+                else
+                    p = x;
+            }
             my[(6 * j + 0) * BLOCK] = p.x;
             my[(6 * j + 1) * BLOCK] = p.y;
             my[(6 * j + 2) * BLOCK] = p.z;

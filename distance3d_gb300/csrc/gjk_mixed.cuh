@@ -100,14 +100,23 @@ __device__ __forceinline__ int box_corner(const float* R, f3 d) {
 }
 
 // FP32 support of the mixed form's search phases.  MESH = false leaves out
-// the MeshGraph branch, for kernels launched on stores without meshes.
+// the MeshGraph branch, for kernels launched on stores without meshes.  A
+// non-null `vi` receives the vertex a box, hull or MeshGraph support took
+// (unchanged for the other types), so that the FP64 phases can take the same
+// vertex without searching again (RefineSupportT::eval_at).
 template <bool MESH>
 struct FastSupportT {
-    static __device__ __forceinline__ f3 base(const Col<float>& c, const d3d_store& s, f3 d) {
-        if (c.type == D3D_BOX && c.nv == 8) return load_vertex(s.verts32, c.off + box_corner(c.R, d));
+    static __device__ __forceinline__ f3 base(const Col<float>& c, const d3d_store& s, f3 d, int* vi = nullptr) {
+        if (c.type == D3D_BOX && c.nv == 8) {
+            const int k = box_corner(c.R, d);
+            if (vi) *vi = k;
+            return load_vertex(s.verts32, c.off + k);
+        }
         if (c.type == D3D_BOX || c.type == D3D_HULL) {
             if (c.nv < 1) return mk(NAN, NAN, NAN);
-            return load_vertex(s.verts32, c.off + hull_argmax(s.verts32, c.off, c.nv, d));
+            const int k = hull_argmax(s.verts32, c.off, c.nv, d);
+            if (vi) *vi = k;
+            return load_vertex(s.verts32, c.off + k);
         }
         if (c.type == D3D_SPHERE) {
             const float n2 = dot(d, d);
@@ -116,13 +125,15 @@ struct FastSupportT {
         }
         if (MESH && c.type == D3D_MESH) {
             if (c.nv < 1) return mk(NAN, NAN, NAN);
-            return xform(c.R, c.t, load_vertex(s.verts32, c.off + mesh_climb(c, s, rt_mul(c.R, d))));
+            const int k = mesh_climb(c, s, rt_mul(c.R, d));
+            if (vi) *vi = k;
+            return xform(c.R, c.t, load_vertex(s.verts32, c.off + k));
         }
         const bool up = upper_feature(c.type, c.R, c.p[0], c.p[1], d);
         return xform(c.R, c.t, local_point(c, rt_mul(c.R, d), up));
     }
-    static __device__ __forceinline__ f3 eval(const Col<float>& c, const d3d_store& s, f3 d) {
-        return margin_fast(s, c, base(c, s, d), d);
+    static __device__ __forceinline__ f3 eval(const Col<float>& c, const d3d_store& s, f3 d, int* vi = nullptr) {
+        return margin_fast(s, c, base(c, s, d, vi), d);
     }
 };
 using FastSupport = FastSupportT<true>;
@@ -132,6 +143,19 @@ template <bool MESH>
 struct RefineSupportT {
     static __device__ __forceinline__ d3 eval(const Col<double>& c, const d3d_store& s, d3 d) {
         return margin_fast(s, c, base(c, s, d), d);
+    }
+
+    // eval, given the vertex FastSupport took along the FP32 rounding of d
+    // (vi >= 0; -1: unknown): a box, hull or MeshGraph reads that vertex
+    // instead of searching again (the same search on the same FP32 inputs
+    // would return it), the other types evaluate as eval does.
+    static __device__ __forceinline__ d3 eval_at(const Col<double>& c, const d3d_store& s, d3 d, int vi) {
+        if (vi >= 0 && vi < c.nv) {
+            if (c.type == D3D_BOX || c.type == D3D_HULL) return margin_fast(s, c, load_vertex(s.verts64, c.off + vi), d);
+            if (MESH && c.type == D3D_MESH)
+                return margin_fast(s, c, xform(c.R, c.t, load_vertex(s.verts64, c.off + vi)), d);
+        }
+        return eval(c, s, d);
     }
 
     static __device__ __forceinline__ d3 base(const Col<double>& c, const d3d_store& s, d3 d) {
@@ -206,9 +230,11 @@ __device__ __forceinline__ JoltEps<float> fp32_eps() {
 
 enum PhaseAOutcome { PA_SEPARATED = 0, PA_TOUCHING = 1, PA_CLIPPED = 2, PA_FAILED = 3, PA_BAD_INDEX = 4 };
 
-// What phase A hands to phase B for one pair (80 bytes): the final closest
-// point (xyz) with the outcome, simplex size and iteration count packed in w,
-// and the search direction of each simplex row.
+// What phase A hands to the refinement pass for one pair (80 bytes): the
+// final closest point (xyz) with the outcome, simplex size and iteration
+// count packed in w, and per simplex row the search direction (xyz) and, in
+// w, the vertices the supports of a box, hull or MeshGraph took along it
+// (16 bits per collider, 0xffff for none; see handoff_vertex).
 struct __align__(16) Handoff {
     float4 v;
     float4 d[4];
@@ -217,10 +243,16 @@ struct __align__(16) Handoff {
 __device__ __forceinline__ int handoff_outcome(const Handoff& h) { return __float_as_int(h.v.w) & 0xff; }
 __device__ __forceinline__ int handoff_rows(const Handoff& h) { return (__float_as_int(h.v.w) >> 8) & 0xff; }
 __device__ __forceinline__ int handoff_iters(float4 v) { return (__float_as_int(v.w) >> 16) & 0xffff; }
+// the vertex collider k (0: i1, 1: i2) of a row took, -1 if none
+__device__ __forceinline__ int handoff_vertex(float4 d, int k) {
+    const int x = (int)((__float_as_uint(d.w) >> (16 * k)) & 0xffffu);
+    return x == 0xffff ? -1 : x;
+}
 
 // ---------------------------------------------------------------- phase A
 // The Jolt loop (gjk_step) in FP32 on the FP32 mirror; row j of S.P holds
-// the search direction that produced row j of S.Y.
+// the search direction that produced row j of S.Y, and row j of S.Q the
+// vertices its polytope supports took (bits of a float, moved with the row).
 struct PhaseALoop {
     Simplex<float> S;
     f3 dir;
@@ -247,14 +279,28 @@ __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a,
     ++L.it;
     const unsigned together = __activemask();
     f3 p, q;
-    pair_supports<float, FastSupportT<MESH>>(s, a, b, L.dir, p, q);
+    // the vertices the polytope supports took, 16 bits per collider (0xffff: none), ride in the
+    // Q row of the simplex (phase A reads only Y and the directions in P) to the handoff
+    unsigned vis = 0;
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        Col<float> c;
+        load_col(s, k ? b : a, c);
+        int vi = -1;
+        const f3 x = FastSupportT<MESH>::eval(c, s, k ? -L.dir : L.dir, &vi);
+        vis |= (unsigned)(vi >= 0 && vi < 0xffff ? vi : 0xffff) << (16 * k);
+        if (k)
+            q = x;
+        else
+            p = x;
+    }
     // reconverge after the type- and size-dependent supports, so that the
     // lanes solve their simplices together (see gjk_step)
     __syncwarp(together);
     f3 w = p - q;
     float dd = dot(L.dir, w);
     if (dd < 0.f && dd * dd > L.vl * max_d2) return PA_CLIPPED;
-    simplex_push(L.S, w, L.dir, q);
+    simplex_push(L.S, w, L.dir, mk(__uint_as_float(vis), 0.f, 0.f));
     f3 nv;
     float nl;
     int set;
@@ -281,7 +327,7 @@ __device__ __forceinline__ Handoff pa_handoff(const PhaseALoop& L, int outcome) 
     int it = L.it < 0xffff ? L.it : 0xffff;
     h.v = make_float4(L.v.x, L.v.y, L.v.z, __int_as_float(outcome | (L.S.n << 8) | (it << 16)));
 #pragma unroll
-    for (int j = 0; j < 4; ++j) h.d[j] = make_float4(L.S.R.P[j].x, L.S.R.P[j].y, L.S.R.P[j].z, 0.f);
+    for (int j = 0; j < 4; ++j) h.d[j] = make_float4(L.S.R.P[j].x, L.S.R.P[j].y, L.S.R.P[j].z, L.S.R.Q[j].x);
     return h;
 }
 

@@ -87,6 +87,25 @@ def test_gjk_distance_guard(scene, precision):
         assert np.array_equal(got[k][good], want[k], equal_nan=True), k
 
 
+def test_gjk_distance_cached_guard(scene):
+    """The MeshGraph-cached entry point (one thread per pair): the same
+    reports, and the cache entries of a rejected pair pass through."""
+    st, view, a, b, bad = scene
+    n = a.numel()
+    cache = torch.full((n, 2), -1, dtype=torch.int32, device=st.device)
+    cache[:, 1] = 7  # entries of colliders without meshes pass through
+    got = host(gjk_distance_batch(view, a, b, mesh_cache=cache))
+    assert (got["status"][bad] == _lib.STATUS_BAD_INDEX).all()
+    assert np.isnan(got["dist"][bad]).all()
+    c = cache.cpu().numpy()
+    assert (c[:, 0] == -1).all() and (c[:, 1] == 7).all()
+    good = ~bad
+    ok = torch.as_tensor(np.flatnonzero(good), device=st.device)
+    want = host(gjk_distance_batch(st, a[ok], b[ok]))
+    for k in ("dist", "cp1", "cp2", "n_simplex", "status", "iterations"):
+        assert np.array_equal(got[k][good], want[k], equal_nan=True), k
+
+
 def test_gjk_intersection_guard(scene):
     st, view, a, b, bad = scene
     got = host(gjk_intersection_batch(view, a, b))

@@ -76,6 +76,139 @@ __global__ void __launch_bounds__(BLOCK, f64_min_blocks<BLOCK>()) k_gjk_distance
     }
 }
 
+// The same loop with the simplex solves of a block regrouped by simplex
+// size.  The lanes of a warp hold simplices of different sizes, and each
+// size takes its own branch of closest_to_origin, so a warp ran the segment,
+// triangle and tetrahedron code one after the other with a few lanes each,
+// while FP64 instructions cost the pipe the same however few lanes are
+// active.  Here every round, after the supports (gjk_step_begin), each lane
+// with a simplex to solve writes its rows to shared memory at a place sorted
+// by size (tetrahedra, triangles, segments, points); thread t of the block
+// then solves the t-th simplex of that order, and each lane reads its result
+// back for gjk_step_end.  The solve reads only the rows, the row count and
+// prev, so it is the same arithmetic wherever it runs.  The block runs its
+// rounds in step (two barriers per round), to the end of its last pair.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, f64_min_blocks<BLOCK>()) k_gjk_distance_f64_grouped(
+    d3d_store s, const int32_t* __restrict__ i1, const int32_t* __restrict__ i2, const int32_t* __restrict__ order,
+    int64_t n, const unsigned long long* __restrict__ n_dev, unsigned long long* __restrict__ cursor,
+    d3d_gjk_options opt, DistanceOut o) {
+    constexpr int W = BLOCK / 32;
+    constexpr unsigned kAll = 0xffffffffu;
+    __shared__ double rows[24 * BLOCK];  // the simplex P/Q rows of each lane
+    __shared__ double ty[12 * BLOCK];    // task t: row r, coordinate c at [(3 r + c) BLOCK + t]
+    __shared__ double tprev[BLOCK];
+    __shared__ double rv[4 * BLOCK];     // result of the lane that owns a task: v (3), v.v
+    __shared__ int tmeta[BLOCK];         // task t: row count | owner << 8
+    __shared__ int rset[BLOCK];          // owner's result: set | closer << 8
+    __shared__ int cnt[4 * W];           // simplices per size class and warp
+    if (n_dev) n = (int64_t)*n_dev;
+    const JoltEps<double> E = reference_eps<double>();
+    const double tol_sq = opt.tolerance * opt.tolerance;
+    const int ln = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    GjkLoop<double, SmemRows<double, BLOCK>> g;
+    g.S.R.base = rows + threadIdx.x;
+    int64_t pid = 0;
+    int a = 0, b = 0;
+    bool have = false, exhausted = false, bad = false;
+    WarpChunk chunk;
+    while (true) {
+        __syncwarp();
+        const bool want = !have && !exhausted;
+        const long long slot = fetch_slot_chunked(cursor, want, chunk, kAll, kChunk, n);
+        if (want) {
+            if (slot >= n) {
+                exhausted = true;
+            } else {
+                pid = order ? order[slot] : slot;
+                a = i1[pid];
+                b = i2[pid];
+                bad = !pair_ok(s, a, b);
+                simplex_clear(g.S);
+                const d3 dir = mk(1.0, 0.0, 0.0);
+                gjk_begin(g, dir, dot(dir, dir), DBL_MAX);
+                have = true;
+            }
+        }
+        if (!__syncthreads_or(have)) break;
+        bool solve = false;
+        if (have) {
+            if (bad) {  // out-of-range index: reported at once, no record read
+                store_bad_index(o, pid);
+                have = false;
+            } else if (gjk_step_begin<double>(g, s, a, b, opt.max_distance_squared, opt.max_iterations)) {
+                GjkResult<double> r;
+                gjk_end(g, opt.sanity_check, E, r);
+                store_result(o, pid, r, g.S);
+                have = false;
+            } else {
+                solve = true;
+            }
+        }
+        // the solve's place: size class (0 tetrahedron .. 3 point), then warp, then lane
+        const int cls = solve ? 4 - g.S.n : 4;
+        int rank = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const unsigned m = __ballot_sync(kAll, cls == c);
+            if (cls == c) rank = __popc(m & ((1u << ln) - 1u));
+            if (ln == 0) cnt[c * W + wp] = __popc(m);
+        }
+        __syncthreads();
+        int t = 0, ntask = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const int k = cnt[c * W + w];
+                if (c < cls || (c == cls && w < wp)) t += k;
+                ntask += k;
+            }
+        t += rank;
+        if (solve) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                ty[(3 * r) * BLOCK + t] = g.S.Y[r].x;
+                ty[(3 * r + 1) * BLOCK + t] = g.S.Y[r].y;
+                ty[(3 * r + 2) * BLOCK + t] = g.S.Y[r].z;
+            }
+            tprev[t] = g.prev;
+            tmeta[t] = g.S.n | ((int)threadIdx.x << 8);
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < ntask) {
+            const int u = threadIdx.x;
+            Simplex<double> S;
+            const int meta = tmeta[u];
+            S.n = meta & 0xff;
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                S.Y[r] = mk(ty[(3 * r) * BLOCK + u], ty[(3 * r + 1) * BLOCK + u], ty[(3 * r + 2) * BLOCK + u]);
+            d3 nv = mk(0.0, 0.0, 0.0);
+            double nl = 0.0;
+            int set = 0;
+            const bool closer = closest_to_origin(S, tprev[u], E, nv, nl, set);
+            const int owner = meta >> 8;
+            rv[owner] = nv.x;
+            rv[BLOCK + owner] = nv.y;
+            rv[2 * BLOCK + owner] = nv.z;
+            rv[3 * BLOCK + owner] = nl;
+            rset[owner] = (set & 0xff) | (closer ? 256 : 0);
+        }
+        __syncthreads();
+        if (solve) {
+            const int x = rset[threadIdx.x];
+            const d3 nv = mk(rv[threadIdx.x], rv[BLOCK + threadIdx.x], rv[2 * BLOCK + threadIdx.x]);
+            if (gjk_step_end(g, tol_sq, E, (x & 256) != 0, nv, rv[3 * BLOCK + threadIdx.x], x & 0xff)) {
+                GjkResult<double> r;
+                gjk_end(g, opt.sanity_check, E, r);
+                store_result(o, pid, r, g.S);
+                have = false;
+            }
+        }
+    }
+}
+
 // The same loop with the reference's MeshGraph vertex caching: the mesh
 // supports of pair k start from mesh_cache[2k] (collider i1[k]) and
 // mesh_cache[2k+1] (collider i2[k]), -1 meaning the mesh's start vertex, and
@@ -201,14 +334,16 @@ int launch_gjk_f64(const d3d_store& store, const int32_t* i1, const int32_t* i2,
         k_gjk_distance_f64<32><<<blocks > 0 ? blocks : 1, 32, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor,
                                                                            opt, o);
     } else if (t.gjk_block == 64) {
-        const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<64>, 64, n, blocks_per_sm(t, 64));
-        k_gjk_distance_f64<64><<<blocks, 64, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+        const void* k = (const void*)k_gjk_distance_f64_grouped<64>;
+        const int blocks = persistent_blocks(k, 64, n, blocks_per_sm(t, 64));
+        k_gjk_distance_f64_grouped<64><<<blocks, 64, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
     } else if (t.gjk_block == 256) {
         const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<256>, 256, n, blocks_per_sm(t, 256));
         k_gjk_distance_f64<256><<<blocks, 256, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
     } else {
-        const int blocks = persistent_blocks((const void*)k_gjk_distance_f64<128>, 128, n, blocks_per_sm(t, 128));
-        k_gjk_distance_f64<128><<<blocks, 128, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
+        const void* k = (const void*)k_gjk_distance_f64_grouped<128>;
+        const int blocks = persistent_blocks(k, 128, n, blocks_per_sm(t, 128));
+        k_gjk_distance_f64_grouped<128><<<blocks, 128, 0, stream>>>(store, i1, i2, order, n, n_dev, cursor, opt, o);
     }
     return check_launch("d3d_gjk_distance");
 }

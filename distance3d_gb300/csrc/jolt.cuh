@@ -518,9 +518,9 @@ __device__ __forceinline__ void gjk_begin(GjkLoop<T, Rows>& g, V3<T> dir, T vl, 
 // the reference's supports with MeshGraph vertex caching
 // (pair_supports_cached) instead of Sup.
 template <typename T, typename Sup = ExactSupport, bool GAP = false, typename Rows>
-__device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
-                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0), T abs_gap2 = T(0),
-                                         int* mesh_cache = nullptr) {
+__device__ __forceinline__ bool gjk_step_begin(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T max_d2,
+                                               int max_iter, T rel_gap = T(0), T abs_gap2 = T(0),
+                                               int* mesh_cache = nullptr) {
     if (g.it >= max_iter) {
         g.status = D3D_STATUS_MAX_ITER;
         g.state = GJK_NO_INTERSECTION;
@@ -553,10 +553,15 @@ __device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& s
         }
     }
     simplex_push(g.S, w, p, q);
-    V3<T> nv;
-    T nl;
-    int set;
-    if (closest_to_origin(g.S, g.prev, E, nv, nl, set)) {
+    return false;
+}
+
+// The rest of the iteration, given the result of
+// closest_to_origin(g.S, g.prev, E, nv, nl, set) (`closer`: its return value).
+template <typename T, typename Rows>
+__device__ __forceinline__ bool gjk_step_end(GjkLoop<T, Rows>& g, T tol_sq, const JoltEps<T>& E, bool closer,
+                                             V3<T> nv, T nl, int set) {
+    if (closer) {
         g.dir = nv;
         g.vl = nl;
     } else {
@@ -581,6 +586,20 @@ __device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& s
     }
     g.prev = g.vl;
     return false;
+}
+
+// One iteration: gjk_step_begin, the simplex solve, gjk_step_end (kernels
+// that solve the simplices of a block together call the halves themselves).
+template <typename T, typename Sup = ExactSupport, bool GAP = false, typename Rows>
+__device__ __forceinline__ bool gjk_step(GjkLoop<T, Rows>& g, const d3d_store& st, int a, int b, T tol_sq, T max_d2,
+                                         int max_iter, const JoltEps<T>& E, T rel_gap = T(0), T abs_gap2 = T(0),
+                                         int* mesh_cache = nullptr) {
+    if (gjk_step_begin<T, Sup, GAP>(g, st, a, b, max_d2, max_iter, rel_gap, abs_gap2, mesh_cache)) return true;
+    V3<T> nv = mk(T(0), T(0), T(0));
+    T nl = T(0);
+    int set = 0;
+    const bool closer = closest_to_origin(g.S, g.prev, E, nv, nl, set);
+    return gjk_step_end(g, tol_sq, E, closer, nv, nl, set);
 }
 
 // After the loop: closest points, sanity check, distance

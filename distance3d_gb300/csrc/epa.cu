@@ -655,6 +655,434 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same EPA with W pairs per block in lock step (k_epa_exact_block).  Two
+// steps of an iteration cost the FP64 pipe per pair, not per lane: the
+// support of an analytic collider (16 lanes of a half warp evaluate the same
+// FP64 expressions, and the two halves of a pair of different types run one
+// after the other) and the normals of the new faces (one lane per loose edge,
+// ~8 of 32 lanes active).  Here each round every warp runs one iteration of
+// its pair up to the support, posts the supports of its analytic colliders
+// (a box or hull keeps its 16-lane FP64 argmax in the owning warp), and warp
+// 0 evaluates the posted supports one per lane; after the visible faces are
+// removed every warp posts its loose edges (up to 32) and all lanes of the
+// block compute the new faces' normals, one per lane; each warp then commits
+// its new faces in loose-edge order.  Every value is computed by the same
+// expressions as in epa_pair_warp, so the results are the same bit for bit.
+// A warp whose pair ends (or that has none) sits out the rest of the round.
+
+constexpr int kFaceTaskPerWarp = 32;  // loose edges a warp posts per round; more are computed in place
+
+struct BlockTasks {
+    double* sres;            // support results, 3 doubles per task (task 2 w + side)
+    double* sdir;            // support directions of the posted tasks
+    int* scol;               // collider of each posted task, -1 if none
+    double* fn;              // new faces: normal (3 doubles) per task
+    unsigned long long* fk;  // their distance keys (kept faces)
+    unsigned* fid;           // ids | 1 << 31 if kept
+    unsigned* ftask;         // task: warp | edge << 8
+    int* wv;                 // the new vertex of each warp this round
+    int* nface;              // face tasks posted this round
+};
+
+__host__ __device__ inline int block_task_bytes(int W) {
+    const int st = 2 * W;
+    const int ft = W * kFaceTaskPerWarp;
+    return ((st * 48 + st * 4 + ft * (24 + 8 + 4 + 4) + W * 4 + 16) + 15) & ~15;
+}
+
+template <int W>
+__device__ __forceinline__ BlockTasks block_tasks_at(unsigned char* base) {
+    constexpr int ST = 2 * W, FT = W * kFaceTaskPerWarp;
+    BlockTasks T;
+    T.sres = reinterpret_cast<double*>(base);
+    T.sdir = T.sres + 3 * ST;
+    T.fn = T.sdir + 3 * ST;
+    T.fk = reinterpret_cast<unsigned long long*>(T.fn + 3 * FT);
+    T.scol = reinterpret_cast<int*>(T.fk + FT);
+    T.fid = reinterpret_cast<unsigned*>(T.scol + ST);
+    T.ftask = T.fid + FT;
+    T.wv = reinterpret_cast<int*>(T.ftask + FT);
+    T.nface = T.wv + W;
+    return T;
+}
+
+// epa.py:131-146 for loose edge k of polytope P with new vertex wv: the
+// face's unit normal and first corner after the reference's winding fix,
+// whether it is kept (norm >= 0.5), and its vertex ids.
+__device__ __forceinline__ void new_face(const WarpPoly& P, int k, int wv, LengthBounds lb, d3& v0, d3& nrm, bool& keep,
+                                         unsigned& ids) {
+    const unsigned ev = P.eid[k];
+    ids = (ev & 0xffu) | (ev & 0xff00u) | ((unsigned)wv << 16);
+    const d3 e0 = P.vert(ev & 0xffu), e1 = P.vert((ev >> 8) & 0xffu), w = P.vert(wv);
+    v0 = e0;
+    nrm = norm_vec(cross(e1 - e0, w - e0));
+    keep = !(dot(nrm, nrm) < lb.keep);
+    // epa.py:139-146: the reference swaps through a NumPy view of row 0, so
+    // the net effect is v0 := v1 (v1 unchanged), n := -n
+    if (keep && dot(v0, nrm) + 1e-6 < 0.0) {
+        v0 = e1;
+        nrm = -nrm;
+        ids = (ids & ~0xffu) | ((ids >> 8) & 0xffu);
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s, const int32_t* __restrict__ i1,
+                                                            const int32_t* __restrict__ i2,
+                                                            const int32_t* __restrict__ list, int64_t n,
+                                                            const unsigned long long* __restrict__ n_dev,
+                                                            unsigned long long* __restrict__ cursor,
+                                                            const double* __restrict__ simplex, d3d_epa_options o,
+                                                            LengthBounds lb, double* __restrict__ mtv_out,
+                                                            int8_t* __restrict__ status_out,
+                                                            int32_t* __restrict__ n_faces_out,
+                                                            double* __restrict__ faces) {
+    extern __shared__ __align__(16) unsigned char smem_blk[];
+    const int ln = lane_of(), wp = threadIdx.x >> 5;
+    const int pbytes = exact_warp_bytes(o);
+    const WarpPoly P = WarpPoly::at(smem_blk + wp * pbytes, o.max_faces, o.max_loose_edges, o.max_iterations + 4);
+    const BlockTasks T = block_tasks_at<W>(smem_blk + W * pbytes);
+    unsigned long long* const K = P.K;
+    unsigned char* const vis = P.vis;
+    const double eps = o.epsilon;
+    if (n_dev) n = (int64_t)*n_dev;
+    int64_t pid = 0;
+    int a = 0, b = 0, nf = 0, closest = 0, nv = 0, it = 0, stt = 0;
+    bool have = false, exhausted = false;
+    d3 mtv = mk(0.0, 0.0, 0.0);
+    while (true) {
+        // a warp without a pair takes the next one
+        bool fresh = false;
+        if (!have && !exhausted) {
+            long long slot = 0;
+            if (ln == 0) slot = (long long)atomicAdd(cursor, 1ull);
+            slot = __shfl_sync(kWarpAll, slot, 0);
+            if (slot >= n) {
+                exhausted = true;
+            } else {
+                pid = list ? list[slot] : slot;
+                a = i1[pid];
+                b = i2[pid];
+                if (pair_ok(s, a, b)) {
+                    have = true;
+                    fresh = true;
+                } else if (ln == 0) {
+                    epa_store_bad_index(mtv_out, status_out, n_faces_out, pid);
+                }
+            }
+        }
+        if (!__syncthreads_or(have || (!exhausted && ln == 0))) break;
+        if (threadIdx.x == 0) *T.nface = 0;
+        bool run = have;  // this warp iterates this round
+        if (fresh) {
+            // vertices 0-3: the simplex's rows, and their closeness; faces ABC, ACD, ADB, BDC
+            const double* sx = simplex + 12 * pid;
+            if (ln < 12) P.V[ln] = sx[ln];
+            __syncwarp();
+            {
+                const d3 d = ld(P.V + 3 * ((ln >> 2) & 3)) - ld(P.V + 3 * (ln & 3));
+                const unsigned m = __ballot_sync(kWarpAll, ln < 16 && dot(d, d) < lb.edge);
+                if (ln < 4) P.pm[ln * P.W] = (m >> (4 * ln)) & 0xfu;
+            }
+            if (ln < 4) {
+                const int init[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 3, 1}, {1, 3, 2}};
+                const d3 v0 = P.vert(init[ln][0]), v1 = P.vert(init[ln][1]), v2 = P.vert(init[ln][2]);
+                const d3 nn = norm_vec(cross(v1 - v0, v2 - v0));  // epa.py:99-102
+                st(P.N + 3 * ln, nn);
+                K[ln] = dist_key((v0.x * nn.x + v0.y * nn.y) + v0.z * nn.z);
+                P.fid[ln] = (unsigned)init[ln][0] | ((unsigned)init[ln][1] << 8) | ((unsigned)init[ln][2] << 16);
+            }
+            __syncwarp();
+            nf = 4;
+            closest = 0;
+            nv = 4;
+            it = 0;
+        }
+        // the iteration up to the support
+        d3 sd = mk(0.0, 0.0, 0.0);
+        double md = 0.0;
+        if (run) {
+            if (it >= o.max_iterations) {
+                // epa.py:77: closest_face is a view, read after the last iteration's edits
+                const d3 nn = P.normal(closest);
+                mtv = nn * dot(P.corner(closest, 0), nn);
+                stt = D3D_STATUS_EPA_NOT_CONVERGED;
+                run = false;
+            } else if (nf == 0) {
+                mtv = mk(double(NAN), double(NAN), double(NAN));
+                stt = D3D_STATUS_EPA_DEGENERATE;
+                run = false;
+            }
+        }
+        if (run) {
+            unsigned long long bk = ~0ull;
+            int bi = 0x7fffffff;
+            for (int i = ln; i < nf; i += 32) {
+                const unsigned long long k = K[i];
+                if (k < bk) {
+                    bk = k;
+                    bi = i;
+                }
+            }
+            for (int m = 16; m; m >>= 1) {
+                const unsigned long long ok = __shfl_xor_sync(kWarpAll, bk, m);
+                const int oi = __shfl_xor_sync(kWarpAll, bi, m);
+                if (ok < bk || (ok == bk && oi < bi)) {
+                    bk = ok;
+                    bi = oi;
+                }
+            }
+            closest = (K[0] == ~0ull || bk == ~0ull) ? 0 : bi;
+            md = P.dist(closest);
+            sd = P.normal(closest);
+            // supports: a box or hull by its half warp here (first maximum of V . d, a NaN at vertex
+            // 0 wins, later NaNs never do); the other types are posted for warp 0
+            const bool up = ln & 16;
+            const unsigned half = up ? 0xffff0000u : 0x0000ffffu;
+            const int side = up ? 1 : 0;
+            Col<double> c;
+            load_col(s, up ? b : a, c);
+            const d3 dd = up ? -sd : sd;
+            if (c.type == D3D_BOX || c.type == D3D_HULL) {
+                d3 r;
+                if (c.nv < 1) {
+                    r = mk(double(NAN), double(NAN), double(NAN));
+                } else {
+                    const int h = ln & 15;
+                    double bv = 0.0;
+                    int bj = -1;
+                    bool nan0 = false;
+                    for (int k = h; k < c.nv; k += 16) {
+                        const d3 v = load_vertex(s.verts64, c.off + k);
+                        const double x = dot102(v.x, v.y, v.z, dd.x, dd.y, dd.z);
+                        if (k == 0 && x != x) nan0 = true;
+                        if (bj < 0 ? x == x : x > bv) {
+                            bv = x;
+                            bj = k;
+                        }
+                    }
+                    for (int m = 8; m; m >>= 1) {
+                        const double ov = __shfl_xor_sync(half, bv, m);
+                        const int oi = __shfl_xor_sync(half, bj, m);
+                        if (oi >= 0 && (bj < 0 || ov > bv || (ov == bv && oi < bj))) {
+                            bv = ov;
+                            bj = oi;
+                        }
+                    }
+                    const bool any_nan0 = __ballot_sync(half, nan0) != 0u;
+                    const int k = (c.nv == 1 || any_nan0 || bj < 0 || bj >= c.nv) ? 0 : bj;
+                    r = add_margin(c, load_vertex(s.verts64, c.off + k), dd);
+                }
+                if ((ln & 15) == 0) {
+                    st(T.sres + 3 * (2 * wp + side), r);
+                    T.scol[2 * wp + side] = -1;
+                }
+            } else if ((ln & 15) == 0) {
+                st(T.sdir + 3 * (2 * wp + side), dd);
+                T.scol[2 * wp + side] = up ? b : a;
+            }
+        } else if (ln < 2) {
+            T.scol[2 * wp + ln] = -1;
+        }
+        __syncthreads();
+        // warp 0: the posted supports, one per lane
+        if (wp == 0 && ln < 2 * W) {
+            const int ci = T.scol[ln];
+            if (ci >= 0) {
+                Col<double> c;
+                load_col(s, ci, c);
+                st(T.sres + 3 * ln, support(c, s, ld(T.sdir + 3 * ln)));
+            }
+        }
+        __syncthreads();
+        int ne = 0, wv = 0;
+        d3 w = mk(0.0, 0.0, 0.0);
+        if (run) {
+            w = ld(T.sres + 3 * (2 * wp)) - ld(T.sres + 3 * (2 * wp + 1));
+            const double pd = dot(w, sd);
+            if (pd - md < eps) {  // epa.py:67-70
+                mtv = sd * pd;
+                stt = D3D_STATUS_OK;
+                run = false;
+            }
+        }
+        if (run) {
+            ++it;
+            // w becomes vertex wv: its closeness to every vertex (itself
+            // included) fills row wv and column wv of pm
+            wv = nv++;
+            if (ln < 3) P.V[3 * wv + ln] = ln == 0 ? w.x : (ln == 1 ? w.y : w.z);
+            for (int kb = 0; kb <= wv; kb += 32) {
+                const int k = kb + ln;
+                bool c = false;
+                if (k <= wv) {
+                    const d3 d = (k == wv ? w : ld(P.V + 3 * k)) - w;
+                    c = dot(d, d) < lb.edge;
+                }
+                const unsigned m = __ballot_sync(kWarpAll, c);
+                if (ln == 0) P.pm[wv * P.W + (kb >> 5)] = m;
+                if (k < wv) {
+                    unsigned& word = P.pm[k * P.W + (wv >> 5)];
+                    const unsigned bit = (c ? 1u : 0u) << (wv & 31);
+                    word = (wv & 31) == 0 ? bit : (word | bit);
+                }
+            }
+            // epa.py:157-165: visibility of every face (epa.py:122-124)
+            for (int i = ln; i < nf; i += 32) vis[i] = dot(P.normal(i), w - P.corner(i, 0)) > eps ? 1 : 0;
+            __syncwarp();
+            // remove visible faces in the reference's order, collecting edges
+            int i = 0;
+            while (true) {
+                int p = -1;
+                for (int base = i; base < nf; base += 32) {
+                    const int j = base + ln;
+                    const unsigned m = __ballot_sync(kWarpAll, j < nf && vis[j]);
+                    if (m) {
+                        p = base + __ffs(m) - 1;
+                        break;
+                    }
+                }
+                if (p < 0) break;
+                const unsigned fv = P.fid[p];
+                for (int j = 0; j < 3; ++j) {
+                    const int x0 = (fv >> (8 * j)) & 0xff, x1 = (fv >> (8 * ((j + 1) % 3))) & 0xff;
+                    int found = -1;
+                    for (int kb = 0; kb < ne; kb += 32) {
+                        const int k = kb + ln;
+                        bool match = false;
+                        if (k < ne) {
+                            const unsigned e = P.eid[k];
+                            match = P.close(e >> 8, x0) && P.close(e & 0xff, x1);
+                        }
+                        const unsigned m = __ballot_sync(kWarpAll, match);
+                        if (m) {
+                            found = kb + __ffs(m) - 1;
+                            break;
+                        }
+                    }
+                    if (found >= 0) {
+                        if (ln == 0) P.eid[found] = P.eid[ne - 1];
+                        --ne;
+                    } else {
+                        if (ne >= o.max_loose_edges) break;  // epa.py:193-198
+                        if (ln == 0) P.eid[ne] = (unsigned short)(x0 | (x1 << 8));
+                        ++ne;
+                    }
+                    __syncwarp();
+                }
+                // epa.py:118-120: the last face moves into slot p, which is tested again
+                if (ln < 3) P.N[3 * p + ln] = P.N[3 * (nf - 1) + ln];
+                if (ln == 0) {
+                    vis[p] = vis[nf - 1];
+                    K[p] = K[nf - 1];
+                    P.fid[p] = P.fid[nf - 1];
+                }
+                --nf;
+                i = p;
+                __syncwarp();
+            }
+        }
+        // the new faces of up to 32 loose edges per warp go to the block
+        const bool post = run && ne <= kFaceTaskPerWarp;
+        int fbase = 0;
+        if (post && ln == 0) {
+            fbase = atomicAdd(T.nface, ne);
+            T.wv[wp] = wv;
+        }
+        fbase = __shfl_sync(kWarpAll, fbase, 0);
+        if (post && ln < ne) T.ftask[fbase + ln] = (unsigned)wp | ((unsigned)ln << 8);
+        __syncthreads();
+        for (int t = threadIdx.x; t < *T.nface; t += 32 * W) {
+            const unsigned task = T.ftask[t];
+            const int q = task & 0xff, k = task >> 8;
+            const WarpPoly Q = WarpPoly::at(smem_blk + q * pbytes, o.max_faces, o.max_loose_edges,
+                                            o.max_iterations + 4);
+            d3 v0, nrm;
+            bool keep;
+            unsigned ids;
+            new_face(Q, k, T.wv[q], lb, v0, nrm, keep, ids);
+            st(T.fn + 3 * t, nrm);
+            if (keep) T.fk[t] = dist_key((v0.x * nrm.x + v0.y * nrm.y) + v0.z * nrm.z);
+            T.fid[t] = ids | (keep ? 0x80000000u : 0u);
+        }
+        __syncthreads();
+        if (run) {
+            // epa.py:126-137 extend_with_point, in loose-edge order
+            int kept = 0;
+            for (int kb = 0; kb < ne; kb += 32) {
+                const int k = kb + ln;
+                d3 v0 = mk(0.0, 0.0, 0.0), nrm = v0;
+                bool keep = false;
+                unsigned ids = 0;
+                unsigned long long key = 0;
+                if (k < ne) {
+                    if (post) {
+                        const int t = fbase + k;
+                        nrm = ld(T.fn + 3 * t);
+                        ids = T.fid[t];
+                        keep = (ids >> 31) != 0;
+                        ids &= 0x7fffffffu;
+                        if (keep) key = T.fk[t];
+                    } else {
+                        new_face(P, k, wv, lb, v0, nrm, keep, ids);
+                        if (keep) key = dist_key((v0.x * nrm.x + v0.y * nrm.y) + v0.z * nrm.z);
+                    }
+                }
+                const unsigned km = __ballot_sync(kWarpAll, keep);
+                const int before = __popc(km & ((1u << ln) - 1u));
+                // epa.py:128: the face buffer is checked before every loose edge
+                const bool over = k < ne && nf + kept + before >= o.max_faces;
+                const unsigned om = __ballot_sync(kWarpAll, over);
+                const int limit = om ? __ffs(om) - 1 : 32;  // edges of this chunk written before the overflow
+                if (keep && ln < limit) {
+                    const int idx = nf + kept + before;
+                    st(P.N + 3 * idx, nrm);
+                    K[idx] = key;
+                    P.fid[idx] = ids;
+                }
+                if (om) {
+                    nf += kept + __popc(km & ((1u << limit) - 1u));
+                    mtv = mk(double(NAN), double(NAN), double(NAN));
+                    stt = D3D_STATUS_EPA_FACE_OVERFLOW;
+                    run = false;
+                    break;
+                }
+                // epa.py:131-135: a face that is not kept stays in the slot past the live faces
+                // (see epa_pair_warp)
+                if (k == ne - 1 && !keep) {
+                    const int idx = nf + kept + before;
+                    st(P.N + 3 * idx, nrm);
+                    P.fid[idx] = ids;
+                }
+                kept += __popc(km);
+            }
+            if (run) nf += kept;
+            __syncwarp();
+        }
+        // a pair that ended this round
+        if (have && !run) {
+            if (ln == 0) {
+                mtv_out[3 * pid] = mtv.x;
+                mtv_out[3 * pid + 1] = mtv.y;
+                mtv_out[3 * pid + 2] = mtv.z;
+                status_out[pid] = (int8_t)stt;
+                n_faces_out[pid] = stt == D3D_STATUS_EPA_DEGENERATE ? 0 : nf;
+            }
+            if (faces && stt != D3D_STATUS_EPA_DEGENERATE) {
+                double* out = faces + pid * 12 * (int64_t)o.max_faces;
+                for (int f = ln; f < nf; f += 32) {
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) st(out + 12 * f + 3 * j, P.corner(f, j));
+                    st(out + 12 * f + 9, P.normal(f));
+                }
+            }
+            have = false;
+            __syncwarp();
+        }
+    }
+}
+
 constexpr int64_t kExactSmemPerBlock = 227 * 1024;
 
 bool exact_warp_supported(const d3d_epa_options& o) {
@@ -663,12 +1091,52 @@ bool exact_warp_supported(const d3d_epa_options& o) {
            (int64_t)exact_warp_bytes(o) <= kExactSmemPerBlock;
 }
 
-// One warp per block, each block holding one polytope, as many per SM as
-// shared memory and registers allow.
+// W pairs per block in lock step (k_epa_exact_block), W = 8 or 4 as shared
+// memory allows; 0 if neither fits.
+int exact_block_warps(const d3d_epa_options& o) {
+    if (!exact_warp_supported(o)) return 0;
+    for (int w = 8; w >= 4; w /= 2)
+        if ((int64_t)w * exact_warp_bytes(o) + block_task_bytes(w) <= kExactSmemPerBlock) return w;
+    return 0;
+}
+
+template <int W>
+int exact_block_launch_w(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
+                         const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
+                         const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
+                         cudaStream_t stream) {
+    const int smem = W * exact_warp_bytes(o) + block_task_bytes(W);
+    const void* fn = (const void*)k_epa_exact_block<W>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) {
+        set_error("d3d_epa: %s", cudaGetErrorString(e));
+        return D3D_ERR_CUDA;
+    }
+    const int blocks = persistent_blocks(fn, 32 * W, n * 32, 0, smem);
+    k_epa_exact_block<W><<<blocks, 32 * W, smem, stream>>>(store, i1, i2, list, n, n_dev, cursor, simplex, o,
+                                                           length_bounds(o.epsilon), mtv, status, n_faces, faces);
+    return check_launch("d3d_epa");
+}
+
+// The FP64 EPA with the polytopes in shared memory: W pairs per block in lock
+// step where W polytopes fit a block (k_epa_exact_block), else one warp per
+// block, each block holding one polytope, as many per SM as shared memory and
+// registers allow (k_epa_exact_warp).
 int exact_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* i2, const int32_t* list, int64_t n,
                       const unsigned long long* n_dev, unsigned long long* cursor, const double* simplex,
                       const d3d_epa_options& o, double* mtv, int8_t* status, int32_t* n_faces, double* faces,
                       cudaStream_t stream) {
+    // the block form where its polytopes fit
+    const int bw = exact_block_warps(o);
+    if (bw == 8)
+        return exact_block_launch_w<8>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces,
+                                       stream);
+    if (bw == 4)
+        return exact_block_launch_w<4>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces,
+                                       stream);
     const int smem = exact_warp_bytes(o);
     const void* fn = (const void*)k_epa_exact_warp;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

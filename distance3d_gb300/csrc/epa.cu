@@ -1091,11 +1091,14 @@ bool exact_warp_supported(const d3d_epa_options& o) {
            (int64_t)exact_warp_bytes(o) <= kExactSmemPerBlock;
 }
 
-// W pairs per block in lock step (k_epa_exact_block), W = 8 or 4 as shared
-// memory allows; 0 if neither fits.
+// W pairs per block in lock step (k_epa_exact_block), W = 4 or 2 as shared
+// memory allows; 0 if neither fits.  (At the bench's options, 310k pairs:
+// W = 4 61.7 ms, W = 2 70.0 ms, W = 8 69.3 ms, W = 16 78.4 ms, one warp per
+// block 84.1 ms: wider blocks share more supports and normals but wait longer
+// at their barriers, narrower ones share less.)
 int exact_block_warps(const d3d_epa_options& o) {
     if (!exact_warp_supported(o)) return 0;
-    for (int w = 8; w >= 4; w /= 2)
+    for (int w = 4; w >= 2; w /= 2)
         if ((int64_t)w * exact_warp_bytes(o) + block_task_bytes(w) <= kExactSmemPerBlock) return w;
     return 0;
 }
@@ -1131,11 +1134,11 @@ int exact_warp_launch(const d3d_store& store, const int32_t* i1, const int32_t* 
                       cudaStream_t stream) {
     // the block form where its polytopes fit
     const int bw = exact_block_warps(o);
-    if (bw == 8)
-        return exact_block_launch_w<8>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces,
-                                       stream);
     if (bw == 4)
         return exact_block_launch_w<4>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces,
+                                       stream);
+    if (bw == 2)
+        return exact_block_launch_w<2>(store, i1, i2, list, n, n_dev, cursor, simplex, o, mtv, status, n_faces, faces,
                                        stream);
     const int smem = exact_warp_bytes(o);
     const void* fn = (const void*)k_epa_exact_warp;

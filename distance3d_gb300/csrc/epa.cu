@@ -663,8 +663,10 @@ __global__ void k_epa_exact_warp(d3d_store s, const int32_t* __restrict__ i1, co
 // after the other) and the normals of the new faces (one lane per loose edge,
 // ~8 of 32 lanes active).  Here each round every warp runs one iteration of
 // its pair up to the support, posts the supports of its analytic colliders
-// (a box or hull keeps its 16-lane FP64 argmax in the owning warp), and warp
-// 0 evaluates the posted supports one per lane; after the visible faces are
+// (a box or hull keeps its 16-lane FP64 argmax in the owning warp), and the
+// posted supports are evaluated one per lane, the supports of collider type t
+// by warp t % W (so that the warps run different types' paths side by side,
+// 61.8 -> 59.1 ms against warp 0 for all); after the visible faces are
 // removed every warp posts its loose edges (up to 32) and all lanes of the
 // block compute the new faces' normals, one per lane; each warp then commits
 // its new faces in loose-edge order.  Every value is computed by the same
@@ -677,6 +679,7 @@ struct BlockTasks {
     double* sres;            // support results, 3 doubles per task (task 2 w + side)
     double* sdir;            // support directions of the posted tasks
     int* scol;               // collider of each posted task, -1 if none
+    int* stype;              // its collider type
     double* fn;              // new faces: normal (3 doubles) per task
     unsigned long long* fk;  // their distance keys (kept faces)
     unsigned* fid;           // ids | 1 << 31 if kept
@@ -688,7 +691,7 @@ struct BlockTasks {
 __host__ __device__ inline int block_task_bytes(int W) {
     const int st = 2 * W;
     const int ft = W * kFaceTaskPerWarp;
-    return ((st * 48 + st * 4 + ft * (24 + 8 + 4 + 4) + W * 4 + 16) + 15) & ~15;
+    return ((st * 48 + st * 8 + ft * (24 + 8 + 4 + 4) + W * 4 + 16) + 15) & ~15;
 }
 
 template <int W>
@@ -700,7 +703,8 @@ __device__ __forceinline__ BlockTasks block_tasks_at(unsigned char* base) {
     T.fn = T.sdir + 3 * ST;
     T.fk = reinterpret_cast<unsigned long long*>(T.fn + 3 * FT);
     T.scol = reinterpret_cast<int*>(T.fk + FT);
-    T.fid = reinterpret_cast<unsigned*>(T.scol + ST);
+    T.stype = T.scol + ST;
+    T.fid = reinterpret_cast<unsigned*>(T.stype + ST);
     T.ftask = T.fid + FT;
     T.wv = reinterpret_cast<int*>(T.ftask + FT);
     T.nface = T.wv + W;
@@ -881,15 +885,17 @@ __global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s,
             } else if ((ln & 15) == 0) {
                 st(T.sdir + 3 * (2 * wp + side), dd);
                 T.scol[2 * wp + side] = up ? b : a;
+                T.stype[2 * wp + side] = c.type;
             }
         } else if (ln < 2) {
             T.scol[2 * wp + ln] = -1;
         }
         __syncthreads();
-        // warp 0: the posted supports, one per lane
-        if (wp == 0 && ln < 2 * W) {
+        // the posted supports, one per lane, each collider type on warp (type % W), so that the
+        // warps run different types' FP64 paths side by side
+        if (ln < 2 * W) {
             const int ci = T.scol[ln];
-            if (ci >= 0) {
+            if (ci >= 0 && T.stype[ln] % W == wp) {
                 Col<double> c;
                 load_col(s, ci, c);
                 st(T.sres + 3 * ln, support(c, s, ld(T.sdir + 3 * ln)));

@@ -126,72 +126,14 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
     }
 }
 
-// R, one lane per slot of the order (see the top of this file).  The grid
-// covers the capacity; slots at and beyond the pair count are flagged 0.
-template <int BLOCK, bool MESH>
-__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_r(d3d_store s, const int32_t* __restrict__ i1,
-                                                        const int32_t* __restrict__ i2,
-                                                        const int32_t* __restrict__ order, int64_t cap,
-                                                        const int64_t* __restrict__ n_dev, d3d_gjk_options opt,
-                                                        const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
-    // p and q of up to five rows per lane: element e of row j at [(6 j + e) BLOCK]
-    __shared__ double rows[30 * BLOCK];
-    const int64_t n = n_dev ? *n_dev : cap;
-    const int64_t slot = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
-    if (slot >= cap) return;
-    int32_t pid = 0;
-    int outcome = PA_FAILED, nr = 0, it_a = 0;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (slot < n) {
-        pid = order ? order[slot] : (int32_t)slot;
-        v = hand[pid].v;
-        outcome = __float_as_int(v.w) & 0xff;
-        nr = (__float_as_int(v.w) >> 8) & 0xff;
-        it_a = handoff_iters(v);
-    }
-    const bool mine = outcome == PA_SEPARATED || outcome == PA_TOUCHING;  // R or B finishes it
-    const bool rows_ok = mine && nr >= 1 && nr <= 4;
-    const bool sep = rows_ok && outcome == PA_SEPARATED && nr <= 3;
-    const bool touch = rows_ok && outcome == PA_TOUCHING && nr == 4;
-    int a = 0, b = 0;
-    if (rows_ok) {
-        a = i1[pid];
-        b = i2[pid];
-    }
-    // the rows in FP64, then the gap row of a separated pair along -v
-    const int count = rows_ok ? nr + (sep ? 1 : 0) : 0;
-    double* my = rows + threadIdx.x;
-#pragma unroll 1
-    for (int j = 0; j < 5; ++j) {
-        if (j < count) {
-            d3 d;
-            float4 f = make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));  // the gap row: no vertices known
-            if (j < nr) {
-                f = hand[pid].d[j];
-                d = mk((double)f.x, (double)f.y, (double)f.z);
-            } else {
-                d = mk(-(double)v.x, -(double)v.y, -(double)v.z);
-            }
-            // the polytope vertices phase A took along this row's direction are read, not searched again
-            d3 p, q;
-#pragma unroll 1
-            for (int k = 0; k < 2; ++k) {
-                Col<double> c;
-                load_col(s, k ? b : a, c);
-                const d3 x = RefineSupportT<MESH>::eval_at(c, s, k ? -d : d, handoff_vertex(f, k));
-                if (k)
-                    q = x;
-                else
-                    p = x;
-            }
-            my[(6 * j + 0) * BLOCK] = p.x;
-            my[(6 * j + 1) * BLOCK] = p.y;
-            my[(6 * j + 2) * BLOCK] = p.z;
-            my[(6 * j + 3) * BLOCK] = q.x;
-            my[(6 * j + 4) * BLOCK] = q.y;
-            my[(6 * j + 5) * BLOCK] = q.z;
-        }
-    }
+// R's checks and outputs for one pair, its FP64 rows at my[(6 j + e) BLOCK]
+// (the rows of separated pairs end with the gap row).  Run by the thread the
+// block's regrouping gave the pair, which may not be the one that read it.
+template <int BLOCK>
+__device__ __forceinline__ void r_finish(const double* my, int nr, bool sep, bool touch, float4 v, int it_a,
+                                         int32_t pid, int64_t slot, const d3d_gjk_options& opt, const DistanceOut& o,
+                                         const Lists& lists) {
+    const bool rows_ok = sep || touch;
     auto row_p = [&](int j) { return mk(my[(6 * j) * BLOCK], my[(6 * j + 1) * BLOCK], my[(6 * j + 2) * BLOCK]); };
     auto row_q = [&](int j) {
         return mk(my[(6 * j + 3) * BLOCK], my[(6 * j + 4) * BLOCK], my[(6 * j + 5) * BLOCK]);
@@ -267,7 +209,7 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_r(d3d_store s, const int32_
         o.status[pid] = (int8_t)D3D_STATUS_OK;
         // the gap row counts as the FP64 iteration that closed the bracket
         if (o.iterations) o.iterations[pid] = it_a + (sep ? 1 : 0);
-    } else if (mine) {
+    } else {
         EndRecord& e = lists.records[pid];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -283,8 +225,140 @@ __global__ void __launch_bounds__(BLOCK) k_gjk_mixed_r(d3d_store s, const int32_
         }
         e.n = rows_ok ? nr : 0;
     }
-    lists.run_flag[slot] = (int8_t)(mine && !done);
+    lists.run_flag[slot] = (int8_t)(!done);
     lists.run_pid[slot] = pid;
+}
+
+// R, one lane per slot of the order (see the top of this file).  The grid
+// covers the capacity; slots at and beyond the pair count are flagged 0.
+// Each lane evaluates its pair's FP64 rows; the checks that follow run in
+// different branches for touching pairs and for separated pairs of one, two
+// and three rows, so the block regroups them: the pairs are sorted by that
+// class (counting sort over the block, the rows staying where they are in
+// shared memory) and thread t runs the t-th pair's checks (r_finish).
+template <int BLOCK, bool MESH>
+__global__ void __launch_bounds__(BLOCK) k_gjk_mixed_r(d3d_store s, const int32_t* __restrict__ i1,
+                                                        const int32_t* __restrict__ i2,
+                                                        const int32_t* __restrict__ order, int64_t cap,
+                                                        const int64_t* __restrict__ n_dev, d3d_gjk_options opt,
+                                                        const Handoff* __restrict__ hand, DistanceOut o, Lists lists) {
+    constexpr int W = BLOCK / 32;
+    constexpr unsigned kAll = 0xffffffffu;
+    // p and q of up to five rows per lane: element e of row j at [(6 j + e) BLOCK]
+    __shared__ double rows[30 * BLOCK];
+    __shared__ float4 tv[BLOCK];       // the handoff's v of each lane's pair
+    __shared__ int tpid[BLOCK], tita[BLOCK], tcls[BLOCK];
+    __shared__ unsigned short tperm[BLOCK];
+    __shared__ int cnt[4 * W];
+    const int64_t n = n_dev ? *n_dev : cap;
+    const int64_t slot = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+    const int ln = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    int32_t pid = 0;
+    int outcome = PA_FAILED, nr = 0, it_a = 0;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (slot < n && slot < cap) {
+        pid = order ? order[slot] : (int32_t)slot;
+        v = hand[pid].v;
+        outcome = __float_as_int(v.w) & 0xff;
+        nr = (__float_as_int(v.w) >> 8) & 0xff;
+        it_a = handoff_iters(v);
+    }
+    const bool mine = outcome == PA_SEPARATED || outcome == PA_TOUCHING;  // R or B finishes it
+    const bool rows_ok = mine && nr >= 1 && nr <= 4;
+    const bool sep = rows_ok && outcome == PA_SEPARATED && nr <= 3;
+    const bool touch = rows_ok && outcome == PA_TOUCHING && nr == 4;
+    int a = 0, b = 0;
+    if (rows_ok) {
+        a = i1[pid];
+        b = i2[pid];
+    }
+    // the rows in FP64, then the gap row of a separated pair along -v
+    const int count = rows_ok ? nr + (sep ? 1 : 0) : 0;
+    double* my = rows + threadIdx.x;
+#pragma unroll 1
+    for (int j = 0; j < 5; ++j) {
+        if (j < count) {
+            d3 d;
+            float4 f = make_float4(0.f, 0.f, 0.f, __uint_as_float(0xffffffffu));  // the gap row: no vertices known
+            if (j < nr) {
+                f = hand[pid].d[j];
+                d = mk((double)f.x, (double)f.y, (double)f.z);
+            } else {
+                d = mk(-(double)v.x, -(double)v.y, -(double)v.z);
+            }
+            // the polytope vertices phase A took along this row's direction are read, not searched again
+            d3 p, q;
+#pragma unroll 1
+            for (int k = 0; k < 2; ++k) {
+                Col<double> c;
+                load_col(s, k ? b : a, c);
+                const d3 x = RefineSupportT<MESH>::eval_at(c, s, k ? -d : d, handoff_vertex(f, k));
+                if (k)
+                    q = x;
+                else
+                    p = x;
+            }
+            my[(6 * j + 0) * BLOCK] = p.x;
+            my[(6 * j + 1) * BLOCK] = p.y;
+            my[(6 * j + 2) * BLOCK] = p.z;
+            my[(6 * j + 3) * BLOCK] = q.x;
+            my[(6 * j + 4) * BLOCK] = q.y;
+            my[(6 * j + 5) * BLOCK] = q.z;
+        }
+    }
+    // class of the checks: 0 touching (four rows), 1-3 separated with that many rows, 4 none
+    const int cls = touch ? 0 : (sep ? nr : 4);
+    if (cls == 4 && slot < cap) {
+        // a pair R does not check goes to B as it is (rows of a pair of another shape are kept), or
+        // is not R's at all
+        if (mine) {
+            EndRecord& e = lists.records[pid];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (j < nr && rows_ok) {
+                    e.pq[j][0] = my[(6 * j) * BLOCK];
+                    e.pq[j][1] = my[(6 * j + 1) * BLOCK];
+                    e.pq[j][2] = my[(6 * j + 2) * BLOCK];
+                    e.pq[j][3] = my[(6 * j + 3) * BLOCK];
+                    e.pq[j][4] = my[(6 * j + 4) * BLOCK];
+                    e.pq[j][5] = my[(6 * j + 5) * BLOCK];
+                }
+            }
+            e.n = rows_ok ? nr : 0;
+        }
+        lists.run_flag[slot] = (int8_t)mine;
+        lists.run_pid[slot] = pid;
+    }
+    tv[threadIdx.x] = v;
+    tpid[threadIdx.x] = pid;
+    tita[threadIdx.x] = it_a;
+    tcls[threadIdx.x] = cls | (nr << 8);
+    int rank = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const unsigned m = __ballot_sync(kAll, cls == c);
+        if (cls == c) rank = __popc(m & ((1u << ln) - 1u));
+        if (ln == 0) cnt[c * W + wp] = __popc(m);
+    }
+    __syncthreads();
+    int t = 0, ntask = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const int k = cnt[c * W + w];
+            if (c < cls || (c == cls && w < wp)) t += k;
+            ntask += k;
+        }
+    if (cls < 4) tperm[t + rank] = (unsigned short)threadIdx.x;
+    __syncthreads();
+    if ((int)threadIdx.x < ntask) {
+        const int owner = tperm[threadIdx.x];
+        const int x = tcls[owner];
+        const int c = x & 0xff, rn = x >> 8;
+        r_finish<BLOCK>(rows + owner, rn, c >= 1, c == 0, tv[owner], tita[owner], tpid[owner],
+                        (int64_t)blockIdx.x * BLOCK + owner, opt, o, lists);
+    }
 }
 
 // B over R's run list, in the type-sorted order.

@@ -179,6 +179,29 @@ __device__ __forceinline__ int half_argmax(const T* verts, int off, int nv, V3<T
     return bi;
 }
 
+// The FP32 instance with two warp reductions on order-preserving keys: the
+// largest product, then the lowest index holding it (-0 counts as +0; a NaN
+// product loses to every number).
+template <>
+__device__ __forceinline__ int half_argmax<float>(const float* verts, int off, int nv, f3 d, unsigned hm) {
+    unsigned best = 0u;
+    int bi = 0x7fffffff;
+    bool any = false;
+    for (int k = lane_id() & 15; k < nv; k += 16) {
+        const f3 v = load_vertex(verts, off + k);
+        const float x = dot102(v.x, v.y, v.z, d.x, d.y, d.z);
+        const unsigned u = x == 0.f ? 0u : __float_as_uint(x);
+        const unsigned key = x != x ? 0u : ((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+        if (!any || key > best) {
+            best = key;
+            bi = k;
+            any = true;
+        }
+    }
+    const unsigned m = __reduce_max_sync(hm, any ? best : 0u);
+    return (int)__reduce_min_sync(hm, (any && best == m) ? (unsigned)bi : 0xffffffffu);
+}
+
 __device__ __forceinline__ unsigned half_mask() { return (lane_id() & 16) ? 0xffff0000u : 0x0000ffffu; }
 
 // w = s_a(d) - s_b(-d) in FP32: the lower half warp evaluates collider a, the
@@ -311,6 +334,29 @@ __device__ __forceinline__ int closest_face(const Poly<T>& P, int nslots) {
         }
     }
     return bs;
+}
+
+// The same for the FP32 polytope with two warp reductions (REDUX) on
+// order-preserving 32-bit keys of the offsets instead of five shuffle rounds:
+// the smallest key, then the lowest slot holding it.  (-0 counts as +0; a NaN
+// offset loses to every number.)
+template <>
+__device__ __forceinline__ int closest_face<float>(const Poly<float>& P, int nslots) {
+    unsigned best = 0xffffffffu;
+    int bs = 0x7fffffff;
+    for (int f = lane_id(); f < nslots; f += 32) {
+        if (P.fv[f] == kDead) continue;
+        const float d = P.fn[f].w;
+        const unsigned u = d == 0.f ? 0u : __float_as_uint(d);
+        const unsigned key = d != d ? 0xfffffffeu : ((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+        if (key < best) {
+            best = key;
+            bs = f;
+        }
+    }
+    const unsigned m = __reduce_min_sync(kFull, best);
+    if (m == 0xffffffffu) return -1;
+    return (int)__reduce_min_sync(kFull, best == m ? (unsigned)bs : 0xffffffffu);
 }
 
 // Outcome of the FP32 search for one pair.

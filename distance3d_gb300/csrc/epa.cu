@@ -348,6 +348,55 @@ __device__ __forceinline__ unsigned long long dist_key(double d) {
     return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
+// The warp's smallest (key, index): the smallest key, then the smallest index
+// holding it, by REDUX on the keys' 32-bit halves (no shuffle rounds).
+__device__ __forceinline__ void warp_min_key(unsigned long long& k, int& i) {
+    const unsigned hi = __reduce_min_sync(kWarpAll, (unsigned)(k >> 32));
+    const unsigned lo = __reduce_min_sync(kWarpAll, (unsigned)(k >> 32) == hi ? (unsigned)k : 0xffffffffu);
+    const unsigned long long m = ((unsigned long long)hi << 32) | lo;
+    i = (int)__reduce_min_sync(kWarpAll, k == m ? (unsigned)i : 0xffffffffu);
+    k = m;
+}
+
+// Ordering key of a support product for the first-maximum scans: unsigned
+// order equals the order of the doubles (-0 as +0); a NaN is 0, below every
+// number, so that it never beats a number.  Integer work only, which keeps the
+// scans off the FP64 pipe.
+__device__ __forceinline__ unsigned long long max_key(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    if ((u << 1) > 0xffe0000000000000ull) return 0ull;
+    if ((u << 1) == 0ull) return 0x8000000000000000ull;
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// First maximum of V . d over a box's or hull's vertices by the 16 lanes of
+// this half warp (np.argmax): a NaN at vertex 0 wins, later NaNs never do.
+__device__ __forceinline__ int half_first_max(const d3d_store& st, const Col<double>& c, d3 dd, unsigned half) {
+    const int h = lane_of() & 15;
+    unsigned long long bk = 0ull;
+    int bj = 0x7fffffff;
+    bool nan0 = false;
+    for (int k = h; k < c.nv; k += 16) {
+        const d3 v = load_vertex(st.verts64, c.off + k);
+        const unsigned long long key = max_key(dot102(v.x, v.y, v.z, dd.x, dd.y, dd.z));
+        if (k == 0 && key == 0ull) nan0 = true;
+        if (key > bk) {
+            bk = key;
+            bj = k;
+        }
+    }
+    for (int m = 8; m; m >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(half, bk, m);
+        const int oi = __shfl_xor_sync(half, bj, m);
+        if (ok > bk || (ok == bk && oi < bj)) {
+            bk = ok;
+            bj = oi;
+        }
+    }
+    const bool any_nan0 = __ballot_sync(half, nan0) != 0u;
+    return (c.nv == 1 || any_nan0 || bj >= c.nv) ? 0 : bj;
+}
+
 // w = s_a(d) - s_b(-d) with the reference's supports: lanes 0-15 evaluate
 // collider a, lanes 16-31 collider b; a box or hull's first-maximum vertex is
 // found by the 16 lanes of its half (np.argmax).  Every lane returns w.
@@ -365,33 +414,9 @@ __device__ d3 minkowski_exact_warp(const d3d_store& st, int a, int b, d3 d) {
         if (c.nv < 1) {
             s = mk(double(NAN), double(NAN), double(NAN));
         } else {
-            // first maximum of V . d (dot102); a NaN at vertex 0 wins, later NaNs never do.  (The
-            // FP32 filter of hull_argmax_filtered does not pay here: with 16 lanes a typical hull
-            // takes a few FP64 rounds, about what its FP32 passes and reductions cost.)
-            const int h = ln & 15;
-            double bv = 0.0;
-            int bi = -1;
-            bool nan0 = false;
-            for (int k = h; k < c.nv; k += 16) {
-                const d3 v = load_vertex(st.verts64, c.off + k);
-                const double x = dot102(v.x, v.y, v.z, dd.x, dd.y, dd.z);
-                if (k == 0 && x != x) nan0 = true;
-                if (bi < 0 ? x == x : x > bv) {
-                    bv = x;
-                    bi = k;
-                }
-            }
-            for (int m = 8; m; m >>= 1) {
-                const double ov = __shfl_xor_sync(half, bv, m);
-                const int oi = __shfl_xor_sync(half, bi, m);
-                if (oi >= 0 && (bi < 0 || ov > bv || (ov == bv && oi < bi))) {
-                    bv = ov;
-                    bi = oi;
-                }
-            }
-            const bool any_nan0 = __ballot_sync(half, nan0) != 0u;
-            const int k = (c.nv == 1 || any_nan0 || bi < 0 || bi >= c.nv) ? 0 : bi;
-            s = add_margin(c, load_vertex(st.verts64, c.off + k), dd);
+            // (The FP32 filter of hull_argmax_filtered does not pay here: with 16 lanes a typical
+            // hull takes a few FP64 rounds, about what its FP32 passes and reductions cost.)
+            s = add_margin(c, load_vertex(st.verts64, c.off + half_first_max(st, c, dd, half)), dd);
         }
     } else {
         s = support(c, st, dd);
@@ -454,14 +479,7 @@ __device__ int epa_pair_warp(const d3d_store& store, int a, int b, const double*
                 bi = i;
             }
         }
-        for (int m = 16; m; m >>= 1) {
-            const unsigned long long ok = __shfl_xor_sync(kWarpAll, bk, m);
-            const int oi = __shfl_xor_sync(kWarpAll, bi, m);
-            if (ok < bk || (ok == bk && oi < bi)) {
-                bk = ok;
-                bi = oi;
-            }
-        }
+        warp_min_key(bk, bi);
         closest = (K[0] == ~0ull || bk == ~0ull) ? 0 : bi;
         const double md = P.dist(closest);
         const d3 sd = P.normal(closest);
@@ -829,14 +847,7 @@ __global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s,
                     bi = i;
                 }
             }
-            for (int m = 16; m; m >>= 1) {
-                const unsigned long long ok = __shfl_xor_sync(kWarpAll, bk, m);
-                const int oi = __shfl_xor_sync(kWarpAll, bi, m);
-                if (ok < bk || (ok == bk && oi < bi)) {
-                    bk = ok;
-                    bi = oi;
-                }
-            }
+            warp_min_key(bk, bi);
             closest = (K[0] == ~0ull || bk == ~0ull) ? 0 : bi;
             md = P.dist(closest);
             sd = P.normal(closest);
@@ -853,30 +864,7 @@ __global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s,
                 if (c.nv < 1) {
                     r = mk(double(NAN), double(NAN), double(NAN));
                 } else {
-                    const int h = ln & 15;
-                    double bv = 0.0;
-                    int bj = -1;
-                    bool nan0 = false;
-                    for (int k = h; k < c.nv; k += 16) {
-                        const d3 v = load_vertex(s.verts64, c.off + k);
-                        const double x = dot102(v.x, v.y, v.z, dd.x, dd.y, dd.z);
-                        if (k == 0 && x != x) nan0 = true;
-                        if (bj < 0 ? x == x : x > bv) {
-                            bv = x;
-                            bj = k;
-                        }
-                    }
-                    for (int m = 8; m; m >>= 1) {
-                        const double ov = __shfl_xor_sync(half, bv, m);
-                        const int oi = __shfl_xor_sync(half, bj, m);
-                        if (oi >= 0 && (bj < 0 || ov > bv || (ov == bv && oi < bj))) {
-                            bv = ov;
-                            bj = oi;
-                        }
-                    }
-                    const bool any_nan0 = __ballot_sync(half, nan0) != 0u;
-                    const int k = (c.nv == 1 || any_nan0 || bj < 0 || bj >= c.nv) ? 0 : bj;
-                    r = add_margin(c, load_vertex(s.verts64, c.off + k), dd);
+                    r = add_margin(c, load_vertex(s.verts64, c.off + half_first_max(s, c, dd, half)), dd);
                 }
                 if ((ln & 15) == 0) {
                     st(T.sres + 3 * (2 * wp + side), r);

@@ -773,7 +773,12 @@ __global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s,
     int a = 0, b = 0, nf = 0, closest = 0, nv = 0, it = 0, stt = 0;
     bool have = false, exhausted = false;
     d3 mtv = mk(0.0, 0.0, 0.0);
+    // The block's shared work (posted supports, new faces) goes to warps by a rotation that
+    // changes every round and differs between the blocks of an SM, so that it does not always
+    // fall on the same warp slot and with it on one sub-partition's FP64 pipe.
+    int rot = (int)(((unsigned)blockIdx.x * (unsigned)W) / gridDim.x) % W;
     while (true) {
+        rot = rot + 1 == W ? 0 : rot + 1;
         // a warp without a pair takes the next one
         bool fresh = false;
         if (!have && !exhausted) {
@@ -879,11 +884,13 @@ __global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s,
             T.scol[2 * wp + ln] = -1;
         }
         __syncthreads();
-        // the posted supports, one per lane, each collider type on warp (type % W), so that the
-        // warps run different types' FP64 paths side by side
+        // the posted supports, one per lane, each collider type on its own warp where W allows
+        // (the analytic types numbered 0-7, rotated), so that the warps run different types'
+        // FP64 paths side by side
         if (ln < 2 * W) {
             const int ci = T.scol[ln];
-            if (ci >= 0 && T.stype[ln] % W == wp) {
+            const int ty = T.stype[ln];
+            if (ci >= 0 && (ty - (ty > D3D_BOX) - (ty > D3D_HULL) + rot) % W == wp) {
                 Col<double> c;
                 load_col(s, ci, c);
                 st(T.sres + 3 * ln, support(c, s, ld(T.sdir + 3 * ln)));
@@ -987,7 +994,8 @@ __global__ void __launch_bounds__(32 * W, 16 / W) k_epa_exact_block(d3d_store s,
         fbase = __shfl_sync(kWarpAll, fbase, 0);
         if (post && ln < ne) T.ftask[fbase + ln] = (unsigned)wp | ((unsigned)ln << 8);
         __syncthreads();
-        for (int t = threadIdx.x; t < *T.nface; t += 32 * W) {
+        // chunk c of 32 tasks on warp (c + rot) % W
+        for (int t = 32 * ((wp - rot + W) % W) + ln; t < *T.nface; t += 32 * W) {
             const unsigned task = T.ftask[t];
             const int q = task & 0xff, k = task >> 8;
             const WarpPoly Q = WarpPoly::at(smem_blk + q * pbytes, o.max_faces, o.max_loose_edges,

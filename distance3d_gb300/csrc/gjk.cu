@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_gjk_distance_f64_grouped
     int64_t n, const unsigned long long* __restrict__ n_dev, unsigned long long* __restrict__ cursor,
     d3d_gjk_options opt, DistanceOut o) {
     constexpr int W = BLOCK / 32;
+    static_assert((BLOCK & (BLOCK - 1)) == 0, "the solve rotation masks with BLOCK - 1");
     constexpr unsigned kAll = 0xffffffffu;
     __shared__ double rows[24 * BLOCK];  // the simplex P/Q rows of each lane
     __shared__ double ty[12 * BLOCK];    // task t: row r, coordinate c at [(3 r + c) BLOCK + t]
@@ -115,7 +116,12 @@ __global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_gjk_distance_f64_grouped
     int a = 0, b = 0;
     bool have = false, exhausted = false, bad = false;
     WarpChunk chunk;
+    // the sorted solves go to the warps by a rotation that changes every round and differs
+    // between the blocks of an SM, so that the tetrahedra do not always fall on the same warp
+    // slot and with it on one sub-partition's FP64 pipe
+    int rot = (int)(((unsigned)blockIdx.x * (unsigned)W) / gridDim.x) % W;
     while (true) {
+        rot = rot + 1 == W ? 0 : rot + 1;
         __syncwarp();
         const bool want = !have && !exhausted;
         const long long slot = fetch_slot_chunked(cursor, want, chunk, kAll, kChunk, n);
@@ -179,8 +185,8 @@ __global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_gjk_distance_f64_grouped
             tmeta[t] = g.S.n | ((int)threadIdx.x << 8);
         }
         __syncthreads();
-        if ((int)threadIdx.x < ntask) {
-            const int u = threadIdx.x;
+        const int u = (threadIdx.x + 32 * rot) & (BLOCK - 1);
+        if (u < ntask) {
             Simplex<double> S;
             const int meta = tmeta[u];
             S.n = meta & 0xff;

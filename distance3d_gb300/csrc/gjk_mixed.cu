@@ -74,11 +74,12 @@ struct Lists {
 // slots a warp claims from the type-sorted order at a time
 constexpr int kChunk = 32;
 
-// Phase A's register budget: at least 12 resident warps per SM (16 for
-// 256-thread blocks), which ptxas would otherwise trade for a few more
-// registers per thread.
+// Phase A's register budget: 16 resident warps per SM (128 registers), its
+// simplex P/Q rows in shared memory (ARows).  At 1M pairs: 3.9 ms for the
+// mixed GJK, against 4.2 with 12 warps and the rows in registers, 4.2 with 20
+// warps and 4.9 with 24 (more spilled registers).
 template <int BLOCK>
-constexpr int phase_a_min_blocks() { return BLOCK == 256 ? 2 : 384 / BLOCK; }
+constexpr int phase_a_min_blocks() { return 512 / BLOCK; }
 
 template <int BLOCK, bool MESH>
 __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixed_a(d3d_store s, const int32_t* __restrict__ i1,
@@ -88,7 +89,9 @@ __global__ void __launch_bounds__(BLOCK, phase_a_min_blocks<BLOCK>()) k_gjk_mixe
                                                         float max_d2, int max_iter, Handoff* __restrict__ hand,
                                                         DistanceOut out, Lists lists) {
     if (n_dev) n = *n_dev;
-    PhaseALoop L;
+    __shared__ float4 arows[4 * BLOCK];
+    PhaseALoop<ARows<BLOCK>> L;
+    L.S.R.base = arows + threadIdx.x;
     int64_t pid = 0;
     int a = 0, b = 0;
     bool need = true, bad = false;

@@ -253,15 +253,32 @@ __device__ __forceinline__ int handoff_vertex(float4 d, int k) {
 // The Jolt loop (gjk_step) in FP32 on the FP32 mirror; row j of S.P holds
 // the search direction that produced row j of S.Y, and row j of S.Q the
 // vertices its polytope supports took (bits of a float, moved with the row).
+// Phase A's P/Q rows in shared memory, one float4 per row: the FP32
+// direction that produced the row (P) and, in w, the vertex ids its supports
+// took (Q.x; Q.y and Q.z are zero).  Element (row r) of the lane at base[r kStride].
+template <int kStride>
+struct ARows {
+    float4* base;
+    __device__ __forceinline__ void put(int k, f3 p, f3 q) { base[k * kStride] = make_float4(p.x, p.y, p.z, q.x); }
+    __device__ __forceinline__ void move(int dst, int src) { base[dst * kStride] = base[src * kStride]; }
+    __device__ __forceinline__ f3 p(int k) const {
+        const float4 r = base[k * kStride];
+        return mk(r.x, r.y, r.z);
+    }
+    __device__ __forceinline__ f3 q(int k) const { return mk(base[k * kStride].w, 0.f, 0.f); }
+};
+
+template <typename Rows>
 struct PhaseALoop {
-    Simplex<float> S;
+    Simplex<float, Rows> S;
     f3 dir;
     f3 v;
     float vl, prev;
     int it;
 };
 
-__device__ __forceinline__ void pa_begin(PhaseALoop& L) {
+template <typename Rows>
+__device__ __forceinline__ void pa_begin(PhaseALoop<Rows>& L) {
     simplex_clear(L.S);
     L.dir = mk(1.f, 0.f, 0.f);
     L.v = L.dir;
@@ -271,8 +288,8 @@ __device__ __forceinline__ void pa_begin(PhaseALoop& L) {
 }
 
 // one iteration; -1 while running, else a PhaseAOutcome
-template <bool MESH = true>
-__device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a, int b, float tol_sq, float max_d2,
+template <bool MESH, typename Rows>
+__device__ __forceinline__ int pa_step(PhaseALoop<Rows>& L, const d3d_store& s, int a, int b, float tol_sq, float max_d2,
                                        int max_iter) {
     const JoltEps<float> E = fp32_eps();
     if (L.it >= max_iter) return PA_FAILED;
@@ -304,7 +321,7 @@ __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a,
     f3 nv;
     float nl;
     int set;
-    if (closest_to_origin<float, RegRows<float>, true>(L.S, L.prev, E, nv, nl, set)) {
+    if (closest_to_origin<float, Rows, true>(L.S, L.prev, E, nv, nl, set)) {
         L.dir = nv;
         L.vl = nl;
     } else {
@@ -322,12 +339,16 @@ __device__ __forceinline__ int pa_step(PhaseALoop& L, const d3d_store& s, int a,
     return -1;
 }
 
-__device__ __forceinline__ Handoff pa_handoff(const PhaseALoop& L, int outcome) {
+template <typename Rows>
+__device__ __forceinline__ Handoff pa_handoff(const PhaseALoop<Rows>& L, int outcome) {
     Handoff h;
     int it = L.it < 0xffff ? L.it : 0xffff;
     h.v = make_float4(L.v.x, L.v.y, L.v.z, __int_as_float(outcome | (L.S.n << 8) | (it << 16)));
 #pragma unroll
-    for (int j = 0; j < 4; ++j) h.d[j] = make_float4(L.S.R.P[j].x, L.S.R.P[j].y, L.S.R.P[j].z, L.S.R.Q[j].x);
+    for (int j = 0; j < 4; ++j) {
+        const f3 p = L.S.R.p(j);
+        h.d[j] = make_float4(p.x, p.y, p.z, L.S.R.q(j).x);
+    }
     return h;
 }
 

@@ -298,7 +298,9 @@ typedef struct {
 int d3d_chain_fk(const d3d_chain* chain, const double* q, int64_t n_configs, double* poses, void* stream);
 
 /* Launch parameters of the batch kernels (process-wide, per library load).
- * gjk_block: threads per block of the GJK kernels (64, 128 or 256);
+ * gjk_block: threads per block of the GJK kernels (64, 128 or 256; the
+ * plain FP64 GJK, whose blocks solve their simplices together, runs 128 for
+ * 256);
  * gjk_warps_per_sm: resident warps per SM of their persistent grids (0: as
  * many as fit); epa_warps: pairs (warps) per block of the warp EPA (2, 4 or
  * 8); sort_min: batches of at least this many pairs are sorted by collider

@@ -44,9 +44,9 @@ EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 # 131,072-pair workload (k_gjk_mixed_a + _r + _b + _end per pair; k_epa_warp
 # + k_epa_refine per EPA pair, 38,814 of them); traffic grows in proportion
 # to the pairs
-NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78438400 + 3263744 + 112407040 + 8471040 + 16013056 + 0 + 7311872
-                                         + 184320) / 131072,
-                           "epa_mixed": (33029632 + 32000 + 34504960 + 17408) / 38814}
+NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78589696 + 3613952 + 112622080 + 10178304 + 16011520 + 256 + 7312384
+                                         + 185600) / 131072,
+                           "epa_mixed": (33024000 + 32512 + 34504192 + 13568) / 38814}
 # this library's kernels per timed mixed step (one graph replay), used only
 # when the graph cannot be read back (d3d_graph_kernel_nodes): k_pair_keys,
 # k_gjk_mixed_a, k_gjk_mixed_r, k_gjk_mixed_b, k_gjk_mixed_end,

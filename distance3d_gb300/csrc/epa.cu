@@ -1097,7 +1097,8 @@ bool exact_warp_supported(const d3d_epa_options& o) {
 // memory allows; 0 if neither fits.  (At the bench's options, 310k pairs:
 // W = 4 61.7 ms, W = 2 70.0 ms, W = 8 69.3 ms, W = 16 78.4 ms, one warp per
 // block 84.1 ms: wider blocks share more supports and normals but wait longer
-// at their barriers, narrower ones share less.)
+// at their barriers, narrower ones share less.  With the shared work rotated
+// over the warps: W = 4 55.2 ms, W = 8 56.6 ms.)
 int exact_block_warps(const d3d_epa_options& o) {
     if (!exact_warp_supported(o)) return 0;
     for (int w = 4; w >= 2; w /= 2)

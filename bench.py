@@ -360,7 +360,7 @@ def run_reference(args):
     return 0
 
 
-def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=8192, slots=8, repeats=3):
+def serve_report(store, i1_np, i2_np, seconds, seed=7, capacity=4096, slots=16, repeats=3):
     """The continuous-batching server (the library's native server) on the
     same resident store: peak pairs/s with a burst of requests all arriving
     at once, then Poisson arrivals at 50/80/100% of that peak; latency from

@@ -47,6 +47,18 @@ EPA_KW = dict(max_iter=64, max_loose_edges=128, max_faces=256, epsilon=1e-8)
 NCU_DRAM_BYTES_PER_PAIR = {"gjk_mixed": (78589696 + 3613952 + 112622080 + 10178304 + 16011520 + 256 + 7312384
                                          + 185600) / 131072,
                            "epa_mixed": (33024000 + 32512 + 34504192 + 13568) / 38814}
+# Pipe and issue activity (fractions of peak, ncu --set full at 131,072
+# pairs) of the mixed kernels, reported beside the model-FLOP fraction: the
+# model counts only the geometry's arithmetic, while the kernels are bound by
+# instruction issue (EPA search) or latency (phase A), and ncu's FMA-pipe
+# share counts every FP32 instruction, compares and selects included
+NCU_PIPE_ACTIVITY = {
+    "gjk_mixed": {"k_gjk_mixed_a": {"fma_pipe": 0.193, "fp64_pipe": 0.0, "issue": 0.451},
+                  "k_gjk_mixed_r": {"fma_pipe": 0.019, "fp64_pipe": 0.686, "issue": 0.102},
+                  "k_gjk_mixed_b": {"fma_pipe": 0.008, "fp64_pipe": 0.503, "issue": 0.089},
+                  "k_gjk_mixed_end": {"fma_pipe": 0.003, "fp64_pipe": 0.488, "issue": 0.050}},
+    "epa_mixed": {"k_epa_warp<float>": {"fma_pipe": 0.230, "fp64_pipe": 0.072, "issue": 0.749},
+                  "k_epa_refine": {"fma_pipe": 0.029, "fp64_pipe": 0.290, "issue": 0.089}}}
 # this library's kernels per timed mixed step (one graph replay), used only
 # when the graph cannot be read back (d3d_graph_kernel_nodes): k_pair_keys,
 # k_gjk_mixed_a, k_gjk_mixed_r, k_gjk_mixed_b, k_gjk_mixed_end,
@@ -918,7 +930,8 @@ def run_ours(args):
     times = {"gjk_mixed": gjk_mixed, "epa_mixed": epa_mixed, "gjk_fp64": gjk_fp64, "epa_fp64": epa_fp64}
     peak_src = "FMA chains measured in this run (libd3d_peak)"
     compute_roofline = {}
-    for key, kernel, peak in (("gjk_fp64", "k_gjk_distance_f64", peak64), ("epa_fp64", "k_epa_exact_warp", peak64),
+    for key, kernel, peak in (("gjk_fp64", "k_gjk_distance_f64_grouped", peak64),
+                              ("epa_fp64", "k_epa_exact_block", peak64),
                               ("gjk_mixed", "k_gjk_mixed_a/_r/_b/_end", peak32),
                               ("epa_mixed", "k_epa_warp<float> + k_epa_refine", peak32)):
         compute_roofline[key] = {"kernel": kernel, "bound": "fp64 pipe" if peak is peak64 else "fp32 pipe",
@@ -956,6 +969,11 @@ def run_ours(args):
         roofline = dict(hbm, bound="hbm", kernel=dom, traffic=traffic, pipe=pipe)
     roofline["traffic_source"] = ("ncu dram__bytes_read.sum + dram__bytes_write.sum at 131,072 pairs, "
                                   "scaled by the pair count")
+    roofline["ncu_activity"] = {"per_kernel": NCU_PIPE_ACTIVITY[key],
+                                "source": "ncu --set full at 131,072 pairs (profiles/ncu_full_gjk_epa_131k_pairs.md)",
+                                "note": "frac is model FLOPs over the measured FMA peak; the kernels issue many "
+                                        "more instructions than the model counts, and instruction issue is what "
+                                        "binds the EPA search"}
 
     line = None
     if rank == 0:

@@ -165,20 +165,11 @@ __global__ void k_support(d3d_store s, const int32_t* __restrict__ idx, const do
 __device__ __forceinline__ double np_min(double a, double b) { return (a != a || a < b) ? a : b; }
 __device__ __forceinline__ double np_max(double a, double b) { return (a != a || a > b) ? a : b; }
 
-// containment.py:6-229, one collider per thread; writes [axis][min,max]
-__global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n, double* __restrict__ out) {
-    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const int ci = idx ? idx[k] : (int)k;
-    if (!index_ok(s, ci)) {  // out of range: NaN, no record read
-        for (int j = 0; j < 6; ++j) out[6 * k + j] = NAN;
-        return;
-    }
-    Col<double> c;
-    load_col(s, ci, c);
+// containment.py:25-229: the box of a collider of an analytic type (the
+// polytopes and meshes are scanned by aabb_scan)
+__device__ void analytic_aabb(const Col<double>& c, double* lo, double* hi) {
     const double* R = c.R;
     const double* t = c.t;
-    double lo[3], hi[3];
     switch (c.type) {
     case D3D_SPHERE:  // :25-44
         for (int i = 0; i < 3; ++i) {
@@ -247,42 +238,125 @@ __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n,
             hi[i] = np_max(t[i] + e * c.p[0], pb);
         }
         break;
-    case D3D_MESH: {  // colliders.py:234-237: t + V R^T (dgemm, order of dot012), min / max
-        if (c.nv < 1) {
-            for (int i = 0; i < 3; ++i) lo[i] = hi[i] = NAN;
-            break;
-        }
-        for (int r = 0; r < c.nv; ++r) {
-            const d3 v = load_vertex(s.verts64, c.off + r);
-            for (int i = 0; i < 3; ++i) {
-                const double w = t[i] + dot012(v.x, v.y, v.z, R[i * 3], R[i * 3 + 1], R[i * 3 + 2]);
-                if (r == 0 || w < lo[i]) lo[i] = w;
-                if (r == 0 || w > hi[i]) hi[i] = w;
+    default:
+        break;
+    }
+}
+
+// Ordering key of a coordinate for the min / max scans: unsigned order equals
+// the order of the doubles, -0 and +0 equal (the scan keeps the first).
+__device__ __forceinline__ unsigned long long coord_key(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    if ((u << 1) == 0ull) return 0x8000000000000000ull;
+    return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// The warp's smallest (key, index): REDUX on the key halves, then on the index.
+__device__ __forceinline__ int warp_first_min(unsigned long long k, int i) {
+    const unsigned hi = __reduce_min_sync(0xffffffffu, (unsigned)(k >> 32));
+    const unsigned lo = __reduce_min_sync(0xffffffffu, (unsigned)(k >> 32) == hi ? (unsigned)k : 0xffffffffu);
+    const unsigned long long m = ((unsigned long long)hi << 32) | lo;
+    return (int)__reduce_min_sync(0xffffffffu, k == m ? (unsigned)i : 0xffffffffu);
+}
+
+// Per axis the minimum and maximum of a polytope's or mesh's coordinates, by
+// the 32 lanes of the warp (every lane calls it with the same collider): box
+// :47-67 and hull :6-22 (np.min / np.max of the vertices), mesh
+// colliders.py:234-237 (t + V R^T, dgemm in the order of dot012).  The values
+// are those of the sequential scan that starts from vertex 0 and replaces on
+// a strict comparison: the first of equal values (-0 and +0 included), a NaN
+// coordinate of vertex 0 kept, later NaNs skipped.  The compares are integer
+// ones, off the FP64 pipe.
+__device__ void aabb_scan(const d3d_store& s, int off, int nv, bool mesh, const double* R, const double* t,
+                          double* lo, double* hi) {
+    const int ln = threadIdx.x & 31;
+    unsigned long long kmin[3], kmax[3];
+    int imin[3], imax[3];
+    double vmin[3], vmax[3], v0[3];
+    for (int i = 0; i < 3; ++i) {
+        kmin[i] = ~0ull;
+        kmax[i] = 0ull;
+        imin[i] = imax[i] = 0x7fffffff;
+        vmin[i] = vmax[i] = v0[i] = 0.0;
+    }
+    for (int r = ln; r < nv; r += 32) {
+        const d3 v = load_vertex(s.verts64, off + r);
+        double w[3] = {v.x, v.y, v.z};
+        if (mesh)
+            for (int i = 0; i < 3; ++i) w[i] = t[i] + dot012(v.x, v.y, v.z, R[i * 3], R[i * 3 + 1], R[i * 3 + 2]);
+        for (int i = 0; i < 3; ++i) {
+            if (r == 0) v0[i] = w[i];
+            if (w[i] != w[i]) continue;
+            const unsigned long long key = coord_key(w[i]);
+            if (key < kmin[i]) {
+                kmin[i] = key;
+                imin[i] = r;
+                vmin[i] = w[i];
+            }
+            if (key > kmax[i]) {
+                kmax[i] = key;
+                imax[i] = r;
+                vmax[i] = w[i];
             }
         }
-        break;
     }
-    default: {  // box :47-67, hull :6-22
-        if (c.nv < 1) {  // rejected by d3d_store_pack
+    for (int i = 0; i < 3; ++i) {
+        const int a = warp_first_min(kmin[i], imin[i]);
+        const int b = warp_first_min(~kmax[i], imax[i]);
+        const double x0 = __shfl_sync(0xffffffffu, v0[i], 0);
+        // the winner's value from the lane that holds it (vertex r sits on lane r % 32); every
+        // value a NaN: vertex 0's, as the scan keeps it
+        const double xa = __shfl_sync(0xffffffffu, vmin[i], a == 0x7fffffff ? 0 : (a & 31));
+        const double xb = __shfl_sync(0xffffffffu, vmax[i], b == 0x7fffffff ? 0 : (b & 31));
+        lo[i] = (x0 != x0 || a == 0x7fffffff) ? x0 : xa;
+        hi[i] = (x0 != x0 || b == 0x7fffffff) ? x0 : xb;
+    }
+}
+
+// containment.py:6-229, one collider per thread; writes [axis][min,max].  The
+// analytic types each on its own thread; the boxes, hulls and meshes of a
+// warp's lanes one after the other by the whole warp (aabb_scan), so that no
+// thread scans up to 256 vertices alone.
+__global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n, double* __restrict__ out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ln = threadIdx.x & 31;
+    const bool valid = k < n;
+    const int ci = valid ? (idx ? idx[k] : (int)k) : 0;
+    const bool ok = valid && index_ok(s, ci);
+    if (valid && !ok)  // out of range: NaN, no record read
+        for (int j = 0; j < 6; ++j) out[6 * k + j] = NAN;
+    Col<double> c;
+    bool poly = false;
+    double lo[3], hi[3];
+    if (ok) {
+        load_col(s, ci, c);
+        poly = c.type == D3D_BOX || c.type == D3D_HULL || c.type == D3D_MESH;
+        if (!poly) analytic_aabb(c, lo, hi);
+        else if (c.nv < 1)  // rejected by d3d_store_pack
             for (int i = 0; i < 3; ++i) lo[i] = hi[i] = NAN;
-            break;
-        }
-        d3 v = load_vertex(s.verts64, c.off);
-        lo[0] = hi[0] = v.x;
-        lo[1] = hi[1] = v.y;
-        lo[2] = hi[2] = v.z;
-        for (int r = 1; r < c.nv; ++r) {
-            v = load_vertex(s.verts64, c.off + r);
-            if (v.x < lo[0]) lo[0] = v.x;
-            if (v.x > hi[0]) hi[0] = v.x;
-            if (v.y < lo[1]) lo[1] = v.y;
-            if (v.y > hi[1]) hi[1] = v.y;
-            if (v.z < lo[2]) lo[2] = v.z;
-            if (v.z > hi[2]) hi[2] = v.z;
-        }
-        break;
     }
+    // the lanes' polytopes and meshes, one at a time across the warp
+    unsigned todo = __ballot_sync(0xffffffffu, ok && poly && c.nv >= 1);
+    while (todo) {
+        const int owner = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int off = __shfl_sync(0xffffffffu, ok ? c.off : 0, owner);
+        const int nv = __shfl_sync(0xffffffffu, ok ? c.nv : 0, owner);
+        const bool mesh = __shfl_sync(0xffffffffu, ok && c.type == D3D_MESH ? 1 : 0, owner) != 0;
+        double R[9], t[3];
+        if (mesh) {
+            for (int j = 0; j < 9; ++j) R[j] = __shfl_sync(0xffffffffu, ok ? c.R[j] : 0.0, owner);
+            for (int j = 0; j < 3; ++j) t[j] = __shfl_sync(0xffffffffu, ok ? c.t[j] : 0.0, owner);
+        }
+        double l[3], h[3];
+        aabb_scan(s, off, nv, mesh, R, t, l, h);
+        if (ln == owner)
+            for (int i = 0; i < 3; ++i) {
+                lo[i] = l[i];
+                hi[i] = h[i];
+            }
     }
+    if (!ok) return;
     if (c.wrapped) {  // colliders.py:639-643
         for (int i = 0; i < 3; ++i) {
             lo[i] = lo[i] - c.m;

@@ -17,6 +17,33 @@ def test_aabbs_match_reference(golden, name):
     assert np.array_equal(ColliderStore(cs).aabbs().cpu().numpy(), g["aabbs"])
 
 
+def test_aabb_scan_ties_and_nans():
+    """The polytope AABB is scanned by a warp with integer keys: its values
+    are those of the sequential scan (oracle), bit for bit: the first of
+    equal values (-0 and +0 in the same axis), a NaN at vertex 0 kept, later
+    NaNs skipped, hulls shorter and longer than a warp."""
+    rng = np.random.default_rng(12)
+    sizes = [1, 2, 5, 31, 32, 33, 64, 65, 200, 256, 40, 40, 40]
+    verts = [rng.normal(size=(k, 3)) for k in sizes]
+    verts[3][:, 0] = np.abs(verts[3][:, 0])
+    verts[3][[0, 7, 30], 0] = [0.0, -0.0, -0.0]  # the minimum of x: +0 first, then -0
+    verts[5][:, 1] = -np.abs(verts[5][:, 1])
+    verts[5][[4, 32], 1] = [-0.0, 0.0]  # the maximum of y: -0 first (lanes 4 and 0)
+    verts[10][0, 2] = np.nan  # NaN at vertex 0: kept
+    verts[11][17, 2] = np.nan  # NaN later: skipped
+    verts[11][3, 0] = np.nan
+    verts[12][:, 0] = 1.5  # every value tied
+    off = np.concatenate([[0], np.cumsum(sizes)[:-1]])
+    n = len(sizes)
+    cs = ColliderSet(np.full(n, HULL), np.tile(np.concatenate([np.eye(3).ravel(), np.zeros(3)]), (n, 1)),
+                     np.zeros((n, 4)), off, sizes, np.concatenate(verts))
+    got = ColliderStore(cs).aabbs().cpu().numpy()
+    want = oracle.aabbs(cs)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+    assert np.isnan(got[10, 2]).all() and not np.isnan(got[11]).any()
+    assert np.signbit(got[3, 0, 0]) == False and np.signbit(got[5, 1, 1]) == True
+
+
 def test_support_matches_oracle():
     cs = workloads.scene_mixed_six(600, seed=9, half_width=1.0)
     st = ColliderStore(cs)

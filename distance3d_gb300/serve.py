@@ -113,6 +113,8 @@ class CollisionBatch:
         n = len(i1)
         if n > self.capacity:
             raise ValueError(f"{n} pairs exceed the capacity {self.capacity}")
+        # the previous batch's copies read and write the same page-locked buffers
+        self.done.synchronize()
         self.n = n
         self.h_i1.numpy()[:n] = i1
         self.h_i2.numpy()[:n] = i2

@@ -343,7 +343,7 @@ __global__ void k_aabbs(d3d_store s, const int32_t* __restrict__ idx, int64_t n,
         const int off = __shfl_sync(0xffffffffu, ok ? c.off : 0, owner);
         const int nv = __shfl_sync(0xffffffffu, ok ? c.nv : 0, owner);
         const bool mesh = __shfl_sync(0xffffffffu, ok && c.type == D3D_MESH ? 1 : 0, owner) != 0;
-        double R[9], t[3];
+        double R[9] = {}, t[3] = {};  // read only for a mesh
         if (mesh) {
             for (int j = 0; j < 9; ++j) R[j] = __shfl_sync(0xffffffffu, ok ? c.R[j] : 0.0, owner);
             for (int j = 0; j < 3; ++j) t[j] = __shfl_sync(0xffffffffu, ok ? c.t[j] : 0.0, owner);

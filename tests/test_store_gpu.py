@@ -41,7 +41,7 @@ def test_aabb_scan_ties_and_nans():
     want = oracle.aabbs(cs)
     assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
     assert np.isnan(got[10, 2]).all() and not np.isnan(got[11]).any()
-    assert np.signbit(got[3, 0, 0]) == False and np.signbit(got[5, 1, 1]) == True
+    assert not np.signbit(got[3, 0, 0]) and np.signbit(got[5, 1, 1])
 
 
 def test_support_matches_oracle():
